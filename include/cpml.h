@@ -1,0 +1,203 @@
+/*
+ * cpml.h -- C ABI of the GB300 staggered-grid velocity-stress elastic solver
+ * with C-PML absorbing layers.
+ *
+ * This header is the drop-in boundary for the two reference programs
+ *   seismic_CPML_2D_isotropic_second_order.f90       (2D P-SV, per-cell lambda/mu/rho)
+ *   seismic_CPML_3D_isotropic_MPI_OpenMP.f90         (3D, homogeneous scalars)
+ * Those programs have no callable API: their "interface" is the compile-time
+ * parameter block (2D:138-218, 3D:124-218) and the output files they write.
+ * Every entry point below names the reference lines whose behaviour it replaces.
+ *
+ * Conventions
+ *   - Grid indices that cross this ABI are 1-based, as in the Fortran.
+ *   - Host arrays are C order [k][j][i] (3D) or [j][i] (2D), i fastest; this
+ *     is the same memory order as the Fortran arrays a(i,j,k), so a Fortran
+ *     caller passes its arrays unchanged.
+ *   - Seismograms are [nrec][nstep] doubles, the memory order of the Fortran
+ *     sisvx(NSTEP,NREC).
+ *   - Every function returns an int status (CPML_OK = 0, negative = error).
+ *     Nothing aborts, exits or throws across this boundary.
+ *   - The library owns device memory, streams and graphs per handle; it keeps
+ *     no pointer to caller memory after a call returns. One handle = one CUDA
+ *     stream; handles are independent; one handle is not thread-safe.
+ */
+#ifndef CPML_H
+#define CPML_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CPML_OK              0
+#define CPML_ERR_INVALID   (-1)  /* bad parameter or argument                  */
+#define CPML_ERR_CFL       (-2)  /* Courant number > 1 (2D:513-516, 3D:712-717) */
+#define CPML_ERR_OOM       (-3)  /* device allocation failed                    */
+#define CPML_ERR_UNSTABLE  (-4)  /* max |v| > 1e25 or NaN (2D:716-726, 3D:1185-1195) */
+#define CPML_ERR_TIMEOUT   (-5)  /* a bounded device-side wait gave up          */
+#define CPML_ERR_CUDA      (-6)  /* a CUDA runtime call failed                  */
+#define CPML_ERR_NOT_READY (-7)  /* results requested before they exist         */
+#define CPML_ERR_IO        (-8)  /* host file output failed                     */
+#define CPML_ERR_RANGE     (-9)  /* size beyond a documented maximum            */
+
+/* ---- source time functions (2D:644-657, 3D:1055-1075) ------------------ */
+#define CPML_STF_DGAUSSIAN 0     /* first derivative of a Gaussian (reference default, 2D:651) */
+#define CPML_STF_GAUSSIAN  1     /* Gaussian (commented alternative, 2D:648)                   */
+#define CPML_STF_RICKER    2     /* Ricker, second derivative (commented alternative, 2D:654)  */
+
+/* ---- flags ------------------------------------------------------------- */
+#define CPML_FLAG_ENERGY        0x1  /* record kinetic/potential energy every step (2D:694-713) */
+#define CPML_FLAG_EP_PHYSICAL   0x2  /* 3D: use the textbook Ep (eps_zz*sigma_zz) instead of the
+                                        reference's duplicated eps_yy*sigma_yy term (3D:1170-1171) */
+#define CPML_FLAG_NO_STABILITY  0x4  /* skip the max|v| blow-up check at IT_DISPLAY cadence      */
+
+/* ---- fields (for cpml_get_field / cpml_get_plane) ---------------------- */
+#define CPML_FIELD_VX  0
+#define CPML_FIELD_VY  1
+#define CPML_FIELD_VZ  2
+#define CPML_FIELD_SXX 3
+#define CPML_FIELD_SYY 4
+#define CPML_FIELD_SZZ 5
+#define CPML_FIELD_SXY 6
+#define CPML_FIELD_SXZ 7
+#define CPML_FIELD_SYZ 8
+
+/*
+ * Runtime copy of the reference's compile-time parameter block.
+ * Field names follow the Fortran constants (2D:138-218, 3D:124-218).
+ */
+typedef struct cpml_params {
+  int32_t ndim;          /* 2 or 3                                             */
+  int32_t nx, ny, nz;    /* NX, NY, NZ (nz ignored in 2D)                      */
+  int32_t nstep;         /* NSTEP: capacity of the seismogram/energy records  */
+  int32_t npoints_pml;   /* NPOINTS_PML                                        */
+  int32_t use_pml[6];    /* USE_PML_XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX (0/1)   */
+  int32_t isource, jsource, ksource;  /* 1-based source grid point           */
+  int32_t stf;           /* CPML_STF_*                                         */
+  int32_t it_display;    /* IT_DISPLAY: cadence of the max|v| stability check */
+  int32_t flags;         /* CPML_FLAG_*                                        */
+  int32_t reserved_i[4];
+  double deltax, deltay, deltaz;  /* DELTAX, DELTAY, DELTAZ (m)               */
+  double deltat;                  /* DELTAT (s)                               */
+  double cp, cs, rho;    /* homogeneous model; cp also sets the PML d0 (2D:296) */
+  double f0, t0, factor; /* source: dominant frequency, delay, amplitude       */
+  double angle_force;    /* ANGLE_FORCE, degrees clockwise from +y (2D:176)   */
+  double npower;         /* NPOWER (2D:213)                                    */
+  double k_max_pml;      /* K_MAX_PML (2D:217)                                 */
+  double alpha_max_pml;  /* ALPHA_MAX_PML (2D:218); <0 selects 2*pi*(f0/2)     */
+  double rcoef;          /* Rcoef (2D:290)                                     */
+  double reserved_d[4];
+} cpml_params;
+
+typedef struct cpml_handle cpml_handle;
+
+/* Fill *p with the reference 2D program's parameter block (2D:138-218). */
+int cpml_params_default_2d(cpml_params* p);
+/* Fill *p with the reference 3D program's parameter block (3D:124-218),
+   single-domain semantics: source and receivers on global plane k = NZ/2. */
+int cpml_params_default_3d(cpml_params* p);
+
+/* Courant number cp*dt*sqrt(sum 1/d^2) (2D:513, 3D:712) for velocity cp_max. */
+double cpml_courant(const cpml_params* p, double cp_max);
+
+/* Nearest grid point to (x, y) metres by the reference's brute-force search:
+   first minimum in i-fastest order wins (2D:486-509, 3D:683-706). 1-based out. */
+int cpml_nearest_gridpoint(int nx, int ny, double deltax, double deltay,
+                           double x, double y, int* i_out, int* j_out);
+
+/* Build the 1-D C-PML profiles of one axis in FP64 on the host
+   (2D:283-394 for x, 2D:396-465 for y, 3D:560-667 for z). Outputs are arrays
+   of length n: d, K, alpha, a, b at grid points and at half points.
+   Exposed so callers and tests can inspect what the device kernels use. */
+int cpml_pml_profile(const cpml_params* p, int axis, int n,
+                     double* d, double* K, double* alpha, double* a, double* b,
+                     double* d_half, double* K_half, double* alpha_half,
+                     double* a_half, double* b_half);
+
+/* Create a solver: validates *p, checks the Courant number for the
+   homogeneous cp (CPML_ERR_CFL, as 2D:516 stops), allocates device state,
+   builds the C-PML tables in FP64 on the GPU and zeroes the wavefields
+   (2D:522-544, 3D:720-756). Replaces the reference's set-up section. */
+int cpml_create(const cpml_params* p, cpml_handle** out);
+
+/* Per-cell model (host arrays, [k][j][i]): lambda, mu (Pa) and rho (kg/m^3),
+   replacing the homogeneous fill of 2D:468-474. Any may be NULL to keep the
+   homogeneous value. Re-checks the Courant number with max cp of the model. */
+int cpml_set_model(cpml_handle* h, const float* lambda, const float* mu,
+                   const float* rho);
+
+/* Receivers as 1-based grid indices (2D:483-509, 3D:683-706 compute them from
+   metres; use cpml_nearest_gridpoint for that). iz may be NULL in 2D and
+   defaults to ksource in 3D (the reference records on the source plane). */
+int cpml_set_receivers(cpml_handle* h, int nrec, const int* ix, const int* iy,
+                       const int* iz);
+
+/* Zero fields, memory variables, seismograms and energy; set it = 0. */
+int cpml_reset(cpml_handle* h);
+
+/* Advance nsteps time steps of the reference time loop (2D:550-735,
+   3D:802-1245): stress + C-PML, velocity + C-PML, source, Dirichlet edges,
+   receivers, energy, and the max|v| check every it_display steps. */
+int cpml_run(cpml_handle* h, int nsteps);
+
+/* Steps done so far and the last max|v| computed (2D:718, 3D:1185). */
+int cpml_status(cpml_handle* h, int* it, double* vmax);
+
+/* Seismograms recorded so far, [nrec][nstep] doubles (sisvx/sisvy,
+   2D:683-686, 3D:1124-1129). vz may be NULL; it is recorded for 3D only. */
+int cpml_get_seismograms(cpml_handle* h, double* vx, double* vy, double* vz);
+
+/* Kinetic and potential energy per step, nstep doubles each (2D:694-713,
+   3D:1131-1180; the 3D reference writes only ek+ep). Either may be NULL. */
+int cpml_get_energy(cpml_handle* h, double* ek, double* ep);
+
+/* Copy one whole field to host FP32, [k][j][i] with nx*ny*nz values. */
+int cpml_get_field(cpml_handle* h, int field, float* out);
+
+/* Copy one plane of a field: axis 0/1/2 = plane of constant i/j/k, index
+   1-based. Output is row-major over the two remaining axes (slowest first).
+   Used for the snapshots of 2D:729-732 and 3D:1236-1239 (k = NZ/2). */
+int cpml_get_plane(cpml_handle* h, int field, int axis, int index, float* out);
+
+/* Upload a whole field from host FP32 (tests and restarts). */
+int cpml_set_field(cpml_handle* h, int field, const float* in);
+
+/* Bytes the hot path moves per time step by its compulsory count: every
+   wavefield read and written once, per-cell model read once, each C-PML
+   memory variable read and written once where its coefficient a is nonzero. */
+double cpml_algorithmic_bytes_per_step(cpml_handle* h);
+
+/* Milliseconds of device time spent inside the stencil kernels by the last
+   cpml_run (CUDA events on the handle's stream). */
+int cpml_last_run_ms(cpml_handle* h, double* ms);
+
+void cpml_destroy(cpml_handle* h);
+const char* cpml_strerror(int status);
+
+/* ---- reference output files (2D:738-808, 820-999; 3D:1247-1364) -------- */
+
+/* Vx_file_NNN.dat / Vy_file_NNN.dat (/ Vz_file_NNN.dat if vz != NULL), one
+   "t v" line per step in Fortran list-directed REAL(4) style (2D:820-854). */
+int cpml_write_seismograms(const char* dir, const double* vx, const double* vy,
+                           const double* vz, int nt, int nrec, double deltat);
+
+/* energy.dat: 2D writes t, Ek, Ep, Ek+Ep (2D:741-746); 3D writes t, Ek+Ep
+   (3D:1253-1257). ncol selects 4 or 2. */
+int cpml_write_energy(const char* dir, const double* ek, const double* ep,
+                      int nt, double deltat, int ncol);
+
+/* imageNNNNNN_Vx.pnm / _Vy.pnm colour snapshot (2D:861-999). data is one
+   [ny][nx] plane; field_number 1 = Vx, 2 = Vy. */
+int cpml_write_pnm(const char* dir, const float* data, int nx, int ny, int it,
+                   int isource, int jsource, const int* ix_rec,
+                   const int* iy_rec, int nrec, int npoints_pml,
+                   const int* use_pml4, int field_number);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPML_H */

@@ -1,0 +1,584 @@
+// cpml_oracle.cpp -- C++ restatement of the two reference programs.
+//
+// TEST INFRASTRUCTURE ONLY. This is the oracle: tests, the smoke check and
+// the CPU-baseline leg of the benchmark use it as a checker and as the timed
+// CPU implementation. The product library never links, calls or falls back
+// to it.
+//
+// It follows, loop nest by loop nest and in the reference's operation order:
+//   seismic_CPML_2D_isotropic_second_order.f90   2D:283-744
+//   seismic_CPML_3D_isotropic_MPI_OpenMP.f90     3D:399-1180
+// with full-grid memory arrays as in the reference (2D:221-230, 3D:228-247)
+// and OpenMP over the outer loop index as in 3D:825. The 3D program is
+// restated for one domain of NZ planes: the union of the MPI slabs, whose
+// one-plane halo exchanges (3D:811-823, 951-963) make the sweep ranges
+// k = 2..NZ (k2begin on rank 0) and k = 1..NZ-1 (kminus1end on the last
+// rank); the source and receivers sit on global plane ksource (NZ/2 in the
+// reference, 3D:1080, 1126).
+//
+// Templated on the arithmetic type: double is the oracle, float measures the
+// FP32 rounding floor. Built with -ffp-contract=off so results do not depend
+// on the host ISA's FMA contraction.
+//
+// Parity against the reference itself is unpinned: the reference is Fortran,
+// no Fortran compiler exists in this environment, and the reference ships no
+// tests or golden vectors. This file is cross-checked against the independent
+// numpy restatement (oracle/oracle_np.py) instead.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/cpml.h"
+
+namespace {
+
+const double PI = 3.141592653589793238462643;
+
+struct Profile {
+  std::vector<double> d, K, alpha, a, b, dh, Kh, alphah, ah, bh;
+};
+
+// 2D:283-394 (x), 2D:396-465 (y), 3D:560-667 (z)
+Profile build_profile(const cpml_params* p, int axis, int n, double delta) {
+  Profile P;
+  P.d.assign(n, 0.0); P.dh.assign(n, 0.0);
+  P.K.assign(n, 1.0); P.Kh.assign(n, 1.0);
+  P.alpha.assign(n, 0.0); P.alphah.assign(n, 0.0);
+  P.a.assign(n, 0.0); P.ah.assign(n, 0.0);
+  P.b.assign(n, 0.0); P.bh.assign(n, 0.0);
+  const bool use_min = p->use_pml[2 * axis] != 0;
+  const bool use_max = p->use_pml[2 * axis + 1] != 0;
+  const double npower = p->npower;
+  const double kmax = p->k_max_pml;
+  const double amax = p->alpha_max_pml < 0 ? 2.0 * PI * (p->f0 / 2.0) : p->alpha_max_pml;
+  const double thickness = p->npoints_pml * delta;
+  const double d0 = -(npower + 1) * p->cp * std::log(p->rcoef) / (2.0 * thickness);
+  const double oleft = thickness;
+  const double oright = (n - 1) * delta - thickness;
+  for (int i = 1; i <= n; ++i) {
+    const double val = delta * double(i - 1);
+    const int ii = i - 1;
+    if (use_min) {
+      double ab = oleft - val;
+      if (ab >= 0.0) {
+        double nr = ab / thickness;
+        P.d[ii] = d0 * std::pow(nr, npower);
+        P.K[ii] = 1.0 + (kmax - 1.0) * std::pow(nr, npower);
+        P.alpha[ii] = amax * (1.0 - nr);
+      }
+      ab = oleft - (val + delta / 2.0);
+      if (ab >= 0.0) {
+        double nr = ab / thickness;
+        P.dh[ii] = d0 * std::pow(nr, npower);
+        P.Kh[ii] = 1.0 + (kmax - 1.0) * std::pow(nr, npower);
+        P.alphah[ii] = amax * (1.0 - nr);
+      }
+    }
+    if (use_max) {
+      double ab = val - oright;
+      if (ab >= 0.0) {
+        double nr = ab / thickness;
+        P.d[ii] = d0 * std::pow(nr, npower);
+        P.K[ii] = 1.0 + (kmax - 1.0) * std::pow(nr, npower);
+        P.alpha[ii] = amax * (1.0 - nr);
+      }
+      ab = val + delta / 2.0 - oright;
+      if (ab >= 0.0) {
+        double nr = ab / thickness;
+        P.dh[ii] = d0 * std::pow(nr, npower);
+        P.Kh[ii] = 1.0 + (kmax - 1.0) * std::pow(nr, npower);
+        P.alphah[ii] = amax * (1.0 - nr);
+      }
+    }
+    if (P.alpha[ii] < 0.0) P.alpha[ii] = 0.0;
+    if (P.alphah[ii] < 0.0) P.alphah[ii] = 0.0;
+    P.b[ii] = std::exp(-(P.d[ii] / P.K[ii] + P.alpha[ii]) * p->deltat);
+    P.bh[ii] = std::exp(-(P.dh[ii] / P.Kh[ii] + P.alphah[ii]) * p->deltat);
+    if (std::fabs(P.d[ii]) > 1e-6)
+      P.a[ii] = P.d[ii] * (P.b[ii] - 1.0) / (P.K[ii] * (P.d[ii] + P.K[ii] * P.alpha[ii]));
+    if (std::fabs(P.dh[ii]) > 1e-6)
+      P.ah[ii] = P.dh[ii] * (P.bh[ii] - 1.0) / (P.Kh[ii] * (P.dh[ii] + P.Kh[ii] * P.alphah[ii]));
+  }
+  return P;
+}
+
+// Source time function at 1-based step it (2D:644-654).
+double source_term(const cpml_params* p, int it) {
+  const double a = PI * PI * p->f0 * p->f0;
+  const double t = double(it - 1) * p->deltat;
+  const double tt = t - p->t0;
+  const double tt2 = tt * tt;
+  if (p->stf == CPML_STF_GAUSSIAN) return p->factor * std::exp(-(a * tt2));
+  if (p->stf == CPML_STF_RICKER) return p->factor * (1.0 - 2.0 * a * tt2) * std::exp(-(a * tt2));
+  return -(p->factor * 2.0 * a * tt * std::exp(-(a * tt2)));
+}
+
+template <typename R>
+struct Prof1 {  // one axis, rounded to the arithmetic type
+  std::vector<R> a, b, K, ah, bh, Kh;
+  explicit Prof1(const Profile& P) {
+    auto cv = [](const std::vector<double>& v) { return std::vector<R>(v.begin(), v.end()); };
+    a = cv(P.a); b = cv(P.b); K = cv(P.K); ah = cv(P.ah); bh = cv(P.bh); Kh = cv(P.Kh);
+  }
+};
+
+struct Out {
+  int nsteps, nrec;
+  const int *ix, *iy, *iz;
+  double *sisvx, *sisvy, *sisvz, *ek, *ep, *vmax;
+};
+
+// ---------------------------------------------------------------------------
+// 2D program, time loop 2D:550-735
+// ---------------------------------------------------------------------------
+template <typename R>
+int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
+          const double* rho_in, const Out& o, double* fields_out) {
+  const int NX = p->nx, NY = p->ny;
+  const size_t N = size_t(NX) * NY;
+  auto at = [NX](int i, int j) { return size_t(j - 1) * NX + (i - 1); };  // 1-based
+  std::vector<R> lam(N), mu(N), rho(N);
+  const double lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);
+  const double mu0 = p->rho * p->cs * p->cs;
+  for (size_t c = 0; c < N; ++c) {                               // 2D:468-474
+    rho[c] = R(rho_in ? rho_in[c] : p->rho);
+    mu[c] = R(mu_in ? mu_in[c] : mu0);
+    lam[c] = R(lam_in ? lam_in[c] : lam0);
+  }
+  Prof1<R> X(build_profile(p, 0, NX, p->deltax));
+  Prof1<R> Y(build_profile(p, 1, NY, p->deltay));
+  const R DX = R(p->deltax), DY = R(p->deltay), DT = R(p->deltat);
+  std::vector<R> vx(N, 0), vy(N, 0), sxx(N, 0), syy(N, 0), sxy(N, 0);
+  std::vector<R> m_dvx_dx(N, 0), m_dvx_dy(N, 0), m_dvy_dx(N, 0), m_dvy_dy(N, 0);
+  std::vector<R> m_dsxx_dx(N, 0), m_dsyy_dy(N, 0), m_dsxy_dx(N, 0), m_dsxy_dy(N, 0);
+  const int npml = p->npoints_pml;
+  const double ang = p->angle_force * (PI / 180.0);
+  const double sa = std::sin(ang), ca = std::cos(ang);
+
+  for (int it = 1; it <= o.nsteps; ++it) {
+    // sigma_xx, sigma_yy (2D:556-580)
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j);
+        R lam_hx = R(0.5) * (lam[at(i + 1, j)] + lam[c]);
+        R mu_hx = R(0.5) * (mu[at(i + 1, j)] + mu[c]);
+        R l2m = lam_hx + R(2.0) * mu_hx;
+        R dvx_dx = (vx[at(i + 1, j)] - vx[c]) / DX;
+        R dvy_dy = (vy[c] - vy[at(i, j - 1)]) / DY;
+        m_dvx_dx[c] = X.bh[i - 1] * m_dvx_dx[c] + X.ah[i - 1] * dvx_dx;
+        m_dvy_dy[c] = Y.b[j - 1] * m_dvy_dy[c] + Y.a[j - 1] * dvy_dy;
+        dvx_dx = dvx_dx / X.Kh[i - 1] + m_dvx_dx[c];
+        dvy_dy = dvy_dy / Y.K[j - 1] + m_dvy_dy[c];
+        sxx[c] = sxx[c] + (l2m * dvx_dx + lam_hx * dvy_dy) * DT;
+        syy[c] = syy[c] + (lam_hx * dvx_dx + l2m * dvy_dy) * DT;
+      }
+    // sigma_xy (2D:582-600)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j);
+        R mu_hy = R(0.5) * (mu[at(i, j + 1)] + mu[c]);
+        R dvy_dx = (vy[c] - vy[at(i - 1, j)]) / DX;
+        R dvx_dy = (vx[at(i, j + 1)] - vx[c]) / DY;
+        m_dvy_dx[c] = X.b[i - 1] * m_dvy_dx[c] + X.a[i - 1] * dvy_dx;
+        m_dvx_dy[c] = Y.bh[j - 1] * m_dvx_dy[c] + Y.ah[j - 1] * dvx_dy;
+        dvy_dx = dvy_dx / X.K[i - 1] + m_dvy_dx[c];
+        dvx_dy = dvx_dy / Y.Kh[j - 1] + m_dvx_dy[c];
+        sxy[c] = sxy[c] + mu_hy * (dvy_dx + dvx_dy) * DT;
+      }
+    // v_x (2D:606-621)
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j);
+        R d1 = (sxx[c] - sxx[at(i - 1, j)]) / DX;
+        R d2 = (sxy[c] - sxy[at(i, j - 1)]) / DY;
+        m_dsxx_dx[c] = X.b[i - 1] * m_dsxx_dx[c] + X.a[i - 1] * d1;
+        m_dsxy_dy[c] = Y.b[j - 1] * m_dsxy_dy[c] + Y.a[j - 1] * d2;
+        d1 = d1 / X.K[i - 1] + m_dsxx_dx[c];
+        d2 = d2 / Y.K[j - 1] + m_dsxy_dy[c];
+        vx[c] = vx[c] + (d1 + d2) * DT / rho[c];
+      }
+    // v_y (2D:623-641)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j);
+        R rhh = R(0.25) * (rho[c] + rho[at(i + 1, j)] + rho[at(i + 1, j + 1)] + rho[at(i, j + 1)]);
+        R d1 = (sxy[at(i + 1, j)] - sxy[c]) / DX;
+        R d2 = (syy[at(i, j + 1)] - syy[c]) / DY;
+        m_dsxy_dx[c] = X.bh[i - 1] * m_dsxy_dx[c] + X.ah[i - 1] * d1;
+        m_dsyy_dy[c] = Y.bh[j - 1] * m_dsyy_dy[c] + Y.ah[j - 1] * d2;
+        d1 = d1 / X.Kh[i - 1] + m_dsxy_dx[c];
+        d2 = d2 / Y.Kh[j - 1] + m_dsyy_dy[c];
+        vy[c] = vy[c] + (d1 + d2) * DT / rhh;
+      }
+    // source (2D:644-667)
+    {
+      const double st = source_term(p, it);
+      const R fx = R(sa * st), fy = R(ca * st);
+      const int i = p->isource, j = p->jsource;
+      R rhh = R(0.25) * (rho[at(i, j)] + rho[at(i + 1, j)] + rho[at(i + 1, j + 1)] + rho[at(i, j + 1)]);
+      vx[at(i, j)] = vx[at(i, j)] + fx * DT / rho[at(i, j)];
+      vy[at(i, j)] = vy[at(i, j)] + fy * DT / rhh;
+    }
+    // Dirichlet (2D:670-680)
+    for (int j = 1; j <= NY; ++j) {
+      vx[at(1, j)] = 0; vx[at(NX, j)] = 0; vy[at(1, j)] = 0; vy[at(NX, j)] = 0;
+    }
+    for (int i = 1; i <= NX; ++i) {
+      vx[at(i, 1)] = 0; vx[at(i, NY)] = 0; vy[at(i, 1)] = 0; vy[at(i, NY)] = 0;
+    }
+    // seismograms (2D:683-686)
+    for (int r = 0; r < o.nrec; ++r) {
+      o.sisvx[size_t(r) * o.nsteps + it - 1] = double(vx[at(o.ix[r], o.iy[r])]);
+      o.sisvy[size_t(r) * o.nsteps + it - 1] = double(vy[at(o.ix[r], o.iy[r])]);
+    }
+    // energy (2D:694-713), in double whatever R is, sequential i-fastest order
+    if (o.ek || o.ep) {
+      double ek = 0.0, ep = 0.0;
+      for (int j = npml + 1; j <= NY - npml; ++j)
+        for (int i = npml + 1; i <= NX - npml; ++i) {
+          const size_t c = at(i, j);
+          const double vxx = vx[c], vyy = vy[c];
+          ek = ek + double(rho[c]) * (vxx * vxx + vyy * vyy);
+          const double l = lam[c], m = mu[c];
+          const double s1 = sxx[c], s2 = syy[c], s3 = sxy[c];
+          const double exx = ((l + 2.0 * m) * s1 - l * s2) / (4.0 * m * (l + m));
+          const double eyy = ((l + 2.0 * m) * s2 - l * s1) / (4.0 * m * (l + m));
+          const double exy = s3 / (2.0 * m);
+          ep = ep + 0.5 * (exx * s1 + eyy * s2 + 2.0 * exy * s3);
+        }
+      if (o.ek) o.ek[it - 1] = 0.5 * ek;
+      if (o.ep) o.ep[it - 1] = ep;
+    }
+    if (o.vmax) {
+      double vm = 0.0;
+      for (size_t c = 0; c < N; ++c)
+        vm = std::max(vm, std::sqrt(double(vx[c]) * vx[c] + double(vy[c]) * vy[c]));
+      o.vmax[it - 1] = vm;
+    }
+  }
+  if (fields_out) {
+    const std::vector<R>* F[5] = {&vx, &vy, &sxx, &syy, &sxy};
+    for (int f = 0; f < 5; ++f)
+      for (size_t c = 0; c < N; ++c) fields_out[f * N + c] = double((*F[f])[c]);
+  }
+  return CPML_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 3D program, time loop 3D:802-1180, one domain of NZ planes
+// ---------------------------------------------------------------------------
+template <typename R>
+int run3d(const cpml_params* p, const double* lam_in, const double* mu_in,
+          const double* rho_in, const Out& o, double* fields_out) {
+  const int NX = p->nx, NY = p->ny, NZ = p->nz;
+  const size_t N = size_t(NX) * NY * NZ;
+  const size_t SX = 1, SY = size_t(NX), SZ = size_t(NX) * NY;
+  auto at = [=](int i, int j, int k) { return size_t(k - 1) * SZ + size_t(j - 1) * SY + (i - 1); };
+  const bool het = lam_in || mu_in || rho_in;
+  const double lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);  // 3D:142-144
+  const double mu0 = p->rho * p->cs * p->cs;
+  const double l2m0 = p->rho * p->cp * p->cp;
+  std::vector<R> lam, mu, rho;
+  if (het) {
+    lam.resize(N); mu.resize(N); rho.resize(N);
+    for (size_t c = 0; c < N; ++c) {
+      lam[c] = R(lam_in ? lam_in[c] : lam0);
+      mu[c] = R(mu_in ? mu_in[c] : mu0);
+      rho[c] = R(rho_in ? rho_in[c] : p->rho);
+    }
+  }
+  Prof1<R> X(build_profile(p, 0, NX, p->deltax));
+  Prof1<R> Y(build_profile(p, 1, NY, p->deltay));
+  Prof1<R> Z(build_profile(p, 2, NZ, p->deltaz));
+  const R DT = R(p->deltat);
+  const R odx = R(1.0 / p->deltax), ody = R(1.0 / p->deltay), odz = R(1.0 / p->deltaz);
+  const R DT_lam0 = R(p->deltat * lam0), DT_mu0 = R(p->deltat * mu0);   // 3D:296-300
+  const R DT_l2m0 = R(p->deltat * l2m0), DT_rho0 = R(p->deltat / p->rho);
+
+  std::vector<R> vx(N, 0), vy(N, 0), vz(N, 0);
+  std::vector<R> sxx(N, 0), syy(N, 0), szz(N, 0), sxy(N, 0), sxz(N, 0), syz(N, 0);
+  std::vector<R> m_dvx_dx(N, 0), m_dvx_dy(N, 0), m_dvx_dz(N, 0), m_dvy_dx(N, 0), m_dvy_dy(N, 0),
+      m_dvy_dz(N, 0), m_dvz_dx(N, 0), m_dvz_dy(N, 0), m_dvz_dz(N, 0), m_dsxx_dx(N, 0),
+      m_dsyy_dy(N, 0), m_dszz_dz(N, 0), m_dsxy_dx(N, 0), m_dsxy_dy(N, 0), m_dsxz_dx(N, 0),
+      m_dsxz_dz(N, 0), m_dsyz_dy(N, 0), m_dsyz_dz(N, 0);
+  const int npml = p->npoints_pml;
+  const double ang = p->angle_force * (PI / 180.0);
+  const double sa = std::sin(ang), ca = std::cos(ang);
+  const bool q1 = !(p->flags & CPML_FLAG_EP_PHYSICAL);
+  std::vector<double> ekk(NZ + 1), epk(NZ + 1);
+
+  for (int it = 1; it <= o.nsteps; ++it) {
+    // normal stresses: k = 2..NZ, j = 2..NY, i = 1..NX-1 (3D:836-863)
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ; ++k)
+      for (int j = 2; j <= NY; ++j)
+        for (int i = 1; i <= NX - 1; ++i) {
+          const size_t c = at(i, j, k);
+          R dvx_dx = (vx[c + SX] - vx[c]) * odx;
+          R dvy_dy = (vy[c] - vy[c - SY]) * ody;
+          R dvz_dz = (vz[c] - vz[c - SZ]) * odz;
+          m_dvx_dx[c] = X.bh[i - 1] * m_dvx_dx[c] + X.ah[i - 1] * dvx_dx;
+          m_dvy_dy[c] = Y.b[j - 1] * m_dvy_dy[c] + Y.a[j - 1] * dvy_dy;
+          m_dvz_dz[c] = Z.b[k - 1] * m_dvz_dz[c] + Z.a[k - 1] * dvz_dz;
+          dvx_dx = dvx_dx / X.Kh[i - 1] + m_dvx_dx[c];
+          dvy_dy = dvy_dy / Y.K[j - 1] + m_dvy_dy[c];
+          dvz_dz = dvz_dz / Z.K[k - 1] + m_dvz_dz[c];
+          R DTl = DT_lam0, DTl2m = DT_l2m0;
+          if (het) {
+            R lhx = R(0.5) * (lam[c + SX] + lam[c]);
+            R mhx = R(0.5) * (mu[c + SX] + mu[c]);
+            DTl = DT * lhx;
+            DTl2m = DT * (lhx + R(2.0) * mhx);
+          }
+          sxx[c] = DTl2m * dvx_dx + DTl * (dvy_dy + dvz_dz) + sxx[c];
+          syy[c] = DTl * (dvx_dx + dvz_dz) + DTl2m * dvy_dy + syy[c];
+          szz[c] = DTl * (dvx_dx + dvy_dy) + DTl2m * dvz_dz + szz[c];
+        }
+    // sigma_xy: k = 1..NZ, j = 1..NY-1, i = 2..NX (3D:877-894)
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ; ++k)
+      for (int j = 1; j <= NY - 1; ++j)
+        for (int i = 2; i <= NX; ++i) {
+          const size_t c = at(i, j, k);
+          R dvy_dx = (vy[c] - vy[c - SX]) * odx;
+          R dvx_dy = (vx[c + SY] - vx[c]) * ody;
+          m_dvy_dx[c] = X.b[i - 1] * m_dvy_dx[c] + X.a[i - 1] * dvy_dx;
+          m_dvx_dy[c] = Y.bh[j - 1] * m_dvx_dy[c] + Y.ah[j - 1] * dvx_dy;
+          dvy_dx = dvy_dx / X.K[i - 1] + m_dvy_dx[c];
+          dvx_dy = dvx_dy / Y.Kh[j - 1] + m_dvx_dy[c];
+          R DTm = het ? DT * (R(0.5) * (mu[c + SY] + mu[c])) : DT_mu0;
+          sxy[c] = DTm * (dvy_dx + dvx_dy) + sxy[c];
+        }
+    // sigma_xz and sigma_yz: k = 1..NZ-1 (3D:908-943)
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 1; ++k) {
+      for (int j = 1; j <= NY; ++j)
+        for (int i = 2; i <= NX; ++i) {
+          const size_t c = at(i, j, k);
+          R dvz_dx = (vz[c] - vz[c - SX]) * odx;
+          R dvx_dz = (vx[c + SZ] - vx[c]) * odz;
+          m_dvz_dx[c] = X.b[i - 1] * m_dvz_dx[c] + X.a[i - 1] * dvz_dx;
+          m_dvx_dz[c] = Z.bh[k - 1] * m_dvx_dz[c] + Z.ah[k - 1] * dvx_dz;
+          dvz_dx = dvz_dx / X.K[i - 1] + m_dvz_dx[c];
+          dvx_dz = dvx_dz / Z.Kh[k - 1] + m_dvx_dz[c];
+          R DTm = het ? DT * (R(0.5) * (mu[c + SZ] + mu[c])) : DT_mu0;
+          sxz[c] = DTm * (dvz_dx + dvx_dz) + sxz[c];
+        }
+      for (int j = 1; j <= NY - 1; ++j)
+        for (int i = 1; i <= NX; ++i) {
+          const size_t c = at(i, j, k);
+          R dvz_dy = (vz[c + SY] - vz[c]) * ody;
+          R dvy_dz = (vy[c + SZ] - vy[c]) * odz;
+          m_dvz_dy[c] = Y.bh[j - 1] * m_dvz_dy[c] + Y.ah[j - 1] * dvz_dy;
+          m_dvy_dz[c] = Z.bh[k - 1] * m_dvy_dz[c] + Z.ah[k - 1] * dvy_dz;
+          dvz_dy = dvz_dy / Y.Kh[j - 1] + m_dvz_dy[c];
+          dvy_dz = dvy_dz / Z.Kh[k - 1] + m_dvy_dz[c];
+          R DTm = DT_mu0;
+          if (het) {
+            // sigma_yz sits at (i+1/2, j+1/2, k+1/2): 8-point average; on the
+            // last column (never read by the velocity sweeps) i+1 is clamped.
+            const size_t di = (i < NX) ? SX : 0;
+            const R s = ((((((mu[c] + mu[c + di]) + mu[c + SY]) + mu[c + SY + di]) + mu[c + SZ]) +
+                          mu[c + SZ + di]) + mu[c + SZ + SY]) + mu[c + SZ + SY + di];
+            DTm = DT * (R(0.125) * s);
+          }
+          syz[c] = DTm * (dvz_dy + dvy_dz) + syz[c];
+        }
+    }
+    // v_x and v_y: k = 2..NZ (3D:976-1017)
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ; ++k) {
+      for (int j = 2; j <= NY; ++j)
+        for (int i = 2; i <= NX; ++i) {
+          const size_t c = at(i, j, k);
+          R d1 = (sxx[c] - sxx[c - SX]) * odx;
+          R d2 = (sxy[c] - sxy[c - SY]) * ody;
+          R d3 = (sxz[c] - sxz[c - SZ]) * odz;
+          m_dsxx_dx[c] = X.b[i - 1] * m_dsxx_dx[c] + X.a[i - 1] * d1;
+          m_dsxy_dy[c] = Y.b[j - 1] * m_dsxy_dy[c] + Y.a[j - 1] * d2;
+          m_dsxz_dz[c] = Z.b[k - 1] * m_dsxz_dz[c] + Z.a[k - 1] * d3;
+          d1 = d1 / X.K[i - 1] + m_dsxx_dx[c];
+          d2 = d2 / Y.K[j - 1] + m_dsxy_dy[c];
+          d3 = d3 / Z.K[k - 1] + m_dsxz_dz[c];
+          R f = het ? DT / rho[c] : DT_rho0;
+          vx[c] = f * (d1 + d2 + d3) + vx[c];
+        }
+      for (int j = 1; j <= NY - 1; ++j)
+        for (int i = 1; i <= NX - 1; ++i) {
+          const size_t c = at(i, j, k);
+          R d1 = (sxy[c + SX] - sxy[c]) * odx;
+          R d2 = (syy[c + SY] - syy[c]) * ody;
+          R d3 = (syz[c] - syz[c - SZ]) * odz;
+          m_dsxy_dx[c] = X.bh[i - 1] * m_dsxy_dx[c] + X.ah[i - 1] * d1;
+          m_dsyy_dy[c] = Y.bh[j - 1] * m_dsyy_dy[c] + Y.ah[j - 1] * d2;
+          m_dsyz_dz[c] = Z.b[k - 1] * m_dsyz_dz[c] + Z.a[k - 1] * d3;
+          d1 = d1 / X.Kh[i - 1] + m_dsxy_dx[c];
+          d2 = d2 / Y.Kh[j - 1] + m_dsyy_dy[c];
+          d3 = d3 / Z.K[k - 1] + m_dsyz_dz[c];
+          R f = DT_rho0;
+          if (het) f = DT / (R(0.25) * (rho[c] + rho[c + SX] + rho[c + SX + SY] + rho[c + SY]));
+          vy[c] = f * (d1 + d2 + d3) + vy[c];
+        }
+    }
+    // v_z: k = 1..NZ-1, j = 2..NY, i = 1..NX-1 (3D:1031-1052)
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 1; ++k)
+      for (int j = 2; j <= NY; ++j)
+        for (int i = 1; i <= NX - 1; ++i) {
+          const size_t c = at(i, j, k);
+          R d1 = (sxz[c + SX] - sxz[c]) * odx;
+          R d2 = (syz[c] - syz[c - SY]) * ody;
+          R d3 = (szz[c + SZ] - szz[c]) * odz;
+          m_dsxz_dx[c] = X.bh[i - 1] * m_dsxz_dx[c] + X.ah[i - 1] * d1;
+          m_dsyz_dy[c] = Y.b[j - 1] * m_dsyz_dy[c] + Y.a[j - 1] * d2;
+          m_dszz_dz[c] = Z.bh[k - 1] * m_dszz_dz[c] + Z.ah[k - 1] * d3;
+          d1 = d1 / X.Kh[i - 1] + m_dsxz_dx[c];
+          d2 = d2 / Y.K[j - 1] + m_dsyz_dy[c];
+          d3 = d3 / Z.Kh[k - 1] + m_dszz_dz[c];
+          R f = DT_rho0;
+          if (het) f = DT / (R(0.25) * (rho[c] + rho[c + SX] + rho[c + SX + SZ] + rho[c + SZ]));
+          vz[c] = f * (d1 + d2 + d3) + vz[c];
+        }
+    // source on plane ksource, plain rho (3D:1055-1083)
+    {
+      const double st = source_term(p, it);
+      const double fx = sa * st, fy = ca * st;
+      const size_t c = at(p->isource, p->jsource, p->ksource);
+      if (het) {
+        vx[c] = vx[c] + R(fx) * DT / rho[c];
+        vy[c] = vy[c] + R(fy) * DT / rho[c];
+      } else {
+        vx[c] = vx[c] + R(fx * p->deltat / p->rho);
+        vy[c] = vy[c] + R(fy * p->deltat / p->rho);
+      }
+    }
+    // Dirichlet on the six faces (3D:1087-1121)
+    std::vector<R>* V[3] = {&vx, &vy, &vz};
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ; ++k)
+      for (int f = 0; f < 3; ++f) {
+        std::vector<R>& a = *V[f];
+        for (int j = 1; j <= NY; ++j) { a[at(1, j, k)] = 0; a[at(NX, j, k)] = 0; }
+        for (int i = 1; i <= NX; ++i) { a[at(i, 1, k)] = 0; a[at(i, NY, k)] = 0; }
+        if (k == 1 || k == NZ)
+          for (int j = 1; j <= NY; ++j)
+            for (int i = 1; i <= NX; ++i) a[at(i, j, k)] = 0;
+      }
+    // seismograms (3D:1124-1129)
+    for (int r = 0; r < o.nrec; ++r) {
+      const size_t c = at(o.ix[r], o.iy[r], o.iz[r]);
+      o.sisvx[size_t(r) * o.nsteps + it - 1] = double(vx[c]);
+      o.sisvy[size_t(r) * o.nsteps + it - 1] = double(vy[c]);
+      if (o.sisvz) o.sisvz[size_t(r) * o.nsteps + it - 1] = double(vz[c]);
+    }
+    // energy (3D:1131-1180): per-plane partials, summed in k order
+    if (o.ek || o.ep) {
+#pragma omp parallel for schedule(static)
+      for (int k = npml + 1; k <= NZ - npml; ++k) {
+        double ek = 0.0, ep = 0.0;
+        for (int j = npml + 1; j <= NY - npml; ++j)
+          for (int i = npml + 1; i <= NX - npml; ++i) {
+            const size_t c = at(i, j, k);
+            const double r = het ? double(rho[c]) : p->rho;
+            const double l = het ? double(lam[c]) : lam0;
+            const double m = het ? double(mu[c]) : mu0;
+            const double a = vx[c], b = vy[c], cc = vz[c];
+            ek = ek + 0.5 * r * (a * a + b * b + cc * cc);
+            const double s1 = sxx[c], s2 = syy[c], s3 = szz[c];
+            const double s4 = sxy[c], s5 = sxz[c], s6 = syz[c];
+            const double den = 2.0 * m * (3.0 * l + 2.0 * m);
+            const double exx = (2.0 * (l + m) * s1 - l * s2 - l * s3) / den;
+            const double eyy = (2.0 * (l + m) * s2 - l * s1 - l * s3) / den;
+            const double ezz = (2.0 * (l + m) * s3 - l * s1 - l * s2) / den;
+            const double exy = s4 / (2.0 * m), exz = s5 / (2.0 * m), eyz = s6 / (2.0 * m);
+            const double third = q1 ? eyy * s2 : ezz * s3;
+            ep = ep + 0.5 * (exx * s1 + eyy * s2 + third + 2.0 * exy * s4 + 2.0 * exz * s5 +
+                             2.0 * eyz * s6);
+          }
+        ekk[k] = ek; epk[k] = ep;
+      }
+      double ek = 0.0, ep = 0.0;
+      for (int k = npml + 1; k <= NZ - npml; ++k) { ek += ekk[k]; ep += epk[k]; }
+      if (o.ek) o.ek[it - 1] = ek;
+      if (o.ep) o.ep[it - 1] = ep;
+    }
+    if (o.vmax) {
+      double vm = 0.0;
+#pragma omp parallel for reduction(max : vm) schedule(static)
+      for (long long c = 0; c < (long long)N; ++c)
+        vm = std::max(vm, std::sqrt(double(vx[c]) * vx[c] + double(vy[c]) * vy[c] +
+                                    double(vz[c]) * vz[c]));
+      o.vmax[it - 1] = vm;
+    }
+  }
+  if (fields_out) {
+    const std::vector<R>* F[9] = {&vx, &vy, &vz, &sxx, &syy, &szz, &sxy, &sxz, &syz};
+    for (int f = 0; f < 9; ++f)
+      for (size_t c = 0; c < N; ++c) fields_out[f * N + c] = double((*F[f])[c]);
+  }
+  return CPML_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Run the restated program for nsteps steps.
+//   use_double: 1 = FP64 oracle, 0 = FP32 floor study.
+//   lam/mu/rho: per-cell model (NULL = homogeneous), [k][j][i] doubles.
+//   receivers: 1-based (ix, iy, iz); iz ignored in 2D.
+//   sisv*: [nrec][nsteps]; ek/ep/vmax: [nsteps]; any output may be NULL.
+//   fields_out: 5 (2D) or 9 (3D) fields x ncell doubles, in the order
+//   vx vy (vz) sxx syy (szz) sxy (sxz syz); may be NULL.
+//   nthreads <= 0 keeps the OpenMP default.
+int oracle_run(const cpml_params* p, int nsteps, int use_double, const double* lam,
+               const double* mu, const double* rho, int nrec, const int* ix, const int* iy,
+               const int* iz, double* sisvx, double* sisvy, double* sisvz, double* ek,
+               double* ep, double* vmax, double* fields_out, int nthreads) {
+  if (!p || nsteps < 0 || (p->ndim != 2 && p->ndim != 3)) return CPML_ERR_INVALID;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  std::vector<double> sx, sy;
+  if (nrec > 0 && !sisvx) { sx.resize(size_t(nrec) * nsteps); sisvx = sx.data(); }
+  if (nrec > 0 && !sisvy) { sy.resize(size_t(nrec) * nsteps); sisvy = sy.data(); }
+  Out o{nsteps, nrec, ix, iy, iz, sisvx, sisvy, sisvz, ek, ep, vmax};
+  if (p->ndim == 2)
+    return use_double ? run2d<double>(p, lam, mu, rho, o, fields_out)
+                      : run2d<float>(p, lam, mu, rho, o, fields_out);
+  return use_double ? run3d<double>(p, lam, mu, rho, o, fields_out)
+                    : run3d<float>(p, lam, mu, rho, o, fields_out);
+}
+
+// The FP64 profiles of one axis (for tests).
+int oracle_profile(const cpml_params* p, int axis, int n, double delta, double* out10) {
+  Profile P = build_profile(p, axis, n, delta);
+  const std::vector<double>* v[10] = {&P.d, &P.K, &P.alpha, &P.a, &P.b,
+                                      &P.dh, &P.Kh, &P.alphah, &P.ah, &P.bh};
+  for (int q = 0; q < 10; ++q) std::memcpy(out10 + size_t(q) * n, v[q]->data(), sizeof(double) * n);
+  return CPML_OK;
+}
+
+double oracle_source_term(const cpml_params* p, int it) { return source_term(p, it); }
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"
