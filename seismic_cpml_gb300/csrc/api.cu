@@ -1,0 +1,613 @@
+// api.cu -- the libcpml runtime behind include/cpml.h.
+//
+// A handle owns one CUDA stream and all device state of one simulation. The
+// time loop of the reference (2D:550-735, 3D:802-1245) runs as chunks of
+// steps; each chunk is one CUDA graph (its step kernels, then the chunk
+// reduction) replayed from a per-length cache. Kernels read the step counter
+// from device memory, so one graph serves every chunk of the same length.
+// Chunks end on the reference's display steps (it = 5 and multiples of
+// IT_DISPLAY, 2D:716), where the host checks max|v| against the 1e25 blow-up
+// threshold, exactly where the reference checks it.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+#include <algorithm>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cpml.h"
+#include "cpml_internal.cuh"
+
+namespace cpml {
+struct ProfileArgs {
+  int n, npml, use_min, use_max;
+  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
+};
+void launch_build_profile(const ProfileArgs& P, double* out64, float* out32, cudaStream_t st);
+void launch_reduce_chunk(const StepArgs& s, int C, double* ek, double* ep, double* vmax, int* bad,
+                         cudaStream_t st);
+void launch_step3d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
+void launch_step2d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
+int blocks3d(const StepArgs& s);
+int blocks2d(const StepArgs& s);
+}  // namespace cpml
+
+using namespace cpml;
+
+namespace {
+const double kPi = 3.141592653589793238462643;
+const double kStability = 1.0e25;  // STABILITY_THRESHOLD (2D:201)
+const int kMaxChunk = 128;
+
+double source_term(const cpml_params* p, int it) {  // 2D:644-654
+  const double a = kPi * kPi * p->f0 * p->f0;
+  const double tt = double(it - 1) * p->deltat - p->t0;
+  const double tt2 = tt * tt;
+  if (p->stf == CPML_STF_GAUSSIAN) return p->factor * std::exp(-(a * tt2));
+  if (p->stf == CPML_STF_RICKER) return p->factor * (1.0 - 2.0 * a * tt2) * std::exp(-(a * tt2));
+  return -(p->factor * 2.0 * a * tt * std::exp(-(a * tt2)));
+}
+}  // namespace
+
+struct cpml_handle {
+  cpml_params p{};
+  int ndim = 0, nx = 0, ny = 0, nz = 1, px = 0;
+  long long plane = 0;
+  size_t ncellp = 0;  // padded cells
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  float* fld[9] = {};
+  float* prof32[3] = {};
+  double* prof64[3] = {};
+  Axis axes[3] = {};
+  float* model[3] = {};  // lam, mu, rho (per-cell, optional)
+  bool het = false;
+  double cp_max = 0;
+  double rho_src[2] = {0, 0};  // rho used for the x / y source increments
+  float* src_fx = nullptr;
+  float* src_fy = nullptr;
+  int nrec = 0;
+  std::vector<int> rec_ijk;    // 1-based triples
+  int* rec_cell = nullptr;
+  float* seis = nullptr;
+  double* partials = nullptr;
+  int nblocks = 0;
+  double *ek = nullptr, *ep = nullptr, *vmax = nullptr;
+  int* bad = nullptr;
+  int* it_base = nullptr;
+  int it = 0;
+  double last_vmax = 0;
+  std::map<int, cudaGraphExec_t> graphs;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  Slabs slabs{};
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return CPML_OK;
+  if (e == cudaErrorMemoryAllocation) return CPML_ERR_OOM;
+  return CPML_ERR_CUDA;
+}
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+template <typename T>
+int dalloc(cpml_handle* h, T** out, size_t count) {
+  *out = nullptr;
+  if (count == 0) return CPML_OK;
+  void* ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+  if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+  h->allocs.push_back(ptr);
+  *out = (T*)ptr;
+  return CPML_OK;
+}
+
+void drop_graphs(cpml_handle* h) {
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+}
+
+int validate(const cpml_params* p) {
+  if (!p) return CPML_ERR_INVALID;
+  if (p->ndim != 2 && p->ndim != 3) return CPML_ERR_INVALID;
+  const int nz = p->ndim == 3 ? p->nz : 1;
+  if (p->nx < 3 || p->ny < 3 || (p->ndim == 3 && p->nz < 3)) return CPML_ERR_INVALID;
+  if (p->nstep < 1 || p->npoints_pml < 1) return CPML_ERR_INVALID;
+  if (!(p->deltax > 0) || !(p->deltay > 0) || (p->ndim == 3 && !(p->deltaz > 0)) ||
+      !(p->deltat > 0))
+    return CPML_ERR_INVALID;
+  if (!(p->cp > 0) || !(p->cs > 0) || !(p->rho > 0) || !(p->rcoef > 0 && p->rcoef < 1))
+    return CPML_ERR_INVALID;
+  if (p->npower < 1) return CPML_ERR_INVALID;  // 2D:293
+  if (p->isource < 1 || p->isource > p->nx - 1 || p->jsource < 1 || p->jsource > p->ny - 1)
+    return CPML_ERR_INVALID;
+  if (p->ndim == 3 && (p->ksource < 1 || p->ksource > nz)) return CPML_ERR_INVALID;
+  if (p->it_display < 1) return CPML_ERR_INVALID;
+  const double cells = double(p->nx) * p->ny * nz;
+  if (cells > 4.0e9) return CPML_ERR_RANGE;
+  return CPML_OK;
+}
+
+StepArgs make_args(cpml_handle* h) {
+  StepArgs s{};
+  const cpml_params& p = h->p;
+  s.nx = h->nx; s.ny = h->ny; s.nz = h->nz; s.px = h->px; s.plane = h->plane;
+  s.odx = float(1.0 / p.deltax); s.ody = float(1.0 / p.deltay);
+  s.odz = float(1.0 / (h->ndim == 3 ? p.deltaz : 1.0));
+  s.dx = float(p.deltax); s.dy = float(p.deltay);
+  s.dt = float(p.deltat);
+  const double lam = p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs);
+  const double mu = p.rho * p.cs * p.cs;
+  const double l2m = h->ndim == 3 ? p.rho * p.cp * p.cp : lam + 2.0 * mu;  // 3D:144 / 2D:562
+  s.dt_lam = float(p.deltat * lam);
+  s.dt_mu = float(p.deltat * mu);
+  s.dt_l2m = float(p.deltat * l2m);
+  s.dt_over_rho = float(p.deltat / p.rho);
+  s.half_rho = float(0.5 * p.rho);
+  s.inv_2mu = float(1.0 / (2.0 * mu));
+  if (h->ndim == 3) {
+    const double den = 2.0 * mu * (3.0 * lam + 2.0 * mu);  // 3D:1160-1165
+    s.e_c1 = float(2.0 * (lam + mu) / den);
+    s.e_c2 = float(lam / den);
+  } else {
+    const double den = 4.0 * mu * (lam + mu);              // 2D:704-707
+    s.e_c1 = float((lam + 2.0 * mu) / den);
+    s.e_c2 = float(lam / den);
+  }
+  s.ax = h->axes[0]; s.ay = h->axes[1]; s.az = h->axes[2];
+  s.m = h->slabs;
+  s.f.vx = h->fld[0]; s.f.vy = h->fld[1]; s.f.vz = h->fld[2];
+  s.f.sxx = h->fld[3]; s.f.syy = h->fld[4]; s.f.szz = h->fld[5];
+  s.f.sxy = h->fld[6]; s.f.sxz = h->fld[7]; s.f.syz = h->fld[8];
+  s.mdl.lam = h->model[0]; s.mdl.mu = h->model[1]; s.mdl.rho = h->model[2];
+  s.npml = p.npoints_pml;
+  s.isrc = p.isource - 1; s.jsrc = p.jsource - 1; s.ksrc = h->ndim == 3 ? p.ksource - 1 : 0;
+  s.src_fx = h->src_fx; s.src_fy = h->src_fy;
+  s.nrec = h->nrec; s.rec_cell = h->rec_cell; s.seis = h->seis;
+  s.nstep = p.nstep;
+  s.it_base = h->it_base;
+  s.partials = h->partials;
+  s.nblocks = h->nblocks;
+  s.ep_physical = (p.flags & CPML_FLAG_EP_PHYSICAL) ? 1 : 0;
+  return s;
+}
+
+// Per-step source increments: force * DELTAT / rho (2D:664-667, 3D:1080-1081)
+int upload_source(cpml_handle* h) {
+  const cpml_params& p = h->p;
+  const double ang = p.angle_force * (kPi / 180.0);
+  const double sa = std::sin(ang), ca = std::cos(ang);
+  std::vector<float> fx(p.nstep), fy(p.nstep);
+  for (int it = 1; it <= p.nstep; ++it) {
+    const double st = source_term(&p, it);
+    fx[it - 1] = float(sa * st * p.deltat / h->rho_src[0]);
+    fy[it - 1] = float(ca * st * p.deltat / h->rho_src[1]);
+  }
+  CK(cudaMemcpyAsync(h->src_fx, fx.data(), sizeof(float) * p.nstep, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->src_fy, fy.data(), sizeof(float) * p.nstep, cudaMemcpyHostToDevice, h->stream));
+  return cudaStreamSynchronize(h->stream) == cudaSuccess ? CPML_OK : CPML_ERR_CUDA;
+}
+
+int build_axis(cpml_handle* h, int axis, int n, double delta) {
+  const cpml_params& p = h->p;
+  ProfileArgs P{};
+  P.n = n; P.npml = p.npoints_pml;
+  P.use_min = p.use_pml[2 * axis]; P.use_max = p.use_pml[2 * axis + 1];
+  P.delta = delta; P.cp = p.cp; P.f0 = p.f0; P.dt = p.deltat; P.npower = p.npower;
+  P.kmax = p.k_max_pml; P.amax = p.alpha_max_pml < 0 ? 2.0 * kPi * (p.f0 / 2.0) : p.alpha_max_pml;
+  P.rcoef = p.rcoef;
+  int st;
+  if ((st = dalloc(h, &h->prof64[axis], size_t(10) * n))) return st;
+  if ((st = dalloc(h, &h->prof32[axis], size_t(6) * n))) return st;
+  launch_build_profile(P, h->prof64[axis], h->prof32[axis], h->stream);
+  CK(cudaGetLastError());
+  std::vector<double> hp(size_t(10) * n);
+  CK(cudaMemcpyAsync(hp.data(), h->prof64[axis], sizeof(double) * hp.size(), cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  // slab extents: every index whose a or a_half is nonzero must be inside
+  auto nzero = [&](int i) { return hp[3 * size_t(n) + i] != 0.0 || hp[8 * size_t(n) + i] != 0.0; };
+  int lo = 0, hi = 0;
+  for (int i = 0; i < n / 2; ++i) if (nzero(i)) lo = i + 1;
+  for (int i = n - 1; i >= n / 2; --i) if (nzero(i)) hi = n - i;
+  for (int i = lo; i < n - hi; ++i)
+    if (nzero(i)) { lo = n; hi = 0; break; }
+  Axis& A = h->axes[axis];
+  const float* f = h->prof32[axis];
+  A.a = f; A.b = f + n; A.ik = f + 2 * n; A.ah = f + 3 * n; A.bh = f + 4 * n; A.ikh = f + 5 * n;
+  A.n = n; A.lo = lo; A.hi = hi;
+  return CPML_OK;
+}
+
+int alloc_slabs(cpml_handle* h) {
+  const size_t nx = h->nx, ny = h->ny, nz = h->nz, px = h->px;
+  const int nvar = h->ndim == 3 ? 6 : 4;
+  const size_t wx = h->axes[0].width(), wy = h->axes[1].width();
+  const size_t wz = h->ndim == 3 ? h->axes[2].width() : 0;
+  (void)nx;
+  for (int v = 0; v < nvar; ++v) {
+    int st;
+    if ((st = dalloc(h, &h->slabs.x[v], nz * ny * wx))) return st;
+    if ((st = dalloc(h, &h->slabs.y[v], nz * wy * px))) return st;
+    if (h->ndim == 3 && (st = dalloc(h, &h->slabs.z[v], wz * ny * px))) return st;
+  }
+  return CPML_OK;
+}
+
+size_t slab_floats(const cpml_handle* h, int axis) {
+  const size_t ny = h->ny, nz = h->nz, px = h->px;
+  if (axis == 0) return nz * ny * h->axes[0].width();
+  if (axis == 1) return nz * h->axes[1].width() * px;
+  return h->axes[2].width() * ny * px;
+}
+
+int zero_state(cpml_handle* h) {
+  const int nf = h->ndim == 3 ? 9 : 5;
+  const int map2d[5] = {0, 1, 3, 4, 6};
+  for (int q = 0; q < nf; ++q) {
+    const int f = h->ndim == 3 ? q : map2d[q];
+    CK(cudaMemsetAsync(h->fld[f], 0, sizeof(float) * h->ncellp, h->stream));
+  }
+  const int nvar = h->ndim == 3 ? 6 : 4;
+  for (int v = 0; v < nvar; ++v) {
+    if (h->slabs.x[v]) CK(cudaMemsetAsync(h->slabs.x[v], 0, sizeof(float) * slab_floats(h, 0), h->stream));
+    if (h->slabs.y[v]) CK(cudaMemsetAsync(h->slabs.y[v], 0, sizeof(float) * slab_floats(h, 1), h->stream));
+    if (h->slabs.z[v]) CK(cudaMemsetAsync(h->slabs.z[v], 0, sizeof(float) * slab_floats(h, 2), h->stream));
+  }
+  const size_t ns = h->p.nstep;
+  if (h->seis) CK(cudaMemsetAsync(h->seis, 0, sizeof(float) * 3 * size_t(std::max(h->nrec, 1)) * ns, h->stream));
+  CK(cudaMemsetAsync(h->ek, 0, sizeof(double) * ns, h->stream));
+  CK(cudaMemsetAsync(h->ep, 0, sizeof(double) * ns, h->stream));
+  CK(cudaMemsetAsync(h->vmax, 0, sizeof(double) * ns, h->stream));
+  CK(cudaMemsetAsync(h->bad, 0, sizeof(int) * ns, h->stream));
+  CK(cudaMemsetAsync(h->it_base, 0, sizeof(int), h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->it = 0;
+  h->last_vmax = 0;
+  return CPML_OK;
+}
+
+void launch_step(cpml_handle* h, const StepArgs& s, int ls) {
+  if (h->ndim == 3) launch_step3d_two_sweep(s, ls, h->het, h->stream);
+  else launch_step2d_two_sweep(s, ls, h->het, h->stream);
+}
+
+int get_graph(cpml_handle* h, int C, cudaGraphExec_t* out) {
+  auto it = h->graphs.find(C);
+  if (it != h->graphs.end()) { *out = it->second; return CPML_OK; }
+  const StepArgs s = make_args(h);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int ls = 0; ls < C; ++ls) launch_step(h, s, ls);
+  launch_reduce_chunk(s, C, h->ek, h->ep, h->vmax, h->bad, h->stream);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) { cudaGetLastError(); return CPML_ERR_CUDA; }
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { cudaGetLastError(); return CPML_ERR_CUDA; }
+  h->graphs[C] = ex;
+  *out = ex;
+  return CPML_OK;
+}
+
+size_t padded_index(const cpml_handle* h, int i1, int j1, int k1) {
+  return size_t(k1 - 1) * h->plane + size_t(j1 - 1) * h->px + size_t(i1 - 1);
+}
+
+int upload_receivers(cpml_handle* h) {
+  std::vector<int> cells(std::max(h->nrec, 1), 0);
+  for (int r = 0; r < h->nrec; ++r)
+    cells[r] = (int)padded_index(h, h->rec_ijk[3 * r], h->rec_ijk[3 * r + 1], h->rec_ijk[3 * r + 2]);
+  CK(cudaMemcpyAsync(h->rec_cell, cells.data(), sizeof(int) * cells.size(), cudaMemcpyHostToDevice,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpml_create(const cpml_params* pin, cpml_handle** out) {
+  if (!out) return CPML_ERR_INVALID;
+  *out = nullptr;
+  int st = validate(pin);
+  if (st) return st;
+  if (cpml_courant(pin, pin->cp) > 1.0) return CPML_ERR_CFL;  // 2D:516, 3D:717
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) { cudaGetLastError(); return CPML_ERR_CUDA; }
+  cpml_handle* h = new cpml_handle();
+  h->p = *pin;
+  h->ndim = pin->ndim;
+  h->nx = pin->nx; h->ny = pin->ny; h->nz = pin->ndim == 3 ? pin->nz : 1;
+  if (h->ndim == 2) h->p.nz = 1;
+  h->px = (h->nx + 31) / 32 * 32;
+  h->plane = (long long)h->px * h->ny;
+  h->ncellp = size_t(h->plane) * h->nz;
+  h->cp_max = pin->cp;
+  h->rho_src[0] = h->rho_src[1] = pin->rho;
+  auto fail = [&](int code) { cpml_destroy(h); return code; };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CPML_ERR_CUDA);
+  if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) return fail(CPML_ERR_CUDA);
+  const int used3[9] = {1, 1, 1, 1, 1, 1, 1, 1, 1};
+  const int used2[9] = {1, 1, 0, 1, 1, 0, 1, 0, 0};
+  for (int f = 0; f < 9; ++f)
+    if ((h->ndim == 3 ? used3 : used2)[f] && (st = dalloc(h, &h->fld[f], h->ncellp))) return fail(st);
+  if ((st = build_axis(h, 0, h->nx, pin->deltax))) return fail(st);
+  if ((st = build_axis(h, 1, h->ny, pin->deltay))) return fail(st);
+  if (h->ndim == 3) {
+    if ((st = build_axis(h, 2, h->nz, pin->deltaz))) return fail(st);
+  } else {
+    h->axes[2] = Axis{};
+    h->axes[2].n = 1;
+  }
+  if ((st = alloc_slabs(h))) return fail(st);
+  if ((st = dalloc(h, &h->src_fx, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->src_fy, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->ek, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->ep, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->vmax, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->bad, pin->nstep))) return fail(st);
+  if ((st = dalloc(h, &h->it_base, 1))) return fail(st);
+  {
+    StepArgs s = make_args(h);
+    h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
+  }
+  if ((st = dalloc(h, &h->partials, size_t(kMaxChunk) * h->nblocks * 4))) return fail(st);
+  // default receivers: none; seismogram buffer sized for one dummy receiver
+  h->nrec = 0;
+  if ((st = dalloc(h, &h->rec_cell, 1))) return fail(st);
+  if ((st = dalloc(h, &h->seis, size_t(3) * pin->nstep))) return fail(st);
+  if ((st = upload_source(h))) return fail(st);
+  if ((st = zero_state(h))) return fail(st);
+  *out = h;
+  return CPML_OK;
+}
+
+int cpml_set_model(cpml_handle* h, const float* lam, const float* mu, const float* rho) {
+  if (!h) return CPML_ERR_INVALID;
+  if (!lam && !mu && !rho) return CPML_OK;
+  const cpml_params& p = h->p;
+  const size_t n = size_t(h->nx) * h->ny * h->nz;
+  const float def[3] = {float(p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs)), float(p.rho * p.cs * p.cs),
+                        float(p.rho)};
+  const float* src[3] = {lam, mu, rho};
+  // Courant number with the model's largest P velocity
+  double cpm = 0.0;
+  for (size_t c = 0; c < n; ++c) {
+    const double l = lam ? lam[c] : def[0], m = mu ? mu[c] : def[1], r = rho ? rho[c] : def[2];
+    if (!(r > 0) || !(m > 0) || !(l + 2 * m > 0)) return CPML_ERR_INVALID;
+    cpm = std::max(cpm, std::sqrt((l + 2.0 * m) / r));
+  }
+  if (cpml_courant(&p, cpm) > 1.0) return CPML_ERR_CFL;
+  int st;
+  std::vector<float> tmp;
+  for (int q = 0; q < 3; ++q) {
+    if (!h->model[q] && (st = dalloc(h, &h->model[q], h->ncellp))) return st;
+    const float* s = src[q];
+    if (!s) { tmp.assign(n, def[q]); s = tmp.data(); }
+    CK(cudaMemset2DAsync(h->model[q], sizeof(float) * h->px, 0, sizeof(float) * h->px,
+                         size_t(h->ny) * h->nz, h->stream));
+    CK(cudaMemcpy2DAsync(h->model[q], sizeof(float) * h->px, s, sizeof(float) * h->nx,
+                         sizeof(float) * h->nx, size_t(h->ny) * h->nz, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  h->het = true;
+  h->cp_max = cpm;
+  // rho at the source (2D:661-667 uses rho(i,j) and the 4-point average for
+  // v_y; 3D:1080-1081 uses rho for both)
+  auto R = [&](int i1, int j1, int k1) {
+    const size_t c = size_t(k1 - 1) * h->nx * h->ny + size_t(j1 - 1) * h->nx + (i1 - 1);
+    return rho ? double(rho[c]) : double(def[2]);
+  };
+  const int i = p.isource, j = p.jsource, k = h->ndim == 3 ? p.ksource : 1;
+  h->rho_src[0] = R(i, j, k);
+  h->rho_src[1] = h->ndim == 2 ? 0.25 * (R(i, j, 1) + R(i + 1, j, 1) + R(i + 1, j + 1, 1) + R(i, j + 1, 1))
+                               : R(i, j, k);
+  drop_graphs(h);
+  return upload_source(h);
+}
+
+int cpml_set_receivers(cpml_handle* h, int nrec, const int* ix, const int* iy, const int* iz) {
+  if (!h || nrec < 0 || (nrec > 0 && (!ix || !iy))) return CPML_ERR_INVALID;
+  std::vector<int> ijk(size_t(3) * nrec);
+  for (int r = 0; r < nrec; ++r) {
+    const int k = h->ndim == 3 ? (iz ? iz[r] : h->p.ksource) : 1;
+    if (ix[r] < 1 || ix[r] > h->nx || iy[r] < 1 || iy[r] > h->ny || k < 1 || k > h->nz)
+      return CPML_ERR_INVALID;
+    ijk[3 * r] = ix[r]; ijk[3 * r + 1] = iy[r]; ijk[3 * r + 2] = k;
+  }
+  if (h->it != 0) return CPML_ERR_INVALID;  // set receivers before running (or after reset)
+  int st;
+  if (nrec > std::max(h->nrec, 1)) {
+    if ((st = dalloc(h, &h->rec_cell, size_t(nrec)))) return st;
+    if ((st = dalloc(h, &h->seis, size_t(3) * nrec * h->p.nstep))) return st;
+  }
+  h->nrec = nrec;
+  h->rec_ijk = ijk;
+  drop_graphs(h);
+  if ((st = upload_receivers(h))) return st;
+  CK(cudaMemsetAsync(h->seis, 0, sizeof(float) * 3 * size_t(std::max(nrec, 1)) * h->p.nstep, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+int cpml_reset(cpml_handle* h) {
+  if (!h) return CPML_ERR_INVALID;
+  return zero_state(h);
+}
+
+int cpml_run(cpml_handle* h, int nsteps) {
+  if (!h || nsteps < 0) return CPML_ERR_INVALID;
+  if (h->it + nsteps > h->p.nstep) return CPML_ERR_RANGE;
+  const bool check = !(h->p.flags & CPML_FLAG_NO_STABILITY);
+  const int d = h->p.it_display;
+  int st;
+  int done = 0;
+  CK(cudaEventRecord(h->ev0, h->stream));
+  while (done < nsteps) {
+    int end = h->it + (nsteps - done);
+    if (check) {
+      int nd = (h->it / d + 1) * d;
+      if (h->it < 5) nd = std::min(nd, 5);
+      end = std::min(end, nd);
+    }
+    end = std::min(end, h->it + kMaxChunk);
+    const int C = end - h->it;
+    cudaGraphExec_t g;
+    if ((st = get_graph(h, C, &g))) return st;
+    CK(cudaGraphLaunch(g, h->stream));
+    done += C;
+    const int it_end = end;
+    h->it = end;
+    if (check && (it_end % d == 0 || it_end == 5)) {
+      double vm = 0;
+      CK(cudaMemcpyAsync(&vm, h->vmax + (it_end - 1), sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      std::vector<int> bad(C);
+      CK(cudaMemcpyAsync(bad.data(), h->bad + (it_end - C), sizeof(int) * C, cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      h->last_vmax = vm;
+      bool nonfinite = false;
+      for (int b : bad) nonfinite |= b != 0;
+      if (vm > kStability || nonfinite || !(vm == vm)) {  // 2D:724, 3D:1193
+        cudaEventRecord(h->ev1, h->stream);
+        cudaEventSynchronize(h->ev1);
+        return CPML_ERR_UNSTABLE;
+      }
+    }
+  }
+  CK(cudaEventRecord(h->ev1, h->stream));
+  CK(cudaEventSynchronize(h->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->last_ms = ms;
+  CK(cudaGetLastError());
+  return CPML_OK;
+}
+
+int cpml_status(cpml_handle* h, int* it, double* vmax) {
+  if (!h) return CPML_ERR_INVALID;
+  if (it) *it = h->it;
+  if (vmax) *vmax = h->last_vmax;
+  return CPML_OK;
+}
+
+int cpml_get_seismograms(cpml_handle* h, double* vx, double* vy, double* vz) {
+  if (!h) return CPML_ERR_INVALID;
+  const size_t ns = h->p.nstep, nr = h->nrec;
+  if (nr == 0) return CPML_OK;
+  std::vector<float> buf(3 * nr * ns);
+  CK(cudaMemcpyAsync(buf.data(), h->seis, sizeof(float) * buf.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  double* out[3] = {vx, vy, h->ndim == 3 ? vz : nullptr};
+  for (int c = 0; c < 3; ++c) {
+    if (!out[c]) continue;
+    for (size_t r = 0; r < nr; ++r)
+      for (size_t t = 0; t < ns; ++t)
+        out[c][r * ns + t] = t < size_t(h->it) ? double(buf[c * nr * ns + r * ns + t]) : 0.0;
+  }
+  return CPML_OK;
+}
+
+int cpml_get_energy(cpml_handle* h, double* ek, double* ep) {
+  if (!h) return CPML_ERR_INVALID;
+  const size_t ns = h->p.nstep;
+  if (ek) CK(cudaMemcpyAsync(ek, h->ek, sizeof(double) * ns, cudaMemcpyDeviceToHost, h->stream));
+  if (ep) CK(cudaMemcpyAsync(ep, h->ep, sizeof(double) * ns, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+static float* field_ptr(cpml_handle* h, int field) {
+  if (field < 0 || field > 8) return nullptr;
+  return h->fld[field];
+}
+
+int cpml_get_field(cpml_handle* h, int field, float* out) {
+  if (!h || !out) return CPML_ERR_INVALID;
+  float* f = field_ptr(h, field);
+  if (!f) return CPML_ERR_INVALID;
+  CK(cudaMemcpy2DAsync(out, sizeof(float) * h->nx, f, sizeof(float) * h->px, sizeof(float) * h->nx,
+                       size_t(h->ny) * h->nz, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+int cpml_set_field(cpml_handle* h, int field, const float* in) {
+  if (!h || !in) return CPML_ERR_INVALID;
+  float* f = field_ptr(h, field);
+  if (!f) return CPML_ERR_INVALID;
+  CK(cudaMemcpy2DAsync(f, sizeof(float) * h->px, in, sizeof(float) * h->nx, sizeof(float) * h->nx,
+                       size_t(h->ny) * h->nz, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+int cpml_get_plane(cpml_handle* h, int field, int axis, int index, float* out) {
+  if (!h || !out || axis < 0 || axis > 2) return CPML_ERR_INVALID;
+  float* f = field_ptr(h, field);
+  if (!f) return CPML_ERR_INVALID;
+  const int n[3] = {h->nx, h->ny, h->nz};
+  if (index < 1 || index > n[axis]) return CPML_ERR_INVALID;
+  const size_t fs = sizeof(float);
+  if (axis == 2) {         // [j][i]
+    CK(cudaMemcpy2DAsync(out, fs * h->nx, f + size_t(index - 1) * h->plane, fs * h->px, fs * h->nx,
+                         h->ny, cudaMemcpyDeviceToHost, h->stream));
+  } else if (axis == 1) {  // [k][i]
+    CK(cudaMemcpy2DAsync(out, fs * h->nx, f + size_t(index - 1) * h->px, fs * h->plane, fs * h->nx,
+                         h->nz, cudaMemcpyDeviceToHost, h->stream));
+  } else {                 // [k][j]
+    CK(cudaMemcpy2DAsync(out, fs, f + (index - 1), fs * h->px, fs, size_t(h->ny) * h->nz,
+                         cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+double cpml_algorithmic_bytes_per_step(cpml_handle* h) {
+  if (!h) return 0.0;
+  const double ncell = double(h->nx) * h->ny * h->nz;
+  const int nfield = h->ndim == 3 ? 9 : 5;
+  double bytes = 8.0 * nfield * ncell + (h->het ? 12.0 * ncell : 0.0);
+  const int nax = h->ndim;
+  const int per = h->ndim == 3 ? 3 : 2;  // memory variables per (axis, full|half)
+  for (int a = 0; a < nax; ++a) {
+    const int n = h->axes[a].n;
+    std::vector<double> hp(size_t(10) * n);
+    if (cudaMemcpy(hp.data(), h->prof64[a], sizeof(double) * hp.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return 0.0;
+    double nf = 0, nh = 0;
+    for (int i = 0; i < n; ++i) { nf += hp[3 * size_t(n) + i] != 0.0; nh += hp[8 * size_t(n) + i] != 0.0; }
+    const double other = ncell / n;
+    bytes += 8.0 * per * (nf + nh) * other;
+  }
+  return bytes;
+}
+
+int cpml_last_run_ms(cpml_handle* h, double* ms) {
+  if (!h || !ms) return CPML_ERR_INVALID;
+  *ms = h->last_ms;
+  return CPML_OK;
+}
+
+void cpml_destroy(cpml_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// kutil.cuh -- small device helpers shared by the stencil kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "cpml_internal.cuh"
+
+namespace cpml {
+
+// C-PML memory-variable recursion and derivative correction
+// (2D:574-578 and every sweep of 3D:836-1052):
+//   psi <- b*psi + a*d ;  d' = d/K + psi
+// Outside the slab (sidx < 0) a = 0, psi = 0 and K = 1, so d' = d.
+__device__ __forceinline__ float pml(float d, int sidx, float* __restrict__ mem, long long midx,
+                                     const float* __restrict__ a, const float* __restrict__ b,
+                                     const float* __restrict__ ik, int idx) {
+  if (sidx < 0) return d;
+  const float m = __ldg(b + idx) * mem[midx] + __ldg(a + idx) * d;
+  mem[midx] = m;
+  return d * __ldg(ik + idx) + m;
+}
+
+// Compensated (Kahan) FP32 accumulator: per-thread energy partials stay at
+// FP64-like accuracy without FP64 arithmetic per cell (FP64 throughput on
+// this part is a small fraction of FP32).
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_or(int v) {
+  return __any_sync(0xffffffffu, v) ? 1 : 0;
+}
+
+// Deterministic block reduction of (ek, ep, vmax^2, bad) to thread 0, written
+// to out[0..3]. Fixed tree order => bitwise reproducible.
+template <int NT>
+__device__ __forceinline__ void block_partials(double ek, double ep, float vm2, int bad,
+                                               double* __restrict__ out) {
+  constexpr int NW = NT / 32;
+  __shared__ double s_ek[NW], s_ep[NW];
+  __shared__ float s_vm[NW];
+  __shared__ int s_bad[NW];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x + threadIdx.z * blockDim.x * blockDim.y;
+  const int lane = tid & 31, w = tid >> 5;
+  ek = warp_sum(ek);
+  ep = warp_sum(ep);
+  vm2 = warp_max(vm2);
+  bad = warp_or(bad);
+  if (lane == 0) { s_ek[w] = ek; s_ep[w] = ep; s_vm[w] = vm2; s_bad[w] = bad; }
+  __syncthreads();
+  if (w == 0) {
+    ek = lane < NW ? s_ek[lane] : 0.0;
+    ep = lane < NW ? s_ep[lane] : 0.0;
+    vm2 = lane < NW ? s_vm[lane] : 0.f;
+    bad = lane < NW ? s_bad[lane] : 0;
+    ek = warp_sum(ek);
+    ep = warp_sum(ep);
+    vm2 = warp_max(vm2);
+    bad = warp_or(bad);
+    if (lane == 0) { out[0] = ek; out[1] = ep; out[2] = (double)vm2; out[3] = (double)bad; }
+  }
+}
+
+// v^2 check that also catches NaN / Inf (the reference's maxval would skip
+// NaN; flagging it is an extension).
+__device__ __forceinline__ int not_finite(float v2) { return !(v2 <= 3.0e38f); }
+
+}  // namespace cpml

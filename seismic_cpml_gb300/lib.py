@@ -1,0 +1,90 @@
+"""ctypes binding of libcpml.so (include/cpml.h).
+
+Loads the in-tree library built by ``seismic_cpml_gb300.build``. There is no
+fallback: if the library is missing the import of the solver fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .params import CpmlParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcpml.so")
+
+OK = 0
+ERR = {-1: "INVALID", -2: "CFL", -3: "OOM", -4: "UNSTABLE", -5: "TIMEOUT", -6: "CUDA",
+       -7: "NOT_READY", -8: "IO", -9: "RANGE"}
+
+# (name, restype, argtypes) for every entry point declared in include/cpml.h
+_P = ctypes.POINTER
+_dp, _fp, _ip, _vp = _P(ctypes.c_double), _P(ctypes.c_float), _P(ctypes.c_int), ctypes.c_void_p
+_h = ctypes.c_void_p
+SIGNATURES = [
+    ("cpml_params_default_2d", ctypes.c_int, [_P(CpmlParams)]),
+    ("cpml_params_default_3d", ctypes.c_int, [_P(CpmlParams)]),
+    ("cpml_courant", ctypes.c_double, [_P(CpmlParams), ctypes.c_double]),
+    ("cpml_nearest_gridpoint", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                              _ip, _ip]),
+    ("cpml_pml_profile", ctypes.c_int, [_P(CpmlParams), ctypes.c_int, ctypes.c_int] + [_dp] * 10),
+    ("cpml_create", ctypes.c_int, [_P(CpmlParams), _P(_h)]),
+    ("cpml_set_model", ctypes.c_int, [_h, _fp, _fp, _fp]),
+    ("cpml_set_receivers", ctypes.c_int, [_h, ctypes.c_int, _ip, _ip, _ip]),
+    ("cpml_reset", ctypes.c_int, [_h]),
+    ("cpml_run", ctypes.c_int, [_h, ctypes.c_int]),
+    ("cpml_status", ctypes.c_int, [_h, _ip, _dp]),
+    ("cpml_get_seismograms", ctypes.c_int, [_h, _dp, _dp, _dp]),
+    ("cpml_get_energy", ctypes.c_int, [_h, _dp, _dp]),
+    ("cpml_get_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
+    ("cpml_get_plane", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp]),
+    ("cpml_set_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
+    ("cpml_algorithmic_bytes_per_step", ctypes.c_double, [_h]),
+    ("cpml_last_run_ms", ctypes.c_int, [_h, _dp]),
+    ("cpml_destroy", None, [_h]),
+    ("cpml_strerror", ctypes.c_char_p, [ctypes.c_int]),
+    ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_double]),
+    ("cpml_write_energy", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_int]),
+    ("cpml_write_pnm", ctypes.c_int, [ctypes.c_char_p, _fp, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip,
+                                      ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int]),
+]
+
+_lib = None
+
+
+class CpmlError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        name = ERR.get(status, str(status))
+        msg = strerror(status) if _lib is not None else name
+        super().__init__(f"{what}: CPML_ERR_{name} ({msg})" if what else f"CPML_ERR_{name} ({msg})")
+
+
+def load(path: str | None = None):
+    """Load libcpml.so and declare every entry point's signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(f"libcpml.so not built ({path}); run seismic_cpml_gb300.build.build()")
+    L = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def strerror(status: int) -> str:
+    return load().cpml_strerror(status).decode()
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        raise CpmlError(status, what)
