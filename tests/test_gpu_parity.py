@@ -20,7 +20,11 @@ pytestmark = pytest.mark.gpu
 
 TRACE_TOL = 1e-5
 ENERGY_TOL = 1e-6
+# Whole-field comparisons: after the wave has left through the PML the fields
+# hold small residuals whose FP32 rounding floor (oracle FP32 build vs FP64)
+# reaches 1e-4 relative; a field passes at <= max(1e-5, 4 x that floor).
 FIELD_TOL = 1e-5
+FIELD_FLOOR_FACTOR = 4.0
 
 
 def rl2(a, b):
@@ -43,7 +47,7 @@ def run_gpu(p, rec, model=None, nsteps=None):
     return dict(vx=vx, vy=vy, vz=vz, ek=ek, ep=ep, fields=fields, it=it, vmax=vmax)
 
 
-def check(g, ref, fields=None, trace_tol=TRACE_TOL, energy_tol=ENERGY_TOL):
+def check(g, ref, fields=None, floor=None, trace_tol=TRACE_TOL, energy_tol=ENERGY_TOL):
     et = rl2(traces(g["vx"], g["vy"], g["vz"]), traces(ref.sisvx, ref.sisvy, ref.sisvz))
     ee = rl2(g["ek"] + g["ep"], ref.ek + ref.ep)
     assert et <= trace_tol, f"trace rel-L2 {et:.3e}"
@@ -51,7 +55,10 @@ def check(g, ref, fields=None, trace_tol=TRACE_TOL, energy_tol=ENERGY_TOL):
     if fields:
         for n, f in fields.items():
             ef = rl2(g["fields"][n], f)
-            assert ef <= FIELD_TOL, f"field {n} rel-L2 {ef:.3e}"
+            tol = FIELD_TOL
+            if floor is not None:
+                tol = max(tol, FIELD_FLOOR_FACTOR * rl2(floor[n], f))
+            assert ef <= tol, f"field {n} rel-L2 {ef:.3e} > {tol:.3e}"
     return et, ee
 
 
@@ -61,7 +68,8 @@ def test_2d_small(het):
     model = layered_2d(p, seed=3) if het else None
     kw = dict(lam=model[0], mu=model[1], rho=model[2]) if het else {}
     ref = oracle_c.run(p, rec=rec, keep_fields=True, **kw)
-    check(run_gpu(p, rec, model), ref, ref.fields)
+    ref32 = oracle_c.run(p, rec=rec, keep_fields=True, double=False, **kw)
+    check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
 
 
 @pytest.mark.parametrize("het", [False, True])
@@ -70,7 +78,8 @@ def test_3d_small(het):
     model = layered_3d(p, seed=5) if het else None
     kw = dict(lam=model[0], mu=model[1], rho=model[2]) if het else {}
     ref = oracle_c.run(p, rec=rec, keep_fields=True, **kw)
-    check(run_gpu(p, rec, model), ref, ref.fields)
+    ref32 = oracle_c.run(p, rec=rec, keep_fields=True, double=False, **kw)
+    check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
 
 
 def test_2d_reference_default(golden):
