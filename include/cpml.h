@@ -55,6 +55,11 @@ extern "C" {
                                         reference's duplicated eps_yy*sigma_yy term (3D:1170-1171) */
 #define CPML_FLAG_NO_STABILITY  0x4  /* skip the max|v| blow-up check at IT_DISPLAY cadence      */
 
+/* ---- step kernels (cpml_set_tuning) ----------------------------------- */
+#define CPML_KERNEL_AUTO      0  /* fused one-sweep kernel in 3D, two-sweep in 2D     */
+#define CPML_KERNEL_TWO_SWEEP 1  /* stress kernel + velocity kernel, in place         */
+#define CPML_KERNEL_FUSED     2  /* 3D only: one kernel per step, two buffer sets, TMA */
+
 /* ---- fields (for cpml_get_field / cpml_get_plane) ---------------------- */
 #define CPML_FIELD_VX  0
 #define CPML_FIELD_VY  1
@@ -174,6 +179,13 @@ double cpml_algorithmic_bytes_per_step(cpml_handle* h);
 /* Milliseconds of device time spent inside the stencil kernels by the last
    cpml_run (CUDA events on the handle's stream). */
 int cpml_last_run_ms(cpml_handle* h, double* ms);
+
+/* Select the step kernel and its launch shape: tile_y (8 or 16 rows of the
+   32-wide tile) and zchunk (planes per CTA in the z sweep). Only on a fresh
+   or reset handle. No reference counterpart: the reference's loop nests
+   (3D:825-1052) have no tunables; this is what the autotuner drives. */
+int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk);
+int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk);
 
 void cpml_destroy(cpml_handle* h);
 const char* cpml_strerror(int status);

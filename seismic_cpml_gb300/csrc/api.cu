@@ -32,6 +32,12 @@ void launch_step3d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t s
 void launch_step2d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
 int blocks3d(const StepArgs& s);
 int blocks2d(const StepArgs& s);
+bool fused3d_supported();
+size_t fused3d_plan_bytes();
+bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* lam, const float* mu,
+                       const float* rho, int nx, int ny, int nz, int px, int ty, int lz, bool het);
+dim3 fused3d_grid(int nx, int ny, int nz, int ty, int lz);
+cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st);
 }  // namespace cpml
 
 using namespace cpml;
@@ -58,7 +64,13 @@ struct cpml_handle {
   size_t ncellp = 0;  // padded cells
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
-  float* fld[9] = {};
+  float* fld[9] = {};      // buffer set 0
+  float* fld1[9] = {};     // buffer set 1 (fused 3D path: time n+1 while set 0 holds n)
+  bool pingpong = false;   // fields alternate between the sets every step
+  int kernel = 0;          // CPML_KERNEL_*
+  int tile_y = 16, zchunk = 32;
+  std::vector<unsigned char> plan;  // fused-path tensor maps
+  int* err = nullptr;      // device error word
   float* prof32[3] = {};
   double* prof64[3] = {};
   Axis axes[3] = {};
@@ -83,6 +95,8 @@ struct cpml_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   Slabs slabs{};
+  Slabs slabs1{};          // stress-side memory variables of buffer set 1
+  size_t partials_cap = 0;
 };
 
 namespace {
@@ -136,7 +150,8 @@ int validate(const cpml_params* p) {
   return CPML_OK;
 }
 
-StepArgs make_args(cpml_handle* h) {
+// Arguments of a step that reads buffer set `q` (and, ping-ponged, writes 1-q).
+StepArgs make_args(cpml_handle* h, int q = 0) {
   StepArgs s{};
   const cpml_params& p = h->p;
   s.nx = h->nx; s.ny = h->ny; s.nz = h->nz; s.px = h->px; s.plane = h->plane;
@@ -163,10 +178,25 @@ StepArgs make_args(cpml_handle* h) {
     s.e_c2 = float(lam / den);
   }
   s.ax = h->axes[0]; s.ay = h->axes[1]; s.az = h->axes[2];
+  float* const* F = (q == 0 || !h->pingpong) ? h->fld : h->fld1;
+  float* const* Gd = (!h->pingpong) ? F : (q == 0 ? h->fld1 : h->fld);
+  s.f.vx = F[0]; s.f.vy = F[1]; s.f.vz = F[2];
+  s.f.sxx = F[3]; s.f.syy = F[4]; s.f.szz = F[5];
+  s.f.sxy = F[6]; s.f.sxz = F[7]; s.f.syz = F[8];
+  s.g.vx = Gd[0]; s.g.vy = Gd[1]; s.g.vz = Gd[2];
+  s.g.sxx = Gd[3]; s.g.syy = Gd[4]; s.g.szz = Gd[5];
+  s.g.sxy = Gd[6]; s.g.sxz = Gd[7]; s.g.syz = Gd[8];
   s.m = h->slabs;
-  s.f.vx = h->fld[0]; s.f.vy = h->fld[1]; s.f.vz = h->fld[2];
-  s.f.sxx = h->fld[3]; s.f.syy = h->fld[4]; s.f.szz = h->fld[5];
-  s.f.sxy = h->fld[6]; s.f.sxz = h->fld[7]; s.f.syz = h->fld[8];
+  s.mb = h->slabs;
+  if (h->pingpong) {  // stress-side memory variables (indices 0..2) alternate too
+    const Slabs& A = q == 0 ? h->slabs : h->slabs1;
+    const Slabs& B = q == 0 ? h->slabs1 : h->slabs;
+    for (int v = 0; v < 3; ++v) {
+      s.m.x[v] = A.x[v]; s.m.y[v] = A.y[v]; s.m.z[v] = A.z[v];
+      s.mb.x[v] = B.x[v]; s.mb.y[v] = B.y[v]; s.mb.z[v] = B.z[v];
+    }
+  }
+  s.err = h->err;
   s.mdl.lam = h->model[0]; s.mdl.mu = h->model[1]; s.mdl.rho = h->model[2];
   s.npml = p.npoints_pml;
   s.isrc = p.isource - 1; s.jsrc = p.jsource - 1; s.ksrc = h->ndim == 3 ? p.ksource - 1 : 0;
@@ -239,6 +269,13 @@ int alloc_slabs(cpml_handle* h) {
     if ((st = dalloc(h, &h->slabs.y[v], nz * wy * px))) return st;
     if (h->ndim == 3 && (st = dalloc(h, &h->slabs.z[v], wz * ny * px))) return st;
   }
+  if (h->ndim == 3)
+    for (int v = 0; v < 3; ++v) {
+      int st;
+      if ((st = dalloc(h, &h->slabs1.x[v], nz * ny * wx))) return st;
+      if ((st = dalloc(h, &h->slabs1.y[v], nz * wy * px))) return st;
+      if ((st = dalloc(h, &h->slabs1.z[v], wz * ny * px))) return st;
+    }
   return CPML_OK;
 }
 
@@ -255,13 +292,16 @@ int zero_state(cpml_handle* h) {
   for (int q = 0; q < nf; ++q) {
     const int f = h->ndim == 3 ? q : map2d[q];
     CK(cudaMemsetAsync(h->fld[f], 0, sizeof(float) * h->ncellp, h->stream));
+    if (h->fld1[f]) CK(cudaMemsetAsync(h->fld1[f], 0, sizeof(float) * h->ncellp, h->stream));
   }
   const int nvar = h->ndim == 3 ? 6 : 4;
-  for (int v = 0; v < nvar; ++v) {
-    if (h->slabs.x[v]) CK(cudaMemsetAsync(h->slabs.x[v], 0, sizeof(float) * slab_floats(h, 0), h->stream));
-    if (h->slabs.y[v]) CK(cudaMemsetAsync(h->slabs.y[v], 0, sizeof(float) * slab_floats(h, 1), h->stream));
-    if (h->slabs.z[v]) CK(cudaMemsetAsync(h->slabs.z[v], 0, sizeof(float) * slab_floats(h, 2), h->stream));
-  }
+  for (const Slabs* S : {&h->slabs, &h->slabs1})
+    for (int v = 0; v < nvar; ++v) {
+      if (S->x[v]) CK(cudaMemsetAsync(S->x[v], 0, sizeof(float) * slab_floats(h, 0), h->stream));
+      if (S->y[v]) CK(cudaMemsetAsync(S->y[v], 0, sizeof(float) * slab_floats(h, 1), h->stream));
+      if (S->z[v]) CK(cudaMemsetAsync(S->z[v], 0, sizeof(float) * slab_floats(h, 2), h->stream));
+    }
+  CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
   const size_t ns = h->p.nstep;
   if (h->seis) CK(cudaMemsetAsync(h->seis, 0, sizeof(float) * 3 * size_t(std::max(h->nrec, 1)) * ns, h->stream));
   CK(cudaMemsetAsync(h->ek, 0, sizeof(double) * ns, h->stream));
@@ -275,18 +315,27 @@ int zero_state(cpml_handle* h) {
   return CPML_OK;
 }
 
-void launch_step(cpml_handle* h, const StepArgs& s, int ls) {
-  if (h->ndim == 3) launch_step3d_two_sweep(s, ls, h->het, h->stream);
-  else launch_step2d_two_sweep(s, ls, h->het, h->stream);
+// One time step that reads buffer set q.
+void launch_step(cpml_handle* h, int q, int ls) {
+  const StepArgs s = make_args(h, q);
+  if (h->ndim == 3) {
+    if (h->pingpong) fused3d_launch(h->plan.data(), s, ls, q, h->stream);
+    else launch_step3d_two_sweep(s, ls, h->het, h->stream);
+  } else {
+    launch_step2d_two_sweep(s, ls, h->het, h->stream);
+  }
 }
 
+// Graph of one chunk of C steps starting from buffer set q0; cached by (C, q0).
 int get_graph(cpml_handle* h, int C, cudaGraphExec_t* out) {
-  auto it = h->graphs.find(C);
+  const int q0 = h->pingpong ? (h->it & 1) : 0;
+  const int key = 2 * C + q0;
+  auto it = h->graphs.find(key);
   if (it != h->graphs.end()) { *out = it->second; return CPML_OK; }
-  const StepArgs s = make_args(h);
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int ls = 0; ls < C; ++ls) launch_step(h, s, ls);
+  for (int ls = 0; ls < C; ++ls) launch_step(h, h->pingpong ? ((q0 + ls) & 1) : 0, ls);
+  const StepArgs s = make_args(h, h->pingpong ? ((q0 + C) & 1) : 0);  // set holding the chunk's result
   launch_reduce_chunk(s, C, h->ek, h->ep, h->vmax, h->bad, h->stream);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) { cudaGetLastError(); return CPML_ERR_CUDA; }
@@ -294,7 +343,7 @@ int get_graph(cpml_handle* h, int C, cudaGraphExec_t* out) {
   e = cudaGraphInstantiate(&ex, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) { cudaGetLastError(); return CPML_ERR_CUDA; }
-  h->graphs[C] = ex;
+  h->graphs[key] = ex;
   *out = ex;
   return CPML_OK;
 }
@@ -312,6 +361,41 @@ int upload_receivers(cpml_handle* h) {
   CK(cudaStreamSynchronize(h->stream));
   return CPML_OK;
 }
+
+// Choose the step kernel and (re)build what it needs: the fused one-sweep 3D
+// kernel ping-pongs two buffer sets and reads them through TMA tensor maps;
+// the two-sweep kernels update one set in place.
+int configure_path(cpml_handle* h) {
+  const bool fused = h->ndim == 3 && h->kernel != CPML_KERNEL_TWO_SWEEP && fused3d_supported();
+  if (h->ndim == 3 && h->kernel == CPML_KERNEL_FUSED && !fused) return CPML_ERR_CUDA;
+  int st;
+  if (fused) {
+    for (int f = 0; f < 9; ++f)
+      if (!h->fld1[f] && (st = dalloc(h, &h->fld1[f], h->ncellp))) return st;
+    h->plan.assign(fused3d_plan_bytes(), 0);
+    float* sets[2][9];
+    for (int f = 0; f < 9; ++f) { sets[0][f] = h->fld[f]; sets[1][f] = h->fld1[f]; }
+    if (!fused3d_make_maps(h->plan.data(), sets, h->model[0], h->model[1], h->model[2], h->nx, h->ny, h->nz,
+                           h->px, h->tile_y, h->zchunk, h->het))
+      return CPML_ERR_CUDA;
+    const dim3 g = fused3d_grid(h->nx, h->ny, h->nz, h->tile_y, h->zchunk);
+    h->nblocks = int(g.x * g.y);
+  } else {
+    StepArgs s = make_args(h);
+    h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
+  }
+  h->pingpong = fused;
+  const size_t need = size_t(kMaxChunk) * h->nblocks * 4;
+  if (need > h->partials_cap) {
+    if ((st = dalloc(h, &h->partials, need))) return st;
+    h->partials_cap = need;
+  }
+  drop_graphs(h);
+  return CPML_OK;
+}
+
+// Buffer set that holds the current time level.
+float* const* cur_fields(cpml_handle* h) { return (h->pingpong && (h->it & 1)) ? h->fld1 : h->fld; }
 
 }  // namespace
 
@@ -358,11 +442,8 @@ int cpml_create(const cpml_params* pin, cpml_handle** out) {
   if ((st = dalloc(h, &h->vmax, pin->nstep))) return fail(st);
   if ((st = dalloc(h, &h->bad, pin->nstep))) return fail(st);
   if ((st = dalloc(h, &h->it_base, 1))) return fail(st);
-  {
-    StepArgs s = make_args(h);
-    h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
-  }
-  if ((st = dalloc(h, &h->partials, size_t(kMaxChunk) * h->nblocks * 4))) return fail(st);
+  if ((st = dalloc(h, &h->err, 1))) return fail(st);
+  if ((st = configure_path(h))) return fail(st);
   // default receivers: none; seismogram buffer sized for one dummy receiver
   h->nrec = 0;
   if ((st = dalloc(h, &h->rec_cell, 1))) return fail(st);
@@ -403,6 +484,7 @@ int cpml_set_model(cpml_handle* h, const float* lam, const float* mu, const floa
   }
   h->het = true;
   h->cp_max = cpm;
+  if ((st = configure_path(h))) return st;
   // rho at the source (2D:661-667 uses rho(i,j) and the 4-point average for
   // v_y; 3D:1080-1081 uses rho for both)
   auto R = [&](int i1, int j1, int k1) {
@@ -487,6 +569,9 @@ int cpml_run(cpml_handle* h, int nsteps) {
   }
   CK(cudaEventRecord(h->ev1, h->stream));
   CK(cudaEventSynchronize(h->ev1));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return CPML_ERR_TIMEOUT;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_ms = ms;
@@ -529,7 +614,7 @@ int cpml_get_energy(cpml_handle* h, double* ek, double* ep) {
 
 static float* field_ptr(cpml_handle* h, int field) {
   if (field < 0 || field > 8) return nullptr;
-  return h->fld[field];
+  return cur_fields(h)[field];
 }
 
 int cpml_get_field(cpml_handle* h, int field, float* out) {
@@ -596,6 +681,25 @@ double cpml_algorithmic_bytes_per_step(cpml_handle* h) {
 int cpml_last_run_ms(cpml_handle* h, double* ms) {
   if (!h || !ms) return CPML_ERR_INVALID;
   *ms = h->last_ms;
+  return CPML_OK;
+}
+
+int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk) {
+  if (!h || kernel < 0 || kernel > 2) return CPML_ERR_INVALID;
+  if (tile_y != 8 && tile_y != 16) return CPML_ERR_INVALID;
+  if (zchunk < 2) return CPML_ERR_INVALID;
+  if (h->it != 0) return CPML_ERR_INVALID;  // only on a fresh or reset handle
+  h->kernel = kernel;
+  h->tile_y = tile_y;
+  h->zchunk = zchunk;
+  return configure_path(h);
+}
+
+int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk) {
+  if (!h) return CPML_ERR_INVALID;
+  if (kernel) *kernel = h->pingpong ? CPML_KERNEL_FUSED : CPML_KERNEL_TWO_SWEEP;
+  if (tile_y) *tile_y = h->tile_y;
+  if (zchunk) *zchunk = h->zchunk;
   return CPML_OK;
 }
 

@@ -20,8 +20,6 @@
 
 namespace cpml {
 
-constexpr int kMaxRecPerAxis = 0;
-
 // One axis of C-PML coefficients (device pointers).
 struct Axis {
   const float* a;    // a at grid points
@@ -77,8 +75,10 @@ struct StepArgs {
   // energy constants (homogeneous)
   float half_rho, inv_2mu, e_c1, e_c2;   // see kernels
   Axis ax, ay, az;
-  Slabs m;
-  Fields f;
+  Slabs m;                 // memory variables (stress-side: time-n copy when ping-ponged)
+  Slabs mb;                // stress-side memory variables, time n+1 copy (fused path)
+  Fields f;                // wavefields read this step (time n)
+  Fields g;                // wavefields written this step (fused path; == f in place)
   Model mdl;
   int npml;                // energy interior: [npml, n-npml) on every axis
   int isrc, jsrc, ksrc;    // 0-based source cell
@@ -92,6 +92,7 @@ struct StepArgs {
   double* partials;        // [chunk][nblocks][4]: ek, ep, vmax^2, nan
   int nblocks;             // blocks of the velocity kernel
   int ep_physical;         // 3D: textbook Ep instead of the reference's
+  int* err;                // device error word (bounded waits that gave up)
 };
 
 // Linear index helpers

@@ -14,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpml.so")
 
 OK = 0
+KERNEL_AUTO, KERNEL_TWO_SWEEP, KERNEL_FUSED = 0, 1, 2
 ERR = {-1: "INVALID", -2: "CFL", -3: "OOM", -4: "UNSTABLE", -5: "TIMEOUT", -6: "CUDA",
        -7: "NOT_READY", -8: "IO", -9: "RANGE"}
 
@@ -42,6 +43,8 @@ SIGNATURES = [
     ("cpml_set_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
     ("cpml_algorithmic_bytes_per_step", ctypes.c_double, [_h]),
     ("cpml_last_run_ms", ctypes.c_int, [_h, _dp]),
+    ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip]),
     ("cpml_destroy", None, [_h]),
     ("cpml_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,

@@ -28,13 +28,15 @@ def _f32(a):
 
 
 class Solver:
-    def __init__(self, params: CpmlParams, receivers=(), model=None):
+    def __init__(self, params: CpmlParams, receivers=(), model=None, tuning=None):
         self.L = _L.load()
         self.p = params.copy()
         h = ctypes.c_void_p()
         _L.check(self.L.cpml_create(ctypes.byref(self.p), ctypes.byref(h)), "cpml_create")
         self.h = h
         self.shape = (self.p.nz, self.p.ny, self.p.nx) if self.p.ndim == 3 else (self.p.ny, self.p.nx)
+        if tuning is not None:
+            self.set_tuning(*tuning)
         if model is not None:
             self.set_model(*model)
         self.receivers = []
@@ -59,6 +61,15 @@ class Solver:
         _L.check(self.L.cpml_set_receivers(self.h, n, ix.ctypes.data_as(_ip), iy.ctypes.data_as(_ip),
                                            iz.ctypes.data_as(_ip)), "cpml_set_receivers")
         self.receivers = rec
+
+    def set_tuning(self, kernel: int = 0, tile_y: int = 16, zchunk: int = 32) -> None:
+        """Step kernel (0 auto, 1 two-sweep, 2 fused 3D) and launch shape."""
+        _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk)), "set_tuning")
+
+    def tuning(self):
+        k, t, z = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _L.check(self.L.cpml_get_tuning(self.h, ctypes.byref(k), ctypes.byref(t), ctypes.byref(z)))
+        return k.value, t.value, z.value
 
     # -- time loop -------------------------------------------------------
     def run(self, nsteps: int | None = None) -> None:

@@ -35,8 +35,8 @@ def traces(*comps):
     return np.concatenate([c for c in comps if c is not None])
 
 
-def run_gpu(p, rec, model=None, nsteps=None):
-    with Solver(p, rec, model=model) as s:
+def run_gpu(p, rec, model=None, nsteps=None, tuning=None):
+    with Solver(p, rec, model=model, tuning=tuning) as s:
         s.run(nsteps)
         vx, vy, vz = s.seismograms()
         ek, ep = s.energy()
@@ -72,14 +72,19 @@ def test_2d_small(het):
     check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
 
 
+TUNINGS_3D = [(1, 16, 32), (2, 16, 32), (2, 8, 7), (2, 16, 5)]
+
+
 @pytest.mark.parametrize("het", [False, True])
-def test_3d_small(het):
+@pytest.mark.parametrize("tuning", TUNINGS_3D, ids=["two_sweep", "fused16", "fused8_z7", "fused16_z5"])
+def test_3d_small(het, tuning):
     p, rec = P.small_3d()
     model = layered_3d(p, seed=5) if het else None
     kw = dict(lam=model[0], mu=model[1], rho=model[2]) if het else {}
     ref = oracle_c.run(p, rec=rec, keep_fields=True, **kw)
     ref32 = oracle_c.run(p, rec=rec, keep_fields=True, double=False, **kw)
-    check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
+    g = run_gpu(p, rec, model, tuning=tuning)
+    check(g, ref, ref.fields, ref32.fields)
 
 
 def test_2d_reference_default(golden):
@@ -132,13 +137,22 @@ def test_3d_reference_quirk_and_physical_energy():
         check(run_gpu(q, rec), ref)
 
 
-def test_3d_mid_size_vs_oracle():
-    """A 3D case with more than one block in every direction and a z extent
-    spanning several k-chunks, 300 steps."""
+@pytest.mark.parametrize("tuning", [(1, 16, 32), (2, 16, 32), (2, 8, 12)])
+def test_3d_mid_size_vs_oracle(tuning):
+    """A 3D case with more than one tile in every direction and a z extent
+    spanning several z-chunks, 300 steps."""
     p, rec = P.small_3d(n=(70, 52, 44), nstep=300)
     p.npoints_pml = 10
     ref = oracle_c.run(p, rec=rec)
-    check(run_gpu(p, rec), ref)
+    check(run_gpu(p, rec, tuning=tuning), ref)
+
+
+def test_fused_equals_two_sweep_traces():
+    """Both 3D step kernels agree with each other to FP32 rounding."""
+    p, rec = P.small_3d(n=(40, 36, 30), nstep=150)
+    a = run_gpu(p, rec, tuning=(1, 16, 32))
+    b = run_gpu(p, rec, tuning=(2, 16, 8))
+    assert rl2(traces(b["vx"], b["vy"], b["vz"]), traces(a["vx"], a["vy"], a["vz"])) < 2e-6
 
 
 def test_chunked_run_equals_single_run():
