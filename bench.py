@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the 3D plain C-PML workload on GB300.
+
+Workload (the reference's 3D program, run as one domain): 276^3 grid
+(256^3 interior + 10-point C-PML on all faces), DELTA = 10 m, homogeneous
+cp = 3300 m/s, cs = cp/1.732, rho = 2800, DELTAT = 1.6 ms, NSTEP = 2500,
+Ricker f0 = 7 Hz at the centre, 64 receivers on the x line through the
+centre. One bench step = one whole simulation (NSTEP time steps, from zeroed
+fields to the last seismogram sample). Inputs are synthetic (parameters only;
+the model is homogeneous). The working set (two 757 MB buffer sets) is far
+larger than L2, so no flush is needed between steps.
+
+metric: Mcell-updates/s (cells x time steps / s), higher is better.
+  value : device time of K steps through the resident handle
+          (cpml_reset + cpml_run), CUDA events on the handle's stream.
+  e2e   : the C ABI as a caller uses it, per step: cpml_create (parameters and
+          receiver indices host->device), cpml_run, cpml_get_seismograms and
+          cpml_get_energy (device->host), cpml_destroy.
+  roofline: the fused step kernel, HBM-bound; achieved = algorithmic bytes per
+          launch (every field read and written once, per-cell model once,
+          every C-PML memory variable read and written where its a != 0)
+          / average launch duration over the timed region.
+  cpu_baseline: the FP64 C++ restatement of the reference time loop with
+          OpenMP on every host core, on a bounded sample of the same grid.
+
+--impl reference times that CPU restatement alone (the reference is Fortran
+and no Fortran compiler exists on either machine), on the same config and
+metric, each step a bounded sample of time steps.
+
+Multi-GPU: the path has no exchange step in this build (one domain per GPU);
+N ranks run N independent replicas of the workload ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "fused3d_276cube.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nstep", type=int, default=None, help="time steps per bench step")
+    ap.add_argument("--tuning", type=str, default=None, help="kernel,tile_y,zchunk,depth")
+    ap.add_argument("--cpu-sample-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def n_chunks(nstep, it_display):
+    """Chunks of the runtime's time loop: ends at it = 5 and every display step."""
+    it, n = 0, 0
+    while it < nstep:
+        nd = (it // it_display + 1) * it_display
+        if it < 5:
+            nd = min(nd, 5)
+        it = min(nstep, nd, it + 128)
+        n += 1
+    return n
+
+
+def cpu_baseline(p, sample_steps, nthreads):
+    from oracle import oracle_c
+    sess = oracle_c.Session(p, nthreads=nthreads)
+    sess.run(1)  # touch every page once
+    t = time.perf_counter()
+    sess.run(sample_steps)
+    dt = time.perf_counter() - t
+    sess.close()
+    ncell = p.nx * p.ny * p.nz
+    return ncell * sample_steps / dt / 1e6, dt
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, world, rank, pg):
+    from seismic_cpml_gb300 import params as P
+    p, _ = P.config_3d_plain()
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    sample = args.cpu_sample_steps or 10
+    from oracle import oracle_c
+    sess = oracle_c.Session(p, nthreads=cores)
+    sess.run(1)
+    for _ in range(args.warmup):
+        sess.run(sample)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        sess.run(sample)
+    dt = time.perf_counter() - t
+    sess.close()
+    ncell = p.nx * p.ny * p.nz
+    value = ncell * sample * args.steps / dt / 1e6
+    line = {
+        "impl": "reference",
+        "metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "3d_plain_276cube", "grid": [p.nx, p.ny, p.nz],
+                   "nstep_per_bench_step": sample, "parallelism": "replicas"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-updates/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{sample} time steps of the 276^3 grid per bench step, "
+                                   "FP64 C++ restatement of the reference time loop, OpenMP"},
+        "e2e": {"value": round(value, 3), "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    from seismic_cpml_gb300 import params as P
+    from seismic_cpml_gb300.solver import Solver
+    torch.cuda.set_device(local)
+    p, rec = P.config_3d_plain()
+    if args.nstep:
+        p.nstep = args.nstep
+    tuning = tuple(int(x) for x in args.tuning.split(",")) if args.tuning else None
+    ncell = p.nx * p.ny * p.nz
+
+    s = Solver(p, rec, tuning=tuning)
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    for _ in range(args.warmup):
+        s.reset()
+        s.run()
+    torch.cuda.synchronize()
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.reset()
+        s.run()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier(pg)
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    dev_ms = max_over_ranks(pg, dev_ms)
+    bytes_step = s.algorithmic_bytes_per_step()
+    kern = s.tuning()
+    vx, vy, vz = s.seismograms()
+    s.close()
+
+    value = world * ncell * p.nstep * args.steps / (dev_ms / 1e3) / 1e6
+    launch_ms = dev_ms / (args.steps * p.nstep)
+    achieved = bytes_step / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = None
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            prof = json.load(f)
+        if prof.get("grid") == [p.nx, p.ny, p.nz] and list(prof.get("tuning", [])) == list(kern):
+            traffic = prof.get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        pass
+
+    # end to end through the C ABI: host inputs in, seismograms and energy out
+    e2e = None
+    chunks_e2e = n_chunks(p.nstep, p.it_display)
+    if not args.no_e2e:
+        h2d = d2h = 0
+        torch.cuda.synchronize()
+        barrier(pg)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            with Solver(p, rec, tuning=tuning) as e:
+                e.run()
+                sx, sy, sz = e.seismograms()
+                ek, ep = e.energy()
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(pg, time.perf_counter() - t)
+        # host->device: source increments (2 x nstep FP32), receiver cells (int32)
+        h2d = 2 * 4 * p.nstep + 4 * len(rec)
+        # device->host: samples (3 x nrec x nstep FP32), energy (2 x nstep FP64),
+        # FP64 profiles read back for the slab extents (3 axes x 10 x n), and
+        # the per-chunk max|v| and finiteness words
+        d2h = (3 * 4 * len(rec) * p.nstep + 2 * 8 * p.nstep + 3 * 10 * 8 * p.nx +
+               chunks_e2e * (8 + 4 * 100))
+        e2e = {"value": round(world * ncell * p.nstep * args.steps / e2e_s / 1e6, 3),
+               "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        sample = args.cpu_sample_steps or 12
+        v, dt = cpu_baseline(p, sample, cores)
+        cpu = {"value": round(v, 3), "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} time steps of the 276^3 grid ({dt:.1f} s), FP64 C++ "
+                         "restatement of the reference time loop, OpenMP"}
+
+    chunks = n_chunks(p.nstep, p.it_display)
+    line = {
+        "metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3d_plain_276cube", "grid": [p.nx, p.ny, p.nz], "nstep": p.nstep,
+                   "receivers": len(rec), "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (1.5 GB of wavefields)",
+                   "kernel": {"kind": ["auto", "two_sweep", "fused"][kern[0]], "tile_y": kern[1],
+                              "zchunk": kern[2], "depth": kern[3]}},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 5)},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": args.steps * (p.nstep + 2 * chunks),
+        "clocks": clk,
+        "wall_s": round(wall, 3),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank, pg)
+        return run_ours(args, world, rank, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -176,16 +176,22 @@ int cpml_set_field(cpml_handle* h, int field, const float* in);
    memory variable read and written once where its coefficient a is nonzero. */
 double cpml_algorithmic_bytes_per_step(cpml_handle* h);
 
-/* Milliseconds of device time spent inside the stencil kernels by the last
-   cpml_run (CUDA events on the handle's stream). */
+/* Milliseconds of device time of the last cpml_run (CUDA events recorded on
+   the handle's stream around it). */
 int cpml_last_run_ms(cpml_handle* h, double* ms);
 
-/* Select the step kernel and its launch shape: tile_y (8 or 16 rows of the
-   32-wide tile) and zchunk (planes per CTA in the z sweep). Only on a fresh
-   or reset handle. No reference counterpart: the reference's loop nests
-   (3D:825-1052) have no tunables; this is what the autotuner drives. */
-int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk);
-int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+   work or timing events against the solver's kernels. No reference
+   counterpart: the reference has no device. */
+int cpml_get_stream(cpml_handle* h, void** stream);
+
+/* Select the step kernel and its launch shape: tile_y (rows of the 32-wide
+   tile), zchunk (planes per CTA in the z sweep) and depth (planes the TMA
+   loads run ahead). Supported (tile_y, depth): (8,2) (16,2). Only on a fresh or reset handle. No reference counterpart: the
+   reference's loop nests (3D:825-1052) have no tunables; the autotuner
+   drives this. */
+int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth);
+int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth);
 
 void cpml_destroy(cpml_handle* h);
 const char* cpml_strerror(int status);

@@ -138,30 +138,49 @@ struct Out {
 // 2D program, time loop 2D:550-735
 // ---------------------------------------------------------------------------
 template <typename R>
-int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
-          const double* rho_in, const Out& o, double* fields_out) {
-  const int NX = p->nx, NY = p->ny;
-  const size_t N = size_t(NX) * NY;
-  auto at = [NX](int i, int j) { return size_t(j - 1) * NX + (i - 1); };  // 1-based
-  std::vector<R> lam(N), mu(N), rho(N);
-  const double lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);
-  const double mu0 = p->rho * p->cs * p->cs;
-  for (size_t c = 0; c < N; ++c) {                               // 2D:468-474
-    rho[c] = R(rho_in ? rho_in[c] : p->rho);
-    mu[c] = R(mu_in ? mu_in[c] : mu0);
-    lam[c] = R(lam_in ? lam_in[c] : lam0);
+struct State2D {
+  const cpml_params* p;
+  int NX, NY;
+  size_t N;
+  std::vector<R> lam, mu, rho;
+  Prof1<R> X, Y;
+  R DX, DY, DT;
+  std::vector<R> vx, vy, sxx, syy, sxy;
+  std::vector<R> m_dvx_dx, m_dvx_dy, m_dvy_dx, m_dvy_dy;
+  std::vector<R> m_dsxx_dx, m_dsyy_dy, m_dsxy_dx, m_dsxy_dy;
+  int npml;
+  double sa, ca;
+  State2D(const cpml_params* p_, const double* lam_in, const double* mu_in, const double* rho_in)
+      : p(p_), NX(p_->nx), NY(p_->ny), N(size_t(p_->nx) * p_->ny),
+        X(build_profile(p_, 0, p_->nx, p_->deltax)), Y(build_profile(p_, 1, p_->ny, p_->deltay)) {
+    lam.resize(N); mu.resize(N); rho.resize(N);
+    const double lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);
+    const double mu0 = p->rho * p->cs * p->cs;
+    for (size_t c = 0; c < N; ++c) {                               // 2D:468-474
+      rho[c] = R(rho_in ? rho_in[c] : p->rho);
+      mu[c] = R(mu_in ? mu_in[c] : mu0);
+      lam[c] = R(lam_in ? lam_in[c] : lam0);
+    }
+    DX = R(p->deltax); DY = R(p->deltay); DT = R(p->deltat);
+    for (auto* v : {&vx, &vy, &sxx, &syy, &sxy, &m_dvx_dx, &m_dvx_dy, &m_dvy_dx, &m_dvy_dy, &m_dsxx_dx,
+                    &m_dsyy_dy, &m_dsxy_dx, &m_dsxy_dy})
+      v->assign(N, R(0));
+    npml = p->npoints_pml;
+    const double ang = p->angle_force * (PI / 180.0);
+    sa = std::sin(ang); ca = std::cos(ang);
   }
-  Prof1<R> X(build_profile(p, 0, NX, p->deltax));
-  Prof1<R> Y(build_profile(p, 1, NY, p->deltay));
-  const R DX = R(p->deltax), DY = R(p->deltay), DT = R(p->deltat);
-  std::vector<R> vx(N, 0), vy(N, 0), sxx(N, 0), syy(N, 0), sxy(N, 0);
-  std::vector<R> m_dvx_dx(N, 0), m_dvx_dy(N, 0), m_dvy_dx(N, 0), m_dvy_dy(N, 0);
-  std::vector<R> m_dsxx_dx(N, 0), m_dsyy_dy(N, 0), m_dsxy_dx(N, 0), m_dsxy_dy(N, 0);
-  const int npml = p->npoints_pml;
-  const double ang = p->angle_force * (PI / 180.0);
-  const double sa = std::sin(ang), ca = std::cos(ang);
+  size_t at(int i, int j) const { return size_t(j - 1) * NX + (i - 1); }  // 1-based
+  void step(int it, const Out& o);
+  void fields(double* out) const {
+    const std::vector<R>* F[5] = {&vx, &vy, &sxx, &syy, &sxy};
+    for (int f = 0; f < 5; ++f)
+      for (size_t c = 0; c < N; ++c) out[f * N + c] = double((*F[f])[c]);
+  }
+};
 
-  for (int it = 1; it <= o.nsteps; ++it) {
+// one pass of the time loop 2D:550-735
+template <typename R>
+void State2D<R>::step(int it, const Out& o) {
     // sigma_xx, sigma_yy (2D:556-580)
 #pragma omp parallel for schedule(static)
     for (int j = 2; j <= NY; ++j)
@@ -266,11 +285,13 @@ int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
       o.vmax[it - 1] = vm;
     }
   }
-  if (fields_out) {
-    const std::vector<R>* F[5] = {&vx, &vy, &sxx, &syy, &sxy};
-    for (int f = 0; f < 5; ++f)
-      for (size_t c = 0; c < N; ++c) fields_out[f * N + c] = double((*F[f])[c]);
-  }
+
+template <typename R>
+int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
+          const double* rho_in, const Out& o, double* fields_out) {
+  State2D<R> S(p, lam_in, mu_in, rho_in);
+  for (int it = 1; it <= o.nsteps; ++it) S.step(it, o);
+  if (fields_out) S.fields(fields_out);
   return CPML_OK;
 }
 
@@ -278,46 +299,66 @@ int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
 // 3D program, time loop 3D:802-1180, one domain of NZ planes
 // ---------------------------------------------------------------------------
 template <typename R>
-int run3d(const cpml_params* p, const double* lam_in, const double* mu_in,
-          const double* rho_in, const Out& o, double* fields_out) {
-  const int NX = p->nx, NY = p->ny, NZ = p->nz;
-  const size_t N = size_t(NX) * NY * NZ;
-  const size_t SX = 1, SY = size_t(NX), SZ = size_t(NX) * NY;
-  auto at = [=](int i, int j, int k) { return size_t(k - 1) * SZ + size_t(j - 1) * SY + (i - 1); };
-  const bool het = lam_in || mu_in || rho_in;
-  const double lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);  // 3D:142-144
-  const double mu0 = p->rho * p->cs * p->cs;
-  const double l2m0 = p->rho * p->cp * p->cp;
+struct State3D {
+  const cpml_params* p;
+  int NX, NY, NZ;
+  size_t N, SX, SY, SZ;
+  bool het;
+  double lam0, mu0, l2m0;
   std::vector<R> lam, mu, rho;
-  if (het) {
-    lam.resize(N); mu.resize(N); rho.resize(N);
-    for (size_t c = 0; c < N; ++c) {
-      lam[c] = R(lam_in ? lam_in[c] : lam0);
-      mu[c] = R(mu_in ? mu_in[c] : mu0);
-      rho[c] = R(rho_in ? rho_in[c] : p->rho);
+  Prof1<R> X, Y, Z;
+  R DT, odx, ody, odz, DT_lam0, DT_mu0, DT_l2m0, DT_rho0;
+  std::vector<R> vx, vy, vz, sxx, syy, szz, sxy, sxz, syz;
+  std::vector<R> m_dvx_dx, m_dvx_dy, m_dvx_dz, m_dvy_dx, m_dvy_dy, m_dvy_dz, m_dvz_dx, m_dvz_dy,
+      m_dvz_dz, m_dsxx_dx, m_dsyy_dy, m_dszz_dz, m_dsxy_dx, m_dsxy_dy, m_dsxz_dx, m_dsxz_dz,
+      m_dsyz_dy, m_dsyz_dz;
+  int npml;
+  double sa, ca;
+  bool q1;
+  std::vector<double> ekk, epk;
+  State3D(const cpml_params* p_, const double* lam_in, const double* mu_in, const double* rho_in)
+      : p(p_), NX(p_->nx), NY(p_->ny), NZ(p_->nz), N(size_t(p_->nx) * p_->ny * p_->nz), SX(1),
+        SY(size_t(p_->nx)), SZ(size_t(p_->nx) * p_->ny), het(lam_in || mu_in || rho_in),
+        X(build_profile(p_, 0, p_->nx, p_->deltax)), Y(build_profile(p_, 1, p_->ny, p_->deltay)),
+        Z(build_profile(p_, 2, p_->nz, p_->deltaz)) {
+    lam0 = p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs);  // 3D:142-144
+    mu0 = p->rho * p->cs * p->cs;
+    l2m0 = p->rho * p->cp * p->cp;
+    if (het) {
+      lam.resize(N); mu.resize(N); rho.resize(N);
+      for (size_t c = 0; c < N; ++c) {
+        lam[c] = R(lam_in ? lam_in[c] : lam0);
+        mu[c] = R(mu_in ? mu_in[c] : mu0);
+        rho[c] = R(rho_in ? rho_in[c] : p->rho);
+      }
     }
+    DT = R(p->deltat);
+    odx = R(1.0 / p->deltax); ody = R(1.0 / p->deltay); odz = R(1.0 / p->deltaz);
+    DT_lam0 = R(p->deltat * lam0); DT_mu0 = R(p->deltat * mu0);   // 3D:296-300
+    DT_l2m0 = R(p->deltat * l2m0); DT_rho0 = R(p->deltat / p->rho);
+    for (auto* v : {&vx, &vy, &vz, &sxx, &syy, &szz, &sxy, &sxz, &syz, &m_dvx_dx, &m_dvx_dy,
+                    &m_dvx_dz, &m_dvy_dx, &m_dvy_dy, &m_dvy_dz, &m_dvz_dx, &m_dvz_dy, &m_dvz_dz,
+                    &m_dsxx_dx, &m_dsyy_dy, &m_dszz_dz, &m_dsxy_dx, &m_dsxy_dy, &m_dsxz_dx,
+                    &m_dsxz_dz, &m_dsyz_dy, &m_dsyz_dz})
+      v->assign(N, R(0));
+    npml = p->npoints_pml;
+    const double ang = p->angle_force * (PI / 180.0);
+    sa = std::sin(ang); ca = std::cos(ang);
+    q1 = !(p->flags & CPML_FLAG_EP_PHYSICAL);
+    ekk.assign(NZ + 1, 0.0); epk.assign(NZ + 1, 0.0);
   }
-  Prof1<R> X(build_profile(p, 0, NX, p->deltax));
-  Prof1<R> Y(build_profile(p, 1, NY, p->deltay));
-  Prof1<R> Z(build_profile(p, 2, NZ, p->deltaz));
-  const R DT = R(p->deltat);
-  const R odx = R(1.0 / p->deltax), ody = R(1.0 / p->deltay), odz = R(1.0 / p->deltaz);
-  const R DT_lam0 = R(p->deltat * lam0), DT_mu0 = R(p->deltat * mu0);   // 3D:296-300
-  const R DT_l2m0 = R(p->deltat * l2m0), DT_rho0 = R(p->deltat / p->rho);
+  size_t at(int i, int j, int k) const { return size_t(k - 1) * SZ + size_t(j - 1) * SY + (i - 1); }
+  void step(int it, const Out& o);
+  void fields(double* out) const {
+    const std::vector<R>* F[9] = {&vx, &vy, &vz, &sxx, &syy, &szz, &sxy, &sxz, &syz};
+    for (int f = 0; f < 9; ++f)
+      for (size_t c = 0; c < N; ++c) out[f * N + c] = double((*F[f])[c]);
+  }
+};
 
-  std::vector<R> vx(N, 0), vy(N, 0), vz(N, 0);
-  std::vector<R> sxx(N, 0), syy(N, 0), szz(N, 0), sxy(N, 0), sxz(N, 0), syz(N, 0);
-  std::vector<R> m_dvx_dx(N, 0), m_dvx_dy(N, 0), m_dvx_dz(N, 0), m_dvy_dx(N, 0), m_dvy_dy(N, 0),
-      m_dvy_dz(N, 0), m_dvz_dx(N, 0), m_dvz_dy(N, 0), m_dvz_dz(N, 0), m_dsxx_dx(N, 0),
-      m_dsyy_dy(N, 0), m_dszz_dz(N, 0), m_dsxy_dx(N, 0), m_dsxy_dy(N, 0), m_dsxz_dx(N, 0),
-      m_dsxz_dz(N, 0), m_dsyz_dy(N, 0), m_dsyz_dz(N, 0);
-  const int npml = p->npoints_pml;
-  const double ang = p->angle_force * (PI / 180.0);
-  const double sa = std::sin(ang), ca = std::cos(ang);
-  const bool q1 = !(p->flags & CPML_FLAG_EP_PHYSICAL);
-  std::vector<double> ekk(NZ + 1), epk(NZ + 1);
-
-  for (int it = 1; it <= o.nsteps; ++it) {
+// one pass of the time loop 3D:802-1180
+template <typename R>
+void State3D<R>::step(int it, const Out& o) {
     // normal stresses: k = 2..NZ, j = 2..NY, i = 1..NX-1 (3D:836-863)
 #pragma omp parallel for schedule(static)
     for (int k = 2; k <= NZ; ++k)
@@ -521,11 +562,13 @@ int run3d(const cpml_params* p, const double* lam_in, const double* mu_in,
       o.vmax[it - 1] = vm;
     }
   }
-  if (fields_out) {
-    const std::vector<R>* F[9] = {&vx, &vy, &vz, &sxx, &syy, &szz, &sxy, &sxz, &syz};
-    for (int f = 0; f < 9; ++f)
-      for (size_t c = 0; c < N; ++c) fields_out[f * N + c] = double((*F[f])[c]);
-  }
+
+template <typename R>
+int run3d(const cpml_params* p, const double* lam_in, const double* mu_in,
+          const double* rho_in, const Out& o, double* fields_out) {
+  State3D<R> S(p, lam_in, mu_in, rho_in);
+  for (int it = 1; it <= o.nsteps; ++it) S.step(it, o);
+  if (fields_out) S.fields(fields_out);
   return CPML_OK;
 }
 
@@ -560,6 +603,55 @@ int oracle_run(const cpml_params* p, int nsteps, int use_double, const double* l
                       : run2d<float>(p, lam, mu, rho, o, fields_out);
   return use_double ? run3d<double>(p, lam, mu, rho, o, fields_out)
                     : run3d<float>(p, lam, mu, rho, o, fields_out);
+}
+
+// A persistent run for timing the reference's time loop without its set-up:
+// create (allocates and zeroes like 2D:522-544 / 3D:720-756), then advance.
+struct Session {
+  cpml_params p;
+  State2D<double>* s2 = nullptr;
+  State3D<double>* s3 = nullptr;
+  int it = 0;
+  std::vector<double> ek, ep;
+};
+
+void* oracle_session_create(const cpml_params* p, const double* lam, const double* mu,
+                            const double* rho, int nthreads) {
+  if (!p || (p->ndim != 2 && p->ndim != 3)) return nullptr;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  Session* S = new Session();
+  S->p = *p;
+  if (p->ndim == 2) S->s2 = new State2D<double>(&S->p, lam, mu, rho);
+  else S->s3 = new State3D<double>(&S->p, lam, mu, rho);
+  return S;
+}
+
+// Advance nsteps steps with the reference's per-step energy; returns steps done.
+int oracle_session_run(void* h, int nsteps) {
+  Session* S = static_cast<Session*>(h);
+  if (!S || nsteps < 0) return CPML_ERR_INVALID;
+  S->ek.resize(S->it + nsteps);
+  S->ep.resize(S->it + nsteps);
+  Out o{S->it + nsteps, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        S->ek.data(), S->ep.data(), nullptr};
+  for (int q = 0; q < nsteps; ++q) {
+    ++S->it;
+    if (S->s2) S->s2->step(S->it, o);
+    else S->s3->step(S->it, o);
+  }
+  return S->it;
+}
+
+void oracle_session_destroy(void* h) {
+  Session* S = static_cast<Session*>(h);
+  if (!S) return;
+  delete S->s2;
+  delete S->s3;
+  delete S;
 }
 
 // The FP64 profiles of one axis (for tests).

@@ -44,6 +44,12 @@ def lib():
         L.oracle_source_term.restype = ctypes.c_double
         L.oracle_source_term.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
+        L.oracle_session_create.restype = ctypes.c_void_p
+        L.oracle_session_create.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int]
+        L.oracle_session_run.restype = ctypes.c_int
+        L.oracle_session_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.oracle_session_destroy.restype = None
+        L.oracle_session_destroy.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -113,3 +119,28 @@ def source_term(p, it):
 
 def max_threads():
     return lib().oracle_max_threads()
+
+
+class Session:
+    """The restated time loop kept alive between calls, so its set-up
+    (allocation and zeroing of every array) is outside a timed region."""
+
+    def __init__(self, p, nthreads=0, lam=None, mu=None, rho=None):
+        self.p = p.copy()
+        cv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
+        self._m = [cv(lam), cv(mu), cv(rho)]
+        self.h = lib().oracle_session_create(ctypes.byref(self.p), *[_ptr(a) for a in self._m],
+                                             int(nthreads))
+        if not self.h:
+            raise RuntimeError("oracle_session_create failed")
+
+    def run(self, nsteps):
+        return lib().oracle_session_run(self.h, int(nsteps))
+
+    def close(self):
+        if self.h:
+            lib().oracle_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

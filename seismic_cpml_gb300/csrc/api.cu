@@ -35,7 +35,9 @@ int blocks2d(const StepArgs& s);
 bool fused3d_supported();
 size_t fused3d_plan_bytes();
 bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* lam, const float* mu,
-                       const float* rho, int nx, int ny, int nz, int px, int ty, int lz, bool het);
+                       const float* rho, int nx, int ny, int nz, int px, int ty, int lz, int depth,
+                       bool het);
+bool fused3d_shape_ok(int ty, int depth);
 dim3 fused3d_grid(int nx, int ny, int nz, int ty, int lz);
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st);
 }  // namespace cpml
@@ -68,7 +70,7 @@ struct cpml_handle {
   float* fld1[9] = {};     // buffer set 1 (fused 3D path: time n+1 while set 0 holds n)
   bool pingpong = false;   // fields alternate between the sets every step
   int kernel = 0;          // CPML_KERNEL_*
-  int tile_y = 16, zchunk = 32;
+  int tile_y = 8, zchunk = 24, depth = 2;
   std::vector<unsigned char> plan;  // fused-path tensor maps
   int* err = nullptr;      // device error word
   float* prof32[3] = {};
@@ -376,7 +378,7 @@ int configure_path(cpml_handle* h) {
     float* sets[2][9];
     for (int f = 0; f < 9; ++f) { sets[0][f] = h->fld[f]; sets[1][f] = h->fld1[f]; }
     if (!fused3d_make_maps(h->plan.data(), sets, h->model[0], h->model[1], h->model[2], h->nx, h->ny, h->nz,
-                           h->px, h->tile_y, h->zchunk, h->het))
+                           h->px, h->tile_y, h->zchunk, h->depth, h->het))
       return CPML_ERR_CUDA;
     const dim3 g = fused3d_grid(h->nx, h->ny, h->nz, h->tile_y, h->zchunk);
     h->nblocks = int(g.x * g.y);
@@ -678,28 +680,35 @@ double cpml_algorithmic_bytes_per_step(cpml_handle* h) {
   return bytes;
 }
 
+int cpml_get_stream(cpml_handle* h, void** stream) {
+  if (!h || !stream) return CPML_ERR_INVALID;
+  *stream = (void*)h->stream;
+  return CPML_OK;
+}
+
 int cpml_last_run_ms(cpml_handle* h, double* ms) {
   if (!h || !ms) return CPML_ERR_INVALID;
   *ms = h->last_ms;
   return CPML_OK;
 }
 
-int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk) {
+int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth) {
   if (!h || kernel < 0 || kernel > 2) return CPML_ERR_INVALID;
-  if (tile_y != 8 && tile_y != 16) return CPML_ERR_INVALID;
-  if (zchunk < 2) return CPML_ERR_INVALID;
+  if (zchunk < 2 || !fused3d_shape_ok(tile_y, depth)) return CPML_ERR_INVALID;
   if (h->it != 0) return CPML_ERR_INVALID;  // only on a fresh or reset handle
   h->kernel = kernel;
   h->tile_y = tile_y;
   h->zchunk = zchunk;
+  h->depth = depth;
   return configure_path(h);
 }
 
-int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk) {
+int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth) {
   if (!h) return CPML_ERR_INVALID;
   if (kernel) *kernel = h->pingpong ? CPML_KERNEL_FUSED : CPML_KERNEL_TWO_SWEEP;
   if (tile_y) *tile_y = h->tile_y;
   if (zchunk) *zchunk = h->zchunk;
+  if (depth) *depth = h->depth;
   return CPML_OK;
 }
 

@@ -84,8 +84,6 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, 
       : "memory");
 }
 
-__device__ __forceinline__ int mod3(int m) { return (m + 6) % 3; }
-
 // Memory-variable update with ping-pong: reads the time-n value from mA,
 // writes time n+1 to mB when this CTA owns the cell. `upd` false leaves the
 // variable unchanged (cells outside the reference's loop range).
@@ -101,48 +99,55 @@ __device__ __forceinline__ float pml_pp(float d, bool upd, bool own, int sidx,
   return d * __ldg(ik + idx) + m;
 }
 
-template <int TY, bool HET>
+template <int TY, int D, bool HET>
 struct Geo {
+  static_assert(D == 2, "the ring sizes below assume loads issued two planes ahead");
   static constexpr int BX = FTX + 8;                 // TMA box width (x from i0-4)
   static constexpr int BY = TY + 2;                  // box height (y from j0-1)
   static constexpr int BOX = BX * BY;                // floats per box
   static constexpr int SLOT = (BOX * 4 + 127) / 128 * 32;  // slot stride, 128-byte aligned
   static constexpr int RX = FTX + 2, RY = TY + 2, REG = RX * RY;  // stress ring plane
-  static constexpr int NBOX = 4 + 4 + 3 + 12 + (HET ? 8 : 0);
-  static constexpr int RING = 14 * REG;
-  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 64;
+  // Power-of-two rings so a plane's slot is (m & (S-1)). Loads run two
+  // planes ahead: v_x/v_y need planes m-1..m+3 live at most -> 4 slots (the
+  // oldest is freed before the newest is issued); v_z, mu, rho need 3 -> 4;
+  // old stresses and lambda need 2.
+  static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 2 + 4 + 4 : 0);
+  static constexpr int RING = 16 * REG;              // xx yy xy zz: 2 planes; xz yz: 4
+  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 8 * D + 64;
   static constexpr int NH = 2 * FTX + 2 * TY;        // halo stress cells
 };
 
-template <int TY, bool HET>
-__global__ void __launch_bounds__(FNT, 2)
+template <int TY, int D, bool HET>
+__global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
     fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls, int Lz) {
-  using G = Geo<TY, HET>;
+  using G = Geo<TY, D, HET>;
   constexpr int BX = G::BX, SLOT = G::SLOT, RX = G::RX, REG = G::REG;
+  constexpr int NQ = TY / 8;             // own rows per thread
   extern __shared__ __align__(128) float sm[];
   float* vxs = sm;                       // [4] slots
   float* vys = vxs + 4 * SLOT;           // [4]
-  float* vzs = vys + 4 * SLOT;           // [3]
-  float* sos = vzs + 3 * SLOT;           // [2][6]
-  float* lms = sos + 12 * SLOT;          // HET: lam[2], mu[3], rho[3]
+  float* vzs = vys + 4 * SLOT;           // [4]
+  float* sos = vzs + 4 * SLOT;           // [2][6]
+  float* lms = sos + 12 * SLOT;          // per-cell model: lam[2], mu[4], rho[4]
   float* mus = lms + 2 * SLOT;
-  float* rhs = mus + 3 * SLOT;
+  float* rhs = mus + 4 * SLOT;
   float* ring = sm + G::NBOX * SLOT;
   float* r_sxx = ring;                   // [2]
   float* r_syy = r_sxx + 2 * REG;        // [2]
   float* r_sxy = r_syy + 2 * REG;        // [2]
   float* r_szz = r_sxy + 2 * REG;        // [2]
-  float* r_sxz = r_szz + 2 * REG;        // [3]
-  float* r_syz = r_sxz + 3 * REG;        // [3]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(r_syz + 3 * REG);
+  float* r_sxz = r_szz + 2 * REG;        // [4]
+  float* r_syz = r_sxz + 4 * REG;        // [4]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(r_syz + 4 * REG);
 
   const int tid = threadIdx.x;
   const int tx = tid & 31, ty = tid >> 5;
-  const int nty = (s.ny + TY - 1) / TY;
+  const int nx = s.nx, ny = s.ny, nz = s.nz;
+  const int nty = (ny + TY - 1) / TY;
   const int i0 = blockIdx.x * FTX;
   const int j0 = (blockIdx.y % nty) * TY;
   const int kb = (blockIdx.y / nty) * Lz;
-  const int ke = min(kb + Lz, s.nz);
+  const int ke = min(kb + Lz, nz);
   const int kk0 = kb - 1;
   const long long blin = blockIdx.x + (long long)gridDim.x * blockIdx.y;
   const int it = *s.it_base + ls + 1;
@@ -160,26 +165,28 @@ __global__ void __launch_bounds__(FNT, 2)
   }
 
   constexpr uint32_t kBoxBytes = (uint32_t)G::BOX * 4;
+  // load group g(m): vx(m+1), vy(m+1), vz(m), six old stresses at m
+  // (+ lam(m), mu(m+1), rho(m)); the first group also brings vx(m), vy(m),
+  // vz(m-1) (+ mu(m)).
   auto issue_group = [&](int m, uint64_t* b, bool prologue) {
-    // g(m): vx(m+1), vy(m+1), vz(m), six old stresses at m (+ lam(m), mu(m+1), rho(m))
     const int x = i0 - 4, y = j0 - 1;
-    uint32_t nb = 9 + (HET ? 3 : 0) + (prologue ? (3 + (HET ? 1 : 0)) : 0);
+    const uint32_t nb = 9 + (HET ? 3 : 0) + (prologue ? (3 + (HET ? 1 : 0)) : 0);
     mbar_expect_tx(b, nb * kBoxBytes);
     tma_load_3d(vxs + ((m + 1) & 3) * SLOT, &tm.f[0], x, y, m + 1, b);
     tma_load_3d(vys + ((m + 1) & 3) * SLOT, &tm.f[1], x, y, m + 1, b);
-    tma_load_3d(vzs + mod3(m) * SLOT, &tm.f[2], x, y, m, b);
+    tma_load_3d(vzs + (m & 3) * SLOT, &tm.f[2], x, y, m, b);
 #pragma unroll
     for (int c = 0; c < 6; ++c) tma_load_3d(sos + ((m & 1) * 6 + c) * SLOT, &tm.f[3 + c], x, y, m, b);
     if (HET) {
       tma_load_3d(lms + (m & 1) * SLOT, &tm.lam, x, y, m, b);
-      tma_load_3d(mus + mod3(m + 1) * SLOT, &tm.mu, x, y, m + 1, b);
-      tma_load_3d(rhs + mod3(m) * SLOT, &tm.rho, x, y, m, b);
+      tma_load_3d(mus + ((m + 1) & 3) * SLOT, &tm.mu, x, y, m + 1, b);
+      tma_load_3d(rhs + (m & 3) * SLOT, &tm.rho, x, y, m, b);
     }
     if (prologue) {
       tma_load_3d(vxs + (m & 3) * SLOT, &tm.f[0], x, y, m, b);
       tma_load_3d(vys + (m & 3) * SLOT, &tm.f[1], x, y, m, b);
-      tma_load_3d(vzs + mod3(m - 1) * SLOT, &tm.f[2], x, y, m - 1, b);
-      if (HET) tma_load_3d(mus + mod3(m) * SLOT, &tm.mu, x, y, m, b);
+      tma_load_3d(vzs + ((m - 1) & 3) * SLOT, &tm.f[2], x, y, m - 1, b);
+      if (HET) tma_load_3d(mus + (m & 3) * SLOT, &tm.mu, x, y, m, b);
     }
   };
 
@@ -189,226 +196,416 @@ __global__ void __launch_bounds__(FNT, 2)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) {
-    issue_group(kk0, &bar[0], true);
-    if (kk0 + 1 <= ke) issue_group(kk0 + 1, &bar[1], false);
+  // Only thread 0 waits on the TMA barriers; the CTA barrier that follows
+  // publishes the landed boxes to every thread, so no warp burns issue slots
+  // polling while other CTAs on the SM compute.
+  bool ok_all = true;
+  {
+    bool ok = true;
+    if (tid == 0) {
+      issue_group(kk0, &bar[0], true);
+      if (kk0 + 1 <= ke) issue_group(kk0 + 1, &bar[1], false);
+      ok = mbar_wait_bounded(&bar[0], 0);
+    }
+    if (!__syncthreads_and(ok ? 1 : 0)) ok_all = false;
   }
 
+  // ---- uniform classification of the tile ----------------------------------
   const int wx = s.ax.width(), wy = s.ay.width();
   const long long px = s.px, pl = s.plane;
+  // x / y memory variables exist somewhere in the tile or its halo
+  const bool xs_tile = wx > 0 && (i0 - 1 < s.ax.lo || i0 + FTX >= nx - s.ax.hi);
+  const bool ys_tile = wy > 0 && (j0 - 1 < s.ay.lo || j0 + TY >= ny - s.ay.hi);
+  // the tile or its halo reaches a face or lies partly outside: loop ranges,
+  // rigid faces and bounds need per-cell masks
+  const bool edge_tile = i0 - 1 < 1 || i0 + FTX > nx - 2 || j0 - 1 < 1 || j0 + TY > ny - 2;
+  const int n0 = s.npml;
+  const bool e_full_xy = i0 >= n0 && i0 + FTX <= nx - n0 && j0 >= n0 && j0 + TY <= ny - n0;
+  const bool has_src = s.isrc >= i0 && s.isrc < i0 + FTX && s.jsrc >= j0 && s.jsrc < j0 + TY &&
+                       s.ksrc >= kb && s.ksrc < ke;
+  const float src_x = has_src ? s.src_fx[it - 1] : 0.f;
+  const float src_y = has_src ? s.src_fy[it - 1] : 0.f;
+
+  // ---- per-thread constants -------------------------------------------------
+  const int oi = i0 + tx;
+  const int osx = (oi < nx) ? s.ax.slab(oi) : -1;
+  int oj[NQ], osy[NQ];
+  bool ov[NQ], oe[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    oj[q] = j0 + ty + 8 * q;
+    ov[q] = oi < nx && oj[q] < ny;
+    osy[q] = ov[q] ? s.ay.slab(oj[q]) : -1;
+    oe[q] = e_full_xy || (oi >= n0 && oi < nx - n0 && oj[q] >= n0 && oj[q] < ny - n0);
+  }
+  const int b_own = (ty + 1) * BX + tx + 4;
+  const int r_own = (ty + 1) * RX + tx + 1;
+  int hi = 0, hj = 0, hcomps = 0;
+  if (tid < G::NH) {
+    if (tid < FTX) { hi = i0 + tid; hj = j0 + TY; hcomps = 1; }                        // top: yy
+    else if (tid < 2 * FTX) { hi = i0 + tid - FTX; hj = j0 - 1; hcomps = 2 | 8; }       // bottom: xy, yz
+    else if (tid < 2 * FTX + TY) { hi = i0 - 1; hj = j0 + tid - 2 * FTX; hcomps = 1; }  // left: xx
+    else { hi = i0 + FTX; hj = j0 + tid - 2 * FTX - TY; hcomps = 2 | 4; }               // right: xy, xz
+  }
+  const bool hv = tid < G::NH && hi >= 0 && hi < nx && hj >= 0 && hj < ny;
+  const int hsx = hv ? s.ax.slab(hi) : -1;
+  const int hsy = hv ? s.ay.slab(hj) : -1;
+  const int hb = (hj - j0 + 1) * BX + (hi - i0 + 4);
+  const int hr = (hj - j0 + 1) * RX + (hi - i0 + 1);
+
   Kahan ek, ep;
   float vm2 = 0.f;
   int bad = 0;
-  bool ok_all = true;
-
-  // Stress at cell (i, j) of plane m. comps: 1 normal, 2 xy, 4 xz, 8 yz.
-  // bxi/byj: box coordinates of the cell; rxi/ryj: ring coordinates.
-  auto stress_cell = [&](int i, int j, int m, int comps, bool own) {
-    const int bxi = i - i0 + 4, byj = j - j0 + 1;
-    const int ridx = (j - j0 + 1) * RX + (i - i0 + 1);
-    const bool inside = i >= 0 && i < s.nx && j >= 0 && j < s.ny && m >= 0 && m < s.nz;
-    if (!inside) return;
-    const float* VX0 = vxs + (m & 3) * SLOT;
-    const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
-    const float* VY0 = vys + (m & 3) * SLOT;
-    const float* VY1 = vys + ((m + 1) & 3) * SLOT;
-    const float* VZ0 = vzs + mod3(m) * SLOT;
-    const float* VZm = vzs + mod3(m - 1) * SLOT;
-    const float* SO = sos + (m & 1) * 6 * SLOT;
-    const int b0 = byj * BX + bxi;
-    const float vxc = VX0[b0], vyc = VY0[b0], vzc = VZ0[b0];
-    const int sx = s.ax.slab(i), sy = s.ay.slab(j), sz = s.az.slab(m);
-    const long long mx = ((long long)m * s.ny + j) * wx + sx;
-    const long long my = ((long long)m * wy + sy) * px + i;
-    const long long mz = ((long long)sz * s.ny + j) * px + i;
-    const bool st = own && m >= kb && m < ke;  // this CTA stores the cell
-    const long long c = (long long)m * pl + (long long)j * px + i;
-    if (comps & 1) {
-      const bool upd = m >= 1 && j >= 1 && i <= s.nx - 2;
-      float dxx = (VX0[b0 + 1] - vxc) * s.odx;
-      float dyy = (vyc - VY0[b0 - BX]) * s.ody;
-      float dzz = (vzc - VZm[b0]) * s.odz;
-      dxx = pml_pp(dxx, upd, st, sx, s.m.x[0], s.mb.x[0], mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-      dyy = pml_pp(dyy, upd, st, sy, s.m.y[1], s.mb.y[1], my, s.ay.a, s.ay.b, s.ay.ik, j);
-      dzz = pml_pp(dzz, upd, st, sz, s.m.z[2], s.mb.z[2], mz, s.az.a, s.az.b, s.az.ik, m);
-      float dl = s.dt_lam, dl2m = s.dt_l2m;
-      if (HET) {
-        const float* L = lms + (m & 1) * SLOT;
-        const float* M = mus + mod3(m) * SLOT;
-        const float lh = 0.5f * (L[b0 + 1] + L[b0]);
-        const float mh = 0.5f * (M[b0 + 1] + M[b0]);
-        dl = s.dt * lh;
-        dl2m = s.dt * (lh + 2.0f * mh);
-      }
-      float nxx = SO[0 * SLOT + b0], nyy = SO[1 * SLOT + b0], nzz = SO[2 * SLOT + b0];
-      if (upd) {
-        nxx = nxx + (dl2m * dxx + dl * (dyy + dzz));
-        nyy = nyy + (dl * (dxx + dzz) + dl2m * dyy);
-        nzz = nzz + (dl * (dxx + dyy) + dl2m * dzz);
-      }
-      r_sxx[(m & 1) * REG + ridx] = nxx;
-      r_syy[(m & 1) * REG + ridx] = nyy;
-      r_szz[(m & 1) * REG + ridx] = nzz;
-      if (st) { s.g.sxx[c] = nxx; s.g.syy[c] = nyy; s.g.szz[c] = nzz; }
-    }
-    if (comps & 2) {
-      const bool upd = j <= s.ny - 2 && i >= 1;
-      float d1 = (vyc - VY0[b0 - 1]) * s.odx;
-      float d2 = (VX0[b0 + BX] - vxc) * s.ody;
-      d1 = pml_pp(d1, upd, st, sx, s.m.x[1], s.mb.x[1], mx, s.ax.a, s.ax.b, s.ax.ik, i);
-      d2 = pml_pp(d2, upd, st, sy, s.m.y[0], s.mb.y[0], my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
-      float dm = s.dt_mu;
-      if (HET) {
-        const float* M = mus + mod3(m) * SLOT;
-        dm = s.dt * (0.5f * (M[b0 + BX] + M[b0]));
-      }
-      float n = SO[3 * SLOT + b0];
-      if (upd) n = n + dm * (d1 + d2);
-      r_sxy[(m & 1) * REG + ridx] = n;
-      if (st) s.g.sxy[c] = n;
-    }
-    if (comps & 4) {
-      const bool upd = m <= s.nz - 2 && i >= 1;
-      float d1 = (vzc - VZ0[b0 - 1]) * s.odx;
-      float d2 = (VX1[b0] - vxc) * s.odz;
-      d1 = pml_pp(d1, upd, st, sx, s.m.x[2], s.mb.x[2], mx, s.ax.a, s.ax.b, s.ax.ik, i);
-      d2 = pml_pp(d2, upd, st, sz, s.m.z[0], s.mb.z[0], mz, s.az.ah, s.az.bh, s.az.ikh, m);
-      float dm = s.dt_mu;
-      if (HET) {
-        const float* M0 = mus + mod3(m) * SLOT;
-        const float* M1 = mus + mod3(m + 1) * SLOT;
-        dm = s.dt * (0.5f * (M1[b0] + M0[b0]));
-      }
-      float n = SO[4 * SLOT + b0];
-      if (upd) n = n + dm * (d1 + d2);
-      r_sxz[mod3(m) * REG + ridx] = n;
-      if (st) s.g.sxz[c] = n;
-    }
-    if (comps & 8) {
-      const bool upd = m <= s.nz - 2 && j <= s.ny - 2;
-      float d1 = (VZ0[b0 + BX] - vzc) * s.ody;
-      float d2 = (VY1[b0] - vyc) * s.odz;
-      d1 = pml_pp(d1, upd, st, sy, s.m.y[2], s.mb.y[2], my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
-      d2 = pml_pp(d2, upd, st, sz, s.m.z[1], s.mb.z[1], mz, s.az.ah, s.az.bh, s.az.ikh, m);
-      float dm = s.dt_mu;
-      if (HET) {
-        const float* M0 = mus + mod3(m) * SLOT;
-        const float* M1 = mus + mod3(m + 1) * SLOT;
-        const int di = (i < s.nx - 1) ? 1 : 0;
-        const float sm8 = ((((((M0[b0] + M0[b0 + di]) + M0[b0 + BX]) + M0[b0 + BX + di]) + M1[b0]) +
-                            M1[b0 + di]) + M1[b0 + BX]) + M1[b0 + BX + di];
-        dm = s.dt * (0.125f * sm8);
-      }
-      float n = SO[5 * SLOT + b0];
-      if (upd) n = n + dm * (d1 + d2);
-      r_syz[mod3(m) * REG + ridx] = n;
-      if (st) s.g.syz[c] = n;
-    }
-  };
-
-  for (int m = kk0; m <= ke; ++m) {
-    const int use = m - kk0;
-    const bool ok = mbar_wait_bounded(&bar[use & 1], (uint32_t)((use >> 1) & 1));
-    // ---- stress at plane m: own cells, then halo cells --------------------
+  // the own cells' time-n velocities of the previous plane, carried from the
+  // stress sweep to the velocity sweep one iteration later
+  float cvx[NQ], cvy[NQ], cvz[NQ], nvx[NQ], nvy[NQ], nvz[NQ];
 #pragma unroll
-    for (int q = 0; q < TY / 8; ++q) stress_cell(i0 + tx, j0 + ty + 8 * q, m, 15, true);
-    if (tid < G::NH) {
-      int i, j, comps;
-      if (tid < FTX) { i = i0 + tid; j = j0 + TY; comps = 1; }                 // top row: sigma_yy
-      else if (tid < 2 * FTX) { i = i0 + tid - FTX; j = j0 - 1; comps = 2 | 8; }  // bottom: xy, yz
-      else if (tid < 2 * FTX + TY) { i = i0 - 1; j = j0 + tid - 2 * FTX; comps = 1; }  // left: sigma_xx
-      else { i = i0 + FTX; j = j0 + tid - 2 * FTX - TY; comps = 2 | 4; }       // right: xy, xz
-      stress_cell(i, j, m, comps, false);
+  for (int q = 0; q < NQ; ++q) { cvx[q] = cvy[q] = cvz[q] = nvx[q] = nvy[q] = nvz[q] = 0.f; }
+  // interior tiles take the lean path on interior planes: no memory
+  // variables, no loop-range masks, no rigid faces
+  const bool fast_xy = !HET && !xs_tile && !ys_tile && !edge_tile && e_full_xy;
+
+  for (int m = kk0; ok_all && m <= ke; ++m) {
+    const int use = m - kk0;
+    // ======================= stress at plane m ==============================
+    if (fast_xy && m >= 1 && m <= nz - 2 && s.az.slab(m) < 0) {
+      const float* VX0 = vxs + (m & 3) * SLOT;
+      const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
+      const float* VY0 = vys + (m & 3) * SLOT;
+      const float* VY1 = vys + ((m + 1) & 3) * SLOT;
+      const float* VZ0 = vzs + (m & 3) * SLOT;
+      const float* VZm = vzs + ((m - 1) & 3) * SLOT;
+      const float* SO = sos + (m & 1) * 6 * SLOT;
+      float* Rxx = r_sxx + (m & 1) * REG;
+      float* Ryy = r_syy + (m & 1) * REG;
+      float* Rzz = r_szz + (m & 1) * REG;
+      float* Rxy = r_sxy + (m & 1) * REG;
+      float* Rxz = r_sxz + (m & 3) * REG;
+      float* Ryz = r_syz + (m & 3) * REG;
+      const bool st = m >= kb && m < ke;
+      const long long cpl = (long long)m * pl + (long long)j0 * px + i0;
+      auto cell = [&](int b, int r, int comps, bool store, long long c, float& ox, float& oy, float& oz) {
+        const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
+        ox = vxc; oy = vyc; oz = vzc;
+        if (comps & 1) {
+          const float dxx = (VX0[b + 1] - vxc) * s.odx;
+          const float dyy = (vyc - VY0[b - BX]) * s.ody;
+          const float dzz = (vzc - VZm[b]) * s.odz;
+          const float nxx = SO[b] + (s.dt_l2m * dxx + s.dt_lam * (dyy + dzz));
+          const float nyy = SO[SLOT + b] + (s.dt_lam * (dxx + dzz) + s.dt_l2m * dyy);
+          const float nzz = SO[2 * SLOT + b] + (s.dt_lam * (dxx + dyy) + s.dt_l2m * dzz);
+          Rxx[r] = nxx; Ryy[r] = nyy; Rzz[r] = nzz;
+          if (store) { s.g.sxx[c] = nxx; s.g.syy[c] = nyy; s.g.szz[c] = nzz; }
+        }
+        if (comps & 2) {
+          const float n = SO[3 * SLOT + b] + s.dt_mu * ((vyc - VY0[b - 1]) * s.odx + (VX0[b + BX] - vxc) * s.ody);
+          Rxy[r] = n;
+          if (store) s.g.sxy[c] = n;
+        }
+        if (comps & 4) {
+          const float n = SO[4 * SLOT + b] + s.dt_mu * ((vzc - VZ0[b - 1]) * s.odx + (VX1[b] - vxc) * s.odz);
+          Rxz[r] = n;
+          if (store) s.g.sxz[c] = n;
+        }
+        if (comps & 8) {
+          const float n = SO[5 * SLOT + b] + s.dt_mu * ((VZ0[b + BX] - vzc) * s.ody + (VY1[b] - vyc) * s.odz);
+          Ryz[r] = n;
+          if (store) s.g.syz[c] = n;
+        }
+      };
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        cell(b_own + q * 8 * BX, r_own + q * 8 * RX, 15, st, cpl + (long long)(ty + 8 * q) * px + tx, nvx[q],
+             nvy[q], nvz[q]);
+      if (hv) {
+        float dx, dy, dz;
+        cell(hb, hr, hcomps, false, 0, dx, dy, dz);
+      }
+    } else if (m >= 0 && m < nz) {
+      const float* VX0 = vxs + (m & 3) * SLOT;
+      const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
+      const float* VY0 = vys + (m & 3) * SLOT;
+      const float* VY1 = vys + ((m + 1) & 3) * SLOT;
+      const float* VZ0 = vzs + (m & 3) * SLOT;
+      const float* VZm = vzs + ((m - 1) & 3) * SLOT;
+      const float* SO = sos + (m & 1) * 6 * SLOT;
+      const float* Lm = lms + (m & 1) * SLOT;
+      const float* M0 = mus + (m & 3) * SLOT;
+      const float* M1 = mus + ((m + 1) & 3) * SLOT;
+      float* Rxx = r_sxx + (m & 1) * REG;
+      float* Ryy = r_syy + (m & 1) * REG;
+      float* Rzz = r_szz + (m & 1) * REG;
+      float* Rxy = r_sxy + (m & 1) * REG;
+      float* Rxz = r_sxz + (m & 3) * REG;
+      float* Ryz = r_syz + (m & 3) * REG;
+      const bool st_plane = m >= kb && m < ke;
+      const bool edge = edge_tile || m < 1 || m > nz - 2;
+      const int sz = s.az.slab(m);
+      const bool zs = sz >= 0;
+      float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
+      if (zs) {
+        za = __ldg(s.az.a + m); zb = __ldg(s.az.b + m); zk = __ldg(s.az.ik + m);
+        zah = __ldg(s.az.ah + m); zbh = __ldg(s.az.bh + m); zkh = __ldg(s.az.ikh + m);
+      }
+      const long long mxp = (long long)m * ny * wx;
+      const long long myp = (long long)m * wy * px;
+      const long long mzp = (long long)sz * ny * px;
+      const long long cpl = (long long)m * pl;
+
+      // one stress cell: box/ring offsets b/r, grid (i, j), slab indices,
+      // components (1 normal, 2 xy, 4 xz, 8 yz), own = this CTA stores it
+      auto stress = [&](int b, int r, int i, int j, int sx, int sy, int comps, bool own) {
+        const bool st = own && st_plane;
+        const long long c = cpl + (long long)j * px + i;
+        const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
+        // memory variable of one derivative: psi(n+1) = b psi(n) + a d,
+        // d' = d / K + psi(n+1); time-n values from m, n+1 to mb (own cells)
+        auto psi = [&](float d, bool upd, const float* mA, float* mB, long long mi, float a_, float b_,
+                       float k_) {
+          const float old = mA[mi];
+          const float nw = upd ? b_ * old + a_ * d : old;
+          if (st) mB[mi] = nw;
+          return d * k_ + nw;
+        };
+        const long long mxi = mxp + (long long)j * wx + sx;
+        const long long myi = myp + (long long)sy * px + i;
+        const long long mzi = mzp + (long long)j * px + i;
+        if (comps & 1) {  // sigma_xx, yy, zz: k = 2..NZ, j = 2..NY, i = 1..NX-1 (3D:836-863)
+          float d1 = (VX0[b + 1] - vxc) * s.odx;
+          float d2 = (vyc - VY0[b - BX]) * s.ody;
+          float d3 = (vzc - VZm[b]) * s.odz;
+          const bool upd = !edge || (m >= 1 && j >= 1 && i <= nx - 2);
+          if (xs_tile && sx >= 0)
+            d1 = psi(d1, upd, s.m.x[0], s.mb.x[0], mxi, __ldg(s.ax.ah + i), __ldg(s.ax.bh + i), __ldg(s.ax.ikh + i));
+          if (ys_tile && sy >= 0)
+            d2 = psi(d2, upd, s.m.y[1], s.mb.y[1], myi, __ldg(s.ay.a + j), __ldg(s.ay.b + j), __ldg(s.ay.ik + j));
+          if (zs) d3 = psi(d3, upd, s.m.z[2], s.mb.z[2], mzi, za, zb, zk);
+          float dl = s.dt_lam, dl2m = s.dt_l2m;
+          if (HET) {
+            const float lh = 0.5f * (Lm[b + 1] + Lm[b]);
+            const float mh = 0.5f * (M0[b + 1] + M0[b]);
+            dl = s.dt * lh;
+            dl2m = s.dt * (lh + 2.0f * mh);
+          }
+          const float o1 = SO[b], o2 = SO[SLOT + b], o3 = SO[2 * SLOT + b];
+          float nxx = o1 + (dl2m * d1 + dl * (d2 + d3));
+          float nyy = o2 + (dl * (d1 + d3) + dl2m * d2);
+          float nzz = o3 + (dl * (d1 + d2) + dl2m * d3);
+          if (!upd) { nxx = o1; nyy = o2; nzz = o3; }
+          Rxx[r] = nxx; Ryy[r] = nyy; Rzz[r] = nzz;
+          if (st) { s.g.sxx[c] = nxx; s.g.syy[c] = nyy; s.g.szz[c] = nzz; }
+        }
+        if (comps & 2) {  // sigma_xy: k = 1..NZ, j = 1..NY-1, i = 2..NX (3D:877-894)
+          float d1 = (vyc - VY0[b - 1]) * s.odx;
+          float d2 = (VX0[b + BX] - vxc) * s.ody;
+          const bool upd = !edge || (j <= ny - 2 && i >= 1);
+          if (xs_tile && sx >= 0)
+            d1 = psi(d1, upd, s.m.x[1], s.mb.x[1], mxi, __ldg(s.ax.a + i), __ldg(s.ax.b + i), __ldg(s.ax.ik + i));
+          if (ys_tile && sy >= 0)
+            d2 = psi(d2, upd, s.m.y[0], s.mb.y[0], myi, __ldg(s.ay.ah + j), __ldg(s.ay.bh + j), __ldg(s.ay.ikh + j));
+          const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
+          const float o = SO[3 * SLOT + b];
+          const float n = upd ? o + dm * (d1 + d2) : o;
+          Rxy[r] = n;
+          if (st) s.g.sxy[c] = n;
+        }
+        if (comps & 4) {  // sigma_xz: k = 1..NZ-1, j = 1..NY, i = 2..NX (3D:908-925)
+          float d1 = (vzc - VZ0[b - 1]) * s.odx;
+          float d2 = (VX1[b] - vxc) * s.odz;
+          const bool upd = !edge || (m <= nz - 2 && i >= 1);
+          if (xs_tile && sx >= 0)
+            d1 = psi(d1, upd, s.m.x[2], s.mb.x[2], mxi, __ldg(s.ax.a + i), __ldg(s.ax.b + i), __ldg(s.ax.ik + i));
+          if (zs) d2 = psi(d2, upd, s.m.z[0], s.mb.z[0], mzi, zah, zbh, zkh);
+          const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
+          const float o = SO[4 * SLOT + b];
+          const float n = upd ? o + dm * (d1 + d2) : o;
+          Rxz[r] = n;
+          if (st) s.g.sxz[c] = n;
+        }
+        if (comps & 8) {  // sigma_yz: k = 1..NZ-1, j = 1..NY-1, i = 1..NX (3D:927-942)
+          float d1 = (VZ0[b + BX] - vzc) * s.ody;
+          float d2 = (VY1[b] - vyc) * s.odz;
+          const bool upd = !edge || (m <= nz - 2 && j <= ny - 2);
+          if (ys_tile && sy >= 0)
+            d1 = psi(d1, upd, s.m.y[2], s.mb.y[2], myi, __ldg(s.ay.ah + j), __ldg(s.ay.bh + j), __ldg(s.ay.ikh + j));
+          if (zs) d2 = psi(d2, upd, s.m.z[1], s.mb.z[1], mzi, zah, zbh, zkh);
+          float dm = s.dt_mu;
+          if (HET) {  // 8-point average at (i+1/2, j+1/2, k+1/2); i+1 clamped on the last column
+            const int di = (i < nx - 1) ? 1 : 0;
+            const float sm8 = ((((((M0[b] + M0[b + di]) + M0[b + BX]) + M0[b + BX + di]) + M1[b]) +
+                                M1[b + di]) + M1[b + BX]) + M1[b + BX + di];
+            dm = s.dt * (0.125f * sm8);
+          }
+          const float o = SO[5 * SLOT + b];
+          const float n = upd ? o + dm * (d1 + d2) : o;
+          Ryz[r] = n;
+          if (st) s.g.syz[c] = n;
+        }
+      };
+
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        if (ov[q]) {
+          const int b = b_own + q * 8 * BX;
+          nvx[q] = VX0[b]; nvy[q] = VY0[b]; nvz[q] = VZ0[b];
+          stress(b, r_own + q * 8 * RX, oi, oj[q], osx, osy[q], 15, true);
+        }
+      if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false);
     }
-    if (!__syncthreads_and(ok ? 1 : 0)) { ok_all = false; break; }
-    // ---- velocity at plane p = m - 1 --------------------------------------
+    __syncthreads();
+    // The boxes of g(m+2) go into slots whose last reader was stress(m)
+    // (velocities of the own cells travel in registers), so they can be
+    // requested before the velocity sweep.
+    if (tid == 0 && m + 2 <= ke) issue_group(m + 2, &bar[use & 1], false);
+
+    // ======================= velocity at plane p = m - 1 ====================
     const int p = m - 1;
-    if (p >= kb && p < ke) {
-      const float* VXp = vxs + (p & 3) * SLOT;
-      const float* VYp = vys + (p & 3) * SLOT;
-      const float* VZp = vzs + mod3(p) * SLOT;
+    if (p >= kb && p < ke && fast_xy && p >= 1 && p <= nz - 2 && s.az.slab(p) < 0) {
       const float* Sxx = r_sxx + (p & 1) * REG;
       const float* Syy = r_syy + (p & 1) * REG;
       const float* Sxy = r_sxy + (p & 1) * REG;
       const float* Szz0 = r_szz + (p & 1) * REG;
       const float* Szz1 = r_szz + ((p + 1) & 1) * REG;
-      const float* Sxz0 = r_sxz + mod3(p) * REG;
-      const float* Sxzm = r_sxz + mod3(p - 1) * REG;
-      const float* Syz0 = r_syz + mod3(p) * REG;
-      const float* Syzm = r_syz + mod3(p - 1) * REG;
-      const int sz = s.az.slab(p);
+      const float* Sxz0 = r_sxz + (p & 3) * REG;
+      const float* Sxzm = r_sxz + ((p - 1) & 3) * REG;
+      const float* Syz0 = r_syz + (p & 3) * REG;
+      const float* Syzm = r_syz + ((p - 1) & 3) * REG;
+      const bool e_z = p >= n0 && p < nz - n0;
+      const long long cpl = (long long)p * pl + (long long)j0 * px + i0;
 #pragma unroll
-      for (int q = 0; q < TY / 8; ++q) {
-        const int i = i0 + tx, j = j0 + ty + 8 * q;
-        if (i >= s.nx || j >= s.ny) continue;
-        const int b0 = (j - j0 + 1) * BX + (i - i0 + 4);
-        const int r0 = (j - j0 + 1) * RX + (i - i0 + 1);
-        const int sx = s.ax.slab(i), sy = s.ay.slab(j);
-        const long long mx = ((long long)p * s.ny + j) * wx + sx;
-        const long long my = ((long long)p * wy + sy) * px + i;
-        const long long mz = ((long long)sz * s.ny + j) * px + i;
-        const long long c = (long long)p * pl + (long long)j * px + i;
-        float vx = VXp[b0], vy = VYp[b0], vz = VZp[b0];
-        const float sxx = Sxx[r0], syy = Syy[r0], szz = Szz0[r0];
-        const float sxy = Sxy[r0], sxz = Sxz0[r0], syz = Syz0[r0];
-        if (p >= 1 && j >= 1 && i >= 1) {  // v_x (3D:976-993)
-          float d1 = (sxx - Sxx[r0 - 1]) * s.odx;
-          float d2 = (sxy - Sxy[r0 - RX]) * s.ody;
-          float d3 = (sxz - Sxzm[r0]) * s.odz;
-          d1 = pml(d1, sx, s.m.x[3], mx, s.ax.a, s.ax.b, s.ax.ik, i);
-          d2 = pml(d2, sy, s.m.y[3], my, s.ay.a, s.ay.b, s.ay.ik, j);
-          d3 = pml(d3, sz, s.m.z[3], mz, s.az.a, s.az.b, s.az.ik, p);
-          float f = s.dt_over_rho;
-          if (HET) f = s.dt / (rhs + mod3(p) * SLOT)[b0];
-          vx = vx + f * (d1 + d2 + d3);
-        }
-        if (p >= 1 && j <= s.ny - 2 && i <= s.nx - 2) {  // v_y (3D:995-1014)
-          float d1 = (Sxy[r0 + 1] - sxy) * s.odx;
-          float d2 = (Syy[r0 + RX] - syy) * s.ody;
-          float d3 = (syz - Syzm[r0]) * s.odz;
-          d1 = pml(d1, sx, s.m.x[4], mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-          d2 = pml(d2, sy, s.m.y[4], my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
-          d3 = pml(d3, sz, s.m.z[4], mz, s.az.a, s.az.b, s.az.ik, p);
-          float f = s.dt_over_rho;
-          if (HET) {
-            const float* R = rhs + mod3(p) * SLOT;
-            f = s.dt / (0.25f * (R[b0] + R[b0 + 1] + R[b0 + 1 + BX] + R[b0 + BX]));
-          }
-          vy = vy + f * (d1 + d2 + d3);
-        }
-        if (p <= s.nz - 2 && j >= 1 && i <= s.nx - 2) {  // v_z (3D:1031-1052)
-          float d1 = (Sxz0[r0 + 1] - sxz) * s.odx;
-          float d2 = (syz - Syz0[r0 - RX]) * s.ody;
-          float d3 = (Szz1[r0] - szz) * s.odz;
-          d1 = pml(d1, sx, s.m.x[5], mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-          d2 = pml(d2, sy, s.m.y[5], my, s.ay.a, s.ay.b, s.ay.ik, j);
-          d3 = pml(d3, sz, s.m.z[5], mz, s.az.ah, s.az.bh, s.az.ikh, p);
-          float f = s.dt_over_rho;
-          if (HET) {
-            const float* R0 = rhs + mod3(p) * SLOT;
-            const float* R1 = rhs + mod3(p + 1) * SLOT;
-            f = s.dt / (0.25f * (R0[b0] + R0[b0 + 1] + R1[b0 + 1] + R1[b0]));
-          }
-          vz = vz + f * (d1 + d2 + d3);
-        }
-        if (i == s.isrc && j == s.jsrc && p == s.ksrc) {
-          vx += s.src_fx[it - 1];
-          vy += s.src_fy[it - 1];
-        }
-        if (i == 0 || i == s.nx - 1 || j == 0 || j == s.ny - 1 || p == 0 || p == s.nz - 1) {
-          vx = 0.f; vy = 0.f; vz = 0.f;
+      for (int q = 0; q < NQ; ++q) {
+        const int r = r_own + q * 8 * RX;
+        const long long c = cpl + (long long)(ty + 8 * q) * px + tx;
+        const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
+        const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
+        float vx = cvx[q] + s.dt_over_rho * (((sxx - Sxx[r - 1]) * s.odx + (sxy - Sxy[r - RX]) * s.ody) +
+                                             (sxz - Sxzm[r]) * s.odz);
+        float vy = cvy[q] + s.dt_over_rho * (((Sxy[r + 1] - sxy) * s.odx + (Syy[r + RX] - syy) * s.ody) +
+                                             (syz - Syzm[r]) * s.odz);
+        const float vz = cvz[q] + s.dt_over_rho * (((Sxz0[r + 1] - sxz) * s.odx + (syz - Syz0[r - RX]) * s.ody) +
+                                                   (Szz1[r] - szz) * s.odz);
+        if (has_src && p == s.ksrc && oi == s.isrc && oj[q] == s.jsrc) {
+          vx += src_x;
+          vy += src_y;
         }
         s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
         const float v2 = vx * vx + vy * vy + vz * vz;
         vm2 = fmaxf(vm2, v2);
         bad |= not_finite(v2);
-        const int n0 = s.npml;
-        if (i >= n0 && i < s.nx - n0 && j >= n0 && j < s.ny - n0 && p >= n0 && p < s.nz - n0) {
+        if (e_z) {
+          ek.add(s.half_rho * v2);
+          const float exx = s.e_c1 * sxx - s.e_c2 * (syy + szz);
+          const float eyy = s.e_c1 * syy - s.e_c2 * (sxx + szz);
+          const float third = s.ep_physical ? (s.e_c1 * szz - s.e_c2 * (sxx + syy)) * szz : eyy * syy;
+          ep.add(0.5f * (exx * sxx + eyy * syy + third) + s.inv_2mu * (sxy * sxy + sxz * sxz + syz * syz));
+        }
+      }
+    } else if (p >= kb && p < ke) {
+      const float* R0 = rhs + (p & 3) * SLOT;
+      const float* R1 = rhs + ((p + 1) & 3) * SLOT;
+      const float* Sxx = r_sxx + (p & 1) * REG;
+      const float* Syy = r_syy + (p & 1) * REG;
+      const float* Sxy = r_sxy + (p & 1) * REG;
+      const float* Szz0 = r_szz + (p & 1) * REG;
+      const float* Szz1 = r_szz + ((p + 1) & 1) * REG;
+      const float* Sxz0 = r_sxz + (p & 3) * REG;
+      const float* Sxzm = r_sxz + ((p - 1) & 3) * REG;
+      const float* Syz0 = r_syz + (p & 3) * REG;
+      const float* Syzm = r_syz + ((p - 1) & 3) * REG;
+      const bool edge = edge_tile || p < 1 || p > nz - 2;
+      const bool e_z = p >= n0 && p < nz - n0;
+      const int sz = s.az.slab(p);
+      const bool zs = sz >= 0;
+      float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
+      if (zs) {
+        za = __ldg(s.az.a + p); zb = __ldg(s.az.b + p); zk = __ldg(s.az.ik + p);
+        zah = __ldg(s.az.ah + p); zbh = __ldg(s.az.bh + p); zkh = __ldg(s.az.ikh + p);
+      }
+      const long long mxp = (long long)p * ny * wx;
+      const long long myp = (long long)p * wy * px;
+      const long long mzp = (long long)sz * ny * px;
+      const long long cpl = (long long)p * pl;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        if (!ov[q]) continue;
+        const int i = oi, j = oj[q];
+        const int b = b_own + q * 8 * BX, r = r_own + q * 8 * RX;
+        const long long c = cpl + (long long)j * px + i;
+        const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
+        const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
+        float d1 = (sxx - Sxx[r - 1]) * s.odx;   // v_x (3D:976-993)
+        float d2 = (sxy - Sxy[r - RX]) * s.ody;
+        float d3 = (sxz - Sxzm[r]) * s.odz;
+        float e1 = (Sxy[r + 1] - sxy) * s.odx;   // v_y (3D:995-1014)
+        float e2 = (Syy[r + RX] - syy) * s.ody;
+        float e3 = (syz - Syzm[r]) * s.odz;
+        float f1 = (Sxz0[r + 1] - sxz) * s.odx;  // v_z (3D:1031-1052)
+        float f2 = (syz - Syz0[r - RX]) * s.ody;
+        float f3 = (Szz1[r] - szz) * s.odz;
+        const bool ux = !edge || (p >= 1 && j >= 1 && i >= 1);
+        const bool uy = !edge || (p >= 1 && j <= ny - 2 && i <= nx - 2);
+        const bool uz = !edge || (p <= nz - 2 && j >= 1 && i <= nx - 2);
+        // in-place memory variables of the velocity sweep (only the owner
+        // touches them): updated where the component is
+        auto psi = [&](float d, bool upd, float* mm, long long mi, float a_, float b_, float k_) {
+          float nw = mm[mi];
+          if (upd) { nw = b_ * nw + a_ * d; mm[mi] = nw; }
+          return d * k_ + nw;
+        };
+        if (xs_tile && osx >= 0) {
+          const long long mi = mxp + (long long)j * wx + osx;
+          const float a_ = __ldg(s.ax.a + i), b_ = __ldg(s.ax.b + i), k_ = __ldg(s.ax.ik + i);
+          const float ah_ = __ldg(s.ax.ah + i), bh_ = __ldg(s.ax.bh + i), kh_ = __ldg(s.ax.ikh + i);
+          d1 = psi(d1, ux, s.m.x[3], mi, a_, b_, k_);
+          e1 = psi(e1, uy, s.m.x[4], mi, ah_, bh_, kh_);
+          f1 = psi(f1, uz, s.m.x[5], mi, ah_, bh_, kh_);
+        }
+        if (ys_tile && osy[q] >= 0) {
+          const long long mi = myp + (long long)osy[q] * px + i;
+          const float a_ = __ldg(s.ay.a + j), b_ = __ldg(s.ay.b + j), k_ = __ldg(s.ay.ik + j);
+          const float ah_ = __ldg(s.ay.ah + j), bh_ = __ldg(s.ay.bh + j), kh_ = __ldg(s.ay.ikh + j);
+          d2 = psi(d2, ux, s.m.y[3], mi, a_, b_, k_);
+          e2 = psi(e2, uy, s.m.y[4], mi, ah_, bh_, kh_);
+          f2 = psi(f2, uz, s.m.y[5], mi, a_, b_, k_);
+        }
+        if (zs) {
+          const long long mi = mzp + (long long)j * px + i;
+          d3 = psi(d3, ux, s.m.z[3], mi, za, zb, zk);
+          e3 = psi(e3, uy, s.m.z[4], mi, za, zb, zk);
+          f3 = psi(f3, uz, s.m.z[5], mi, zah, zbh, zkh);
+        }
+        float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
+        if (HET) {
+          fx = s.dt / R0[b];
+          fy = s.dt / (0.25f * (R0[b] + R0[b + 1] + R0[b + 1 + BX] + R0[b + BX]));
+          fz = s.dt / (0.25f * (R0[b] + R0[b + 1] + R1[b + 1] + R1[b]));
+        }
+        const float ox = cvx[q], oy = cvy[q], oz = cvz[q];
+        float vx = ox + fx * (d1 + d2 + d3);
+        float vy = oy + fy * (e1 + e2 + e3);
+        float vz = oz + fz * (f1 + f2 + f3);
+        if (edge) {
+          if (!ux) vx = ox;
+          if (!uy) vy = oy;
+          if (!uz) vz = oz;
+        }
+        if (has_src && p == s.ksrc && i == s.isrc && j == s.jsrc) {  // 3D:1080-1081
+          vx += src_x;
+          vy += src_y;
+        }
+        if (edge && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || p == 0 || p == nz - 1)) {
+          vx = 0.f; vy = 0.f; vz = 0.f;  // rigid faces (3D:1087-1121)
+        }
+        s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
+        const float v2 = vx * vx + vy * vy + vz * vz;
+        vm2 = fmaxf(vm2, v2);
+        bad |= not_finite(v2);
+        if (e_z && oe[q]) {  // energy interior (3D:1136-1143)
           float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
           if (HET) {
             const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
             const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
-            hr = 0.5f * (rhs + mod3(p) * SLOT)[b0];
+            hr = 0.5f * R0[b];
             c1 = 2.0f * (l + mu) * den;
             c2 = l * den;
             i2m = 1.0f / (2.0f * mu);
@@ -416,22 +613,26 @@ __global__ void __launch_bounds__(FNT, 2)
           ek.add(hr * v2);
           const float exx = c1 * sxx - c2 * (syy + szz);
           const float eyy = c1 * syy - c2 * (sxx + szz);
+          // the reference adds eps_yy*sigma_yy twice and no zz term (3D:1170-1171)
           const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
           ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
         }
       }
     }
-    __syncthreads();
-    if (tid == 0 && m + 2 <= ke) issue_group(m + 2, &bar[use & 1], false);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { cvx[q] = nvx[q]; cvy[q] = nvy[q]; cvz[q] = nvz[q]; }
+    bool ok = true;
+    if (tid == 0 && m + 1 <= ke) ok = mbar_wait_bounded(&bar[(use + 1) & 1], (uint32_t)(((use + 1) >> 1) & 1));
+    if (!__syncthreads_and(ok ? 1 : 0)) ok_all = false;
   }
   if (!ok_all) {
     if (tid == 0) {
       atomicOr(s.err, 1);
-      // drain copies that may still be in flight into this CTA's shared memory
-      mbar_wait_bounded(&bar[0], 0);
-      mbar_wait_bounded(&bar[0], 1);
-      mbar_wait_bounded(&bar[1], 0);
-      mbar_wait_bounded(&bar[1], 1);
+      // let copies still in flight into this CTA's shared memory land
+      for (int q = 0; q < 2; ++q) {
+        mbar_wait_bounded(&bar[q], 0);
+        mbar_wait_bounded(&bar[q], 1);
+      }
     }
     __syncthreads();
   }
@@ -473,35 +674,56 @@ static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, 
   return r == CUDA_SUCCESS;
 }
 
-template <int TY, bool HET>
+template <int TY, int D, bool HET>
 static cudaError_t set_smem_attr() {
-  return cudaFuncSetAttribute(fused3d_kernel<TY, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)Geo<TY, HET>::SMEM);
+  return cudaFuncSetAttribute(fused3d_kernel<TY, D, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)Geo<TY, D, HET>::SMEM);
 }
+
+// Instantiated launch shapes: (tile rows, prefetch depth).
+#define CPML_FUSED_SHAPES(X) X(8, 2) X(16, 2)
 
 struct FusedPlan {
   TmapSet maps[2];  // maps[q] reads buffer set q
-  int ty, lz;
+  int ty, lz, depth;
   bool het;
 };
 
+static cudaError_t set_attr_for(int ty, int d, bool het) {
+#define X(T, DD) \
+  if (ty == T && d == DD) return het ? set_smem_attr<T, DD, true>() : set_smem_attr<T, DD, false>();
+  CPML_FUSED_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+bool fused3d_shape_ok(int ty, int d) {
+#define X(T, DD) \
+  if (ty == T && d == DD) return true;
+  CPML_FUSED_SHAPES(X)
+#undef X
+  return false;
+}
+
 bool fused3d_supported() { return encode_fn() != nullptr; }
 
-size_t fused3d_smem(int ty, bool het) {
-  if (ty == 8) return het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
-  return het ? Geo<16, true>::SMEM : Geo<16, false>::SMEM;
+size_t fused3d_smem(int ty, int d, bool het) {
+#define X(T, DD) \
+  if (ty == T && d == DD) return het ? Geo<T, DD, true>::SMEM : Geo<T, DD, false>::SMEM;
+  CPML_FUSED_SHAPES(X)
+#undef X
+  return 0;
 }
 
 // Build the tensor maps of both buffer sets. fields[q][f] = field f of set q.
 bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* lam, const float* mu,
-                       const float* rho, int nx, int ny, int nz, int px, int ty, int lz, bool het) {
+                       const float* rho, int nx, int ny, int nz, int px, int ty, int lz, int depth,
+                       bool het) {
   FusedPlan* P = static_cast<FusedPlan*>(plan_mem);
-  P->ty = ty; P->lz = lz; P->het = het;
+  P->ty = ty; P->lz = lz; P->depth = depth; P->het = het;
   // opt in to the dynamic shared memory once per configuration, outside any
   // stream capture
-  cudaError_t e = ty == 8 ? (het ? set_smem_attr<8, true>() : set_smem_attr<8, false>())
-                          : (het ? set_smem_attr<16, true>() : set_smem_attr<16, false>());
-  if (e != cudaSuccess) return false;
+  if (set_attr_for(ty, depth, het) != cudaSuccess) return false;
   for (int q = 0; q < 2; ++q) {
     for (int f = 0; f < 9; ++f)
       if (!make_map(&P->maps[q].f[f], fields[q][f], nx, ny, nz, px, ty)) return false;
@@ -525,18 +747,23 @@ dim3 fused3d_grid(int nx, int ny, int nz, int ty, int lz) {
   return dim3(ntx, nty * nkz, 1);
 }
 
-template <int TY, bool HET>
+template <int TY, int D, bool HET>
 static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
-  using G = Geo<TY, HET>;
+  using G = Geo<TY, D, HET>;
   const dim3 g = fused3d_grid(s.nx, s.ny, s.nz, TY, P->lz);
-  fused3d_kernel<TY, HET><<<g, FNT, G::SMEM, st>>>(P->maps[parity], s, ls, P->lz);
+  fused3d_kernel<TY, D, HET><<<g, FNT, G::SMEM, st>>>(P->maps[parity], s, ls, P->lz);
   return cudaGetLastError();
 }
 
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st) {
   const FusedPlan* P = static_cast<const FusedPlan*>(plan_mem);
-  if (P->ty == 8) return P->het ? launch_t<8, true>(P, s, ls, parity, st) : launch_t<8, false>(P, s, ls, parity, st);
-  return P->het ? launch_t<16, true>(P, s, ls, parity, st) : launch_t<16, false>(P, s, ls, parity, st);
+#define X(T, DD)                                                            \
+  if (P->ty == T && P->depth == DD)                                         \
+    return P->het ? launch_t<T, DD, true>(P, s, ls, parity, st)             \
+                  : launch_t<T, DD, false>(P, s, ls, parity, st);
+  CPML_FUSED_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace cpml

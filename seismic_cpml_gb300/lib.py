@@ -43,8 +43,9 @@ SIGNATURES = [
     ("cpml_set_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
     ("cpml_algorithmic_bytes_per_step", ctypes.c_double, [_h]),
     ("cpml_last_run_ms", ctypes.c_int, [_h, _dp]),
-    ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
-    ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip]),
+    ("cpml_get_stream", ctypes.c_int, [_h, _P(ctypes.c_void_p)]),
+    ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip, _ip]),
     ("cpml_destroy", None, [_h]),
     ("cpml_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,

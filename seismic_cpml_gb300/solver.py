@@ -62,14 +62,16 @@ class Solver:
                                            iz.ctypes.data_as(_ip)), "cpml_set_receivers")
         self.receivers = rec
 
-    def set_tuning(self, kernel: int = 0, tile_y: int = 16, zchunk: int = 32) -> None:
+    def set_tuning(self, kernel: int = 0, tile_y: int = 8, zchunk: int = 24, depth: int = 2) -> None:
         """Step kernel (0 auto, 1 two-sweep, 2 fused 3D) and launch shape."""
-        _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk)), "set_tuning")
+        _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk), int(depth)),
+                 "set_tuning")
 
     def tuning(self):
-        k, t, z = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        _L.check(self.L.cpml_get_tuning(self.h, ctypes.byref(k), ctypes.byref(t), ctypes.byref(z)))
-        return k.value, t.value, z.value
+        k, t, z, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _L.check(self.L.cpml_get_tuning(self.h, ctypes.byref(k), ctypes.byref(t), ctypes.byref(z),
+                                        ctypes.byref(d)))
+        return k.value, t.value, z.value, d.value
 
     # -- time loop -------------------------------------------------------
     def run(self, nsteps: int | None = None) -> None:
@@ -90,6 +92,12 @@ class Solver:
         v = ctypes.c_double()
         _L.check(self.L.cpml_last_run_ms(self.h, ctypes.byref(v)))
         return v.value
+
+    def stream_ptr(self) -> int:
+        """The handle's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        p = ctypes.c_void_p()
+        _L.check(self.L.cpml_get_stream(self.h, ctypes.byref(p)))
+        return int(p.value or 0)
 
     def algorithmic_bytes_per_step(self) -> float:
         return float(self.L.cpml_algorithmic_bytes_per_step(self.h))

@@ -72,11 +72,11 @@ def test_2d_small(het):
     check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
 
 
-TUNINGS_3D = [(1, 16, 32), (2, 16, 32), (2, 8, 7), (2, 16, 5)]
+TUNINGS_3D = [(1, 8, 32, 2), (2, 16, 32, 2), (2, 8, 7, 2), (2, 16, 5, 2), (2, 8, 9, 2), (2, 8, 11, 2)]
 
 
 @pytest.mark.parametrize("het", [False, True])
-@pytest.mark.parametrize("tuning", TUNINGS_3D, ids=["two_sweep", "fused16", "fused8_z7", "fused16_z5"])
+@pytest.mark.parametrize("tuning", TUNINGS_3D, ids=["two_sweep", "f16z32", "f8z7", "f16z5", "f8z9", "f8z11"])
 def test_3d_small(het, tuning):
     p, rec = P.small_3d()
     model = layered_3d(p, seed=5) if het else None
@@ -137,7 +137,7 @@ def test_3d_reference_quirk_and_physical_energy():
         check(run_gpu(q, rec), ref)
 
 
-@pytest.mark.parametrize("tuning", [(1, 16, 32), (2, 16, 32), (2, 8, 12)])
+@pytest.mark.parametrize("tuning", [(1, 8, 32, 2), (2, 16, 32, 2), (2, 8, 12, 2), (2, 8, 20, 2)])
 def test_3d_mid_size_vs_oracle(tuning):
     """A 3D case with more than one tile in every direction and a z extent
     spanning several z-chunks, 300 steps."""
@@ -150,8 +150,8 @@ def test_3d_mid_size_vs_oracle(tuning):
 def test_fused_equals_two_sweep_traces():
     """Both 3D step kernels agree with each other to FP32 rounding."""
     p, rec = P.small_3d(n=(40, 36, 30), nstep=150)
-    a = run_gpu(p, rec, tuning=(1, 16, 32))
-    b = run_gpu(p, rec, tuning=(2, 16, 8))
+    a = run_gpu(p, rec, tuning=(1, 8, 32, 2))
+    b = run_gpu(p, rec, tuning=(2, 16, 8, 2))
     assert rl2(traces(b["vx"], b["vy"], b["vz"]), traces(a["vx"], a["vy"], a["vz"])) < 2e-6
 
 
