@@ -196,6 +196,27 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
 void cpml_destroy(cpml_handle* h);
 const char* cpml_strerror(int status);
 
+/* Kinetic and potential energy (the 3D program's formulas, 3D:1131-1180) of
+   nine caller-owned FP32 device wavefields, allocating no device memory.
+   No counterpart in the reference: it serves callers that cannot allocate
+   device memory mid-run (a host that owns its fields through its own pool or
+   a fixed memory budget, where cudaMalloc would synchronise or fail).
+     fields: 9 device pointers vx vy vz sxx syy szz sxy sxz syz, each
+             [nz][ny][pitch] floats (pitch >= nx, in floats);
+     npml:   interior = [npml, n - npml) on every axis;
+     lam/mu/rho: homogeneous model, used when the three *_cell device arrays
+             (same layout as the fields) are NULL;
+     flags:  CPML_FLAG_EP_PHYSICAL selects the textbook Ep;
+     out:    device pointer to 2 doubles (Ek, Ep), written on `stream`.
+   Scratch is a static device array of per-plane sums for at most 8192 planes
+   (nz > 8192 returns CPML_ERR_RANGE). Its address is looked up on a device's
+   first call, so make that call before any stream capture. All calls share
+   that array: calls that overlap on the GPU race, so order them. */
+int cpml_energy3d_noalloc(const float* const* fields, int nx, int ny, int nz, int pitch,
+                          int npml, double lam, double mu, double rho,
+                          const float* lam_cell, const float* mu_cell,
+                          const float* rho_cell, int flags, double* out, void* stream);
+
 /* ---- reference output files (2D:738-808, 820-999; 3D:1247-1364) -------- */
 
 /* Vx_file_NNN.dat / Vy_file_NNN.dat (/ Vz_file_NNN.dat if vz != NULL), one

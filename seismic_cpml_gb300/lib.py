@@ -47,6 +47,11 @@ SIGNATURES = [
     ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip, _ip]),
     ("cpml_destroy", None, [_h]),
+    ("cpml_energy3d_noalloc", ctypes.c_int, [_P(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     ("cpml_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_double]),
