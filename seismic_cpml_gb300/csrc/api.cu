@@ -38,7 +38,10 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
                        const float* rho, int nx, int ny, int nz, int px, int ty, int lz, int depth,
                        bool het);
 bool fused3d_shape_ok(int ty, int depth);
-dim3 fused3d_grid(int nx, int ny, int nz, int ty, int lz);
+void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const Axis& az, int npml,
+                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen);
+void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, int n_gen,
+                       cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join);
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st);
 }  // namespace cpml
 
@@ -71,7 +74,9 @@ struct cpml_handle {
   bool pingpong = false;   // fields alternate between the sets every step
   int kernel = 0;          // CPML_KERNEL_*
   int tile_y = 8, zchunk = 24, depth = 2;
-  std::vector<unsigned char> plan;  // fused-path tensor maps
+  std::vector<unsigned char> plan;  // fused-path tensor maps and item lists
+  cudaStream_t aux = nullptr;       // second stream of the fused step's fork/join
+  cudaEvent_t fork = nullptr, join = nullptr;
   int* err = nullptr;      // device error word
   float* prof32[3] = {};
   double* prof64[3] = {};
@@ -380,8 +385,24 @@ int configure_path(cpml_handle* h) {
     if (!fused3d_make_maps(h->plan.data(), sets, h->model[0], h->model[1], h->model[2], h->nx, h->ny, h->nz,
                            h->px, h->tile_y, h->zchunk, h->depth, h->het))
       return CPML_ERR_CUDA;
-    const dim3 g = fused3d_grid(h->nx, h->ny, h->nz, h->tile_y, h->zchunk);
-    h->nblocks = int(g.x * g.y);
+    std::vector<int4> fast, gen;
+    fused3d_items(h->nx, h->ny, h->nz, h->axes[0], h->axes[1], h->axes[2], h->p.npoints_pml, h->tile_y,
+                  h->zchunk, h->het, fast, gen);
+    int4 *dfast = nullptr, *dgen = nullptr;
+    if ((st = dalloc(h, &dfast, fast.size()))) return st;
+    if ((st = dalloc(h, &dgen, gen.size()))) return st;
+    if (!fast.empty())
+      CK(cudaMemcpy(dfast, fast.data(), sizeof(int4) * fast.size(), cudaMemcpyHostToDevice));
+    if (!gen.empty())
+      CK(cudaMemcpy(dgen, gen.data(), sizeof(int4) * gen.size(), cudaMemcpyHostToDevice));
+    if (!h->aux) {
+      CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
+    }
+    fused3d_set_items(h->plan.data(), dfast, (int)fast.size(), dgen, (int)gen.size(), h->aux, h->fork,
+                      h->join);
+    h->nblocks = int(fast.size() + gen.size());
   } else {
     StepArgs s = make_args(h);
     h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
@@ -717,6 +738,10 @@ void cpml_destroy(cpml_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graphs(h);
   for (void* p : h->allocs) cudaFree(p);
+  if (h->aux) cudaStreamSynchronize(h->aux);
+  if (h->fork) cudaEventDestroy(h->fork);
+  if (h->join) cudaEventDestroy(h->join);
+  if (h->aux) cudaStreamDestroy(h->aux);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);

@@ -1,32 +1,39 @@
 // fused3d.cu -- one-sweep 3D velocity-stress C-PML time step for sm_103a.
 //
-// One launch advances every field one full time step of
+// One step advances every field one full time step of
 // seismic_CPML_3D_isotropic_MPI_OpenMP.f90 (stress 3D:836-943, velocity
 // 3D:976-1052, source 3D:1055-1083, rigid faces 3D:1087-1121, energy
 // 3D:1131-1180), reading time level n from buffer set A and writing time
 // level n+1 to buffer set B. With separate read and write sets no CTA can
 // see another CTA's half-updated cells, so the sweep needs no grid-wide
-// synchronisation and every field crosses HBM exactly once per step
-// (9 reads + 9 writes = 72 B/cell, the compulsory minimum).
+// synchronisation and every field crosses HBM once per step (9 reads + 9
+// writes = 72 B/cell, the compulsory minimum).
 //
-// CTA work: a 32 x TY tile of (i, j) columns over a chunk [kb, ke) of planes.
-// The CTA streams planes in z (2.5D): at iteration m it
-//   1. waits for load group g(m): TMA boxes of v_x(m+1), v_y(m+1), v_z(m)
-//      and the six old stresses at plane m, each a (32+8) x (TY+2) box with
-//      a one-cell halo in y and an x window rounded out to 16-byte TMA
-//      alignment (x starts at i0-4);
-//   2. computes the new stresses at plane m on the tile plus the halo cells
+// Work items: a 32 x TY tile of (i, j) columns over a chunk [kb, ke) of
+// planes. Items are split into two lists launched as two kernels that run
+// concurrently (they share no cells and only read set A):
+//   interior items -- the tile, its one-cell halo and all planes kb-1..ke lie
+//       outside every C-PML slab and every rigid face: no memory variables,
+//       no loop-range masks; compiled lean for high occupancy;
+//   general items  -- everything else (PML slabs, faces, partial tiles, and
+//       the per-cell model), with every memory-variable load of a cell issued
+//       together before its arithmetic.
+// A CTA streams its planes in z (2.5D); at iteration m it
+//   1. computes the new stresses at plane m on the tile plus the halo cells
 //      the velocity update reads (left column: sigma_xx, top row: sigma_yy,
 //      right column: sigma_xy/sigma_xz, bottom row: sigma_xy/sigma_yz) into a
-//      shared-memory ring of planes, storing only its own cells to B;
-//   3. computes the new velocities one plane behind (plane m-1), which needs
-//      new stresses at planes m-2..m, all in the ring, then source, rigid
-//      faces, receivers-free store to B and the energy partials;
-//   4. issues load group g(m+2) into the slots freed by this iteration.
-// Old velocities live in a 4-slot (v_x, v_y) / 3-slot (v_z) ring, old
-// stresses in 2 slots, so each TMA box is loaded two iterations ahead.
+//      shared-memory ring of planes, storing its own cells to B; the old
+//      velocities and stresses come from TMA boxes (32+8) x (TY+2) loaded two
+//      planes ahead (x window from i0-4 for 16-byte TMA alignment, one-cell
+//      halo in y, zero fill outside the grid);
+//   2. requests load group g(m+2) into the slots stress(m) was the last to
+//      read (each thread carries its own cells' old velocities in registers);
+//   3. computes the new velocities one plane behind (plane m-1) from the
+//      stress ring (planes m-2..m), then source, rigid faces, store to B and
+//      the energy partials;
+//   4. thread 0 waits for g(m+1); the CTA barrier that follows publishes it.
 // Stress-side C-PML memory variables are ping-ponged like the fields (halo
-// cells read time-n values that the owner is overwriting); velocity-side
+// cells read time-n values that their owner is overwriting); velocity-side
 // ones are updated in place (only the owner touches them).
 //
 // Waits on the TMA barriers are bounded (clock64); on timeout the CTA sets
@@ -34,6 +41,7 @@
 // wait and leaves the sweep. The host reports CPML_ERR_TIMEOUT.
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <vector>
 #include "cpml_internal.cuh"
 #include "kutil.cuh"
 
@@ -84,43 +92,28 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, 
       : "memory");
 }
 
-// Memory-variable update with ping-pong: reads the time-n value from mA,
-// writes time n+1 to mB when this CTA owns the cell. `upd` false leaves the
-// variable unchanged (cells outside the reference's loop range).
-__device__ __forceinline__ float pml_pp(float d, bool upd, bool own, int sidx,
-                                        const float* __restrict__ mA, float* __restrict__ mB,
-                                        long long midx, const float* __restrict__ a,
-                                        const float* __restrict__ b, const float* __restrict__ ik,
-                                        int idx) {
-  if (sidx < 0) return d;
-  const float old = mA[midx];
-  const float m = upd ? __ldg(b + idx) * old + __ldg(a + idx) * d : old;
-  if (own) mB[midx] = m;
-  return d * __ldg(ik + idx) + m;
-}
-
-template <int TY, int D, bool HET>
+template <int TY, bool HET>
 struct Geo {
-  static_assert(D == 2, "the ring sizes below assume loads issued two planes ahead");
   static constexpr int BX = FTX + 8;                 // TMA box width (x from i0-4)
   static constexpr int BY = TY + 2;                  // box height (y from j0-1)
   static constexpr int BOX = BX * BY;                // floats per box
   static constexpr int SLOT = (BOX * 4 + 127) / 128 * 32;  // slot stride, 128-byte aligned
   static constexpr int RX = FTX + 2, RY = TY + 2, REG = RX * RY;  // stress ring plane
-  // Power-of-two rings so a plane's slot is (m & (S-1)). Loads run two
-  // planes ahead: v_x/v_y need planes m-1..m+3 live at most -> 4 slots (the
-  // oldest is freed before the newest is issued); v_z, mu, rho need 3 -> 4;
-  // old stresses and lambda need 2.
+  // Power-of-two rings, a plane's slot is (m & (S-1)). Loads run two planes
+  // ahead: v_x/v_y/v_z, mu and rho need at most 4 live planes, old stresses
+  // and lambda 2.
   static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 2 + 4 + 4 : 0);
   static constexpr int RING = 16 * REG;              // xx yy xy zz: 2 planes; xz yz: 4
-  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 8 * D + 64;
+  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 16 + 64;
   static constexpr int NH = 2 * FTX + 2 * TY;        // halo stress cells
 };
 
-template <int TY, int D, bool HET>
-__global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
-    fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls, int Lz) {
-  using G = Geo<TY, D, HET>;
+template <int TY, bool FAST, bool HET>
+__global__ void __launch_bounds__(FNT, FAST ? 3 : 2)
+    fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls,
+                   const int4* __restrict__ items, int item_base, int record) {
+  static_assert(!(FAST && HET), "the interior kernel is homogeneous only");
+  using G = Geo<TY, HET>;
   constexpr int BX = G::BX, SLOT = G::SLOT, RX = G::RX, REG = G::REG;
   constexpr int NQ = TY / 8;             // own rows per thread
   extern __shared__ __align__(128) float sm[];
@@ -143,19 +136,16 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
   const int tid = threadIdx.x;
   const int tx = tid & 31, ty = tid >> 5;
   const int nx = s.nx, ny = s.ny, nz = s.nz;
-  const int nty = (ny + TY - 1) / TY;
-  const int i0 = blockIdx.x * FTX;
-  const int j0 = (blockIdx.y % nty) * TY;
-  const int kb = (blockIdx.y / nty) * Lz;
-  const int ke = min(kb + Lz, nz);
+  const int4 item = items[blockIdx.x];
+  const int i0 = item.x, j0 = item.y, kb = item.z, ke = item.w;
   const int kk0 = kb - 1;
-  const long long blin = blockIdx.x + (long long)gridDim.x * blockIdx.y;
+  const long long blin = item_base + blockIdx.x;   // slot of this item's energy partials
   const int it = *s.it_base + ls + 1;
 
   // receivers of the step that just ended, from the read set
-  if (ls > 0) {
+  if (record && ls > 0) {
     const size_t slab = (size_t)s.nrec * s.nstep;
-    for (long long r = blin * FNT + tid; r < s.nrec; r += (long long)gridDim.x * gridDim.y * FNT) {
+    for (long long r = (long long)blockIdx.x * FNT + tid; r < s.nrec; r += (long long)gridDim.x * FNT) {
       const long long c = s.rec_cell[r];
       const size_t o = (size_t)r * s.nstep + (size_t)(it - 2);
       s.seis[o] = s.f.vx[c];
@@ -197,7 +187,7 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
   }
   __syncthreads();
   // Only thread 0 waits on the TMA barriers; the CTA barrier that follows
-  // publishes the landed boxes to every thread, so no warp burns issue slots
+  // publishes the landed boxes to every thread, so no warp spends issue slots
   // polling while other CTAs on the SM compute.
   bool ok_all = true;
   {
@@ -210,14 +200,11 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
     if (!__syncthreads_and(ok ? 1 : 0)) ok_all = false;
   }
 
-  // ---- uniform classification of the tile ----------------------------------
+  // ---- tile classification (uniform over the CTA) ---------------------------
   const int wx = s.ax.width(), wy = s.ay.width();
   const long long px = s.px, pl = s.plane;
-  // x / y memory variables exist somewhere in the tile or its halo
   const bool xs_tile = wx > 0 && (i0 - 1 < s.ax.lo || i0 + FTX >= nx - s.ax.hi);
   const bool ys_tile = wy > 0 && (j0 - 1 < s.ay.lo || j0 + TY >= ny - s.ay.hi);
-  // the tile or its halo reaches a face or lies partly outside: loop ranges,
-  // rigid faces and bounds need per-cell masks
   const bool edge_tile = i0 - 1 < 1 || i0 + FTX > nx - 2 || j0 - 1 < 1 || j0 + TY > ny - 2;
   const int n0 = s.npml;
   const bool e_full_xy = i0 >= n0 && i0 + FTX <= nx - n0 && j0 >= n0 && j0 + TY <= ny - n0;
@@ -226,7 +213,7 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
   const float src_x = has_src ? s.src_fx[it - 1] : 0.f;
   const float src_y = has_src ? s.src_fy[it - 1] : 0.f;
 
-  // ---- per-thread constants -------------------------------------------------
+  // ---- per-thread constants ---------------------------------------------------
   const int oi = i0 + tx;
   const int osx = (oi < nx) ? s.ax.slab(oi) : -1;
   int oj[NQ], osy[NQ];
@@ -256,33 +243,30 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
   Kahan ek, ep;
   float vm2 = 0.f;
   int bad = 0;
-  // the own cells' time-n velocities of the previous plane, carried from the
-  // stress sweep to the velocity sweep one iteration later
+  // own cells' time-n velocities of plane m, carried from the stress sweep
+  // of iteration m to the velocity sweep of iteration m+1
   float cvx[NQ], cvy[NQ], cvz[NQ], nvx[NQ], nvy[NQ], nvz[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { cvx[q] = cvy[q] = cvz[q] = nvx[q] = nvy[q] = nvz[q] = 0.f; }
-  // interior tiles take the lean path on interior planes: no memory
-  // variables, no loop-range masks, no rigid faces
-  const bool fast_xy = !HET && !xs_tile && !ys_tile && !edge_tile && e_full_xy;
 
   for (int m = kk0; ok_all && m <= ke; ++m) {
     const int use = m - kk0;
     // ======================= stress at plane m ==============================
-    if (fast_xy && m >= 1 && m <= nz - 2 && s.az.slab(m) < 0) {
-      const float* VX0 = vxs + (m & 3) * SLOT;
-      const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
-      const float* VY0 = vys + (m & 3) * SLOT;
-      const float* VY1 = vys + ((m + 1) & 3) * SLOT;
-      const float* VZ0 = vzs + (m & 3) * SLOT;
-      const float* VZm = vzs + ((m - 1) & 3) * SLOT;
-      const float* SO = sos + (m & 1) * 6 * SLOT;
-      float* Rxx = r_sxx + (m & 1) * REG;
-      float* Ryy = r_syy + (m & 1) * REG;
-      float* Rzz = r_szz + (m & 1) * REG;
-      float* Rxy = r_sxy + (m & 1) * REG;
-      float* Rxz = r_sxz + (m & 3) * REG;
-      float* Ryz = r_syz + (m & 3) * REG;
-      const bool st = m >= kb && m < ke;
+    const float* VX0 = vxs + (m & 3) * SLOT;
+    const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
+    const float* VY0 = vys + (m & 3) * SLOT;
+    const float* VY1 = vys + ((m + 1) & 3) * SLOT;
+    const float* VZ0 = vzs + (m & 3) * SLOT;
+    const float* VZm = vzs + ((m - 1) & 3) * SLOT;
+    const float* SO = sos + (m & 1) * 6 * SLOT;
+    float* Rxx = r_sxx + (m & 1) * REG;
+    float* Ryy = r_syy + (m & 1) * REG;
+    float* Rzz = r_szz + (m & 1) * REG;
+    float* Rxy = r_sxy + (m & 1) * REG;
+    float* Rxz = r_sxz + (m & 3) * REG;
+    float* Ryz = r_syz + (m & 3) * REG;
+    const bool st_plane = m >= kb && m < ke;
+    if (FAST) {
       const long long cpl = (long long)m * pl + (long long)j0 * px + i0;
       auto cell = [&](int b, int r, int comps, bool store, long long c, float& ox, float& oy, float& oz) {
         const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
@@ -315,30 +299,16 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
       };
 #pragma unroll
       for (int q = 0; q < NQ; ++q)
-        cell(b_own + q * 8 * BX, r_own + q * 8 * RX, 15, st, cpl + (long long)(ty + 8 * q) * px + tx, nvx[q],
-             nvy[q], nvz[q]);
-      if (hv) {
+        cell(b_own + q * 8 * BX, r_own + q * 8 * RX, 15, st_plane, cpl + (long long)(ty + 8 * q) * px + tx,
+             nvx[q], nvy[q], nvz[q]);
+      if (tid < G::NH) {
         float dx, dy, dz;
         cell(hb, hr, hcomps, false, 0, dx, dy, dz);
       }
     } else if (m >= 0 && m < nz) {
-      const float* VX0 = vxs + (m & 3) * SLOT;
-      const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
-      const float* VY0 = vys + (m & 3) * SLOT;
-      const float* VY1 = vys + ((m + 1) & 3) * SLOT;
-      const float* VZ0 = vzs + (m & 3) * SLOT;
-      const float* VZm = vzs + ((m - 1) & 3) * SLOT;
-      const float* SO = sos + (m & 1) * 6 * SLOT;
       const float* Lm = lms + (m & 1) * SLOT;
       const float* M0 = mus + (m & 3) * SLOT;
       const float* M1 = mus + ((m + 1) & 3) * SLOT;
-      float* Rxx = r_sxx + (m & 1) * REG;
-      float* Ryy = r_syy + (m & 1) * REG;
-      float* Rzz = r_szz + (m & 1) * REG;
-      float* Rxy = r_sxy + (m & 1) * REG;
-      float* Rxz = r_sxz + (m & 3) * REG;
-      float* Ryz = r_syz + (m & 3) * REG;
-      const bool st_plane = m >= kb && m < ke;
       const bool edge = edge_tile || m < 1 || m > nz - 2;
       const int sz = s.az.slab(m);
       const bool zs = sz >= 0;
@@ -352,34 +322,48 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
       const long long mzp = (long long)sz * ny * px;
       const long long cpl = (long long)m * pl;
 
-      // one stress cell: box/ring offsets b/r, grid (i, j), slab indices,
-      // components (1 normal, 2 xy, 4 xz, 8 yz), own = this CTA stores it
+      // one stress cell: box/ring offsets, grid (i, j), slab indices,
+      // components (1 normal, 2 xy, 4 xz, 8 yz); own = this CTA stores it
       auto stress = [&](int b, int r, int i, int j, int sx, int sy, int comps, bool own) {
         const bool st = own && st_plane;
         const long long c = cpl + (long long)j * px + i;
-        const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
-        // memory variable of one derivative: psi(n+1) = b psi(n) + a d,
-        // d' = d / K + psi(n+1); time-n values from m, n+1 to mb (own cells)
-        auto psi = [&](float d, bool upd, const float* mA, float* mB, long long mi, float a_, float b_,
-                       float k_) {
-          const float old = mA[mi];
+        const bool hx = xs_tile && sx >= 0, hy = ys_tile && sy >= 0;
+        const long long mxi = mxp + (long long)j * wx + sx;
+        const long long myi = myp + (long long)sy * px + i;
+        const long long mzi = mzp + (long long)j * px + i;
+        // every time-n memory variable and coefficient of the cell, issued
+        // together so their latencies overlap
+        float qx0 = 0.f, qx1 = 0.f, qx2 = 0.f, qy0 = 0.f, qy1 = 0.f, qy2 = 0.f;
+        float qz0 = 0.f, qz1 = 0.f, qz2 = 0.f;
+        float xa = 0.f, xb = 0.f, xk = 1.f, xah = 0.f, xbh = 0.f, xkh = 1.f;
+        float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
+        if (hx) {
+          qx0 = s.m.x[0][mxi]; qx1 = s.m.x[1][mxi]; qx2 = s.m.x[2][mxi];
+          xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
+          xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
+        }
+        if (hy) {
+          qy0 = s.m.y[0][myi]; qy1 = s.m.y[1][myi]; qy2 = s.m.y[2][myi];
+          ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
+          yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
+        }
+        if (zs) { qz0 = s.m.z[0][mzi]; qz1 = s.m.z[1][mzi]; qz2 = s.m.z[2][mzi]; }
+        // psi(n+1) = b psi(n) + a d ; d' = d / K + psi(n+1) (3D:846-852 and
+        // the other sweeps); unchanged where the component is not updated
+        auto psi = [&](float d, bool upd, float old, float* mB, long long mi, float a_, float b_, float k_) {
           const float nw = upd ? b_ * old + a_ * d : old;
           if (st) mB[mi] = nw;
           return d * k_ + nw;
         };
-        const long long mxi = mxp + (long long)j * wx + sx;
-        const long long myi = myp + (long long)sy * px + i;
-        const long long mzi = mzp + (long long)j * px + i;
+        const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
         if (comps & 1) {  // sigma_xx, yy, zz: k = 2..NZ, j = 2..NY, i = 1..NX-1 (3D:836-863)
           float d1 = (VX0[b + 1] - vxc) * s.odx;
           float d2 = (vyc - VY0[b - BX]) * s.ody;
           float d3 = (vzc - VZm[b]) * s.odz;
           const bool upd = !edge || (m >= 1 && j >= 1 && i <= nx - 2);
-          if (xs_tile && sx >= 0)
-            d1 = psi(d1, upd, s.m.x[0], s.mb.x[0], mxi, __ldg(s.ax.ah + i), __ldg(s.ax.bh + i), __ldg(s.ax.ikh + i));
-          if (ys_tile && sy >= 0)
-            d2 = psi(d2, upd, s.m.y[1], s.mb.y[1], myi, __ldg(s.ay.a + j), __ldg(s.ay.b + j), __ldg(s.ay.ik + j));
-          if (zs) d3 = psi(d3, upd, s.m.z[2], s.mb.z[2], mzi, za, zb, zk);
+          if (hx) d1 = psi(d1, upd, qx0, s.mb.x[0], mxi, xah, xbh, xkh);
+          if (hy) d2 = psi(d2, upd, qy1, s.mb.y[1], myi, ya, yb, yk);
+          if (zs) d3 = psi(d3, upd, qz2, s.mb.z[2], mzi, za, zb, zk);
           float dl = s.dt_lam, dl2m = s.dt_l2m;
           if (HET) {
             const float lh = 0.5f * (Lm[b + 1] + Lm[b]);
@@ -399,10 +383,8 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
           float d1 = (vyc - VY0[b - 1]) * s.odx;
           float d2 = (VX0[b + BX] - vxc) * s.ody;
           const bool upd = !edge || (j <= ny - 2 && i >= 1);
-          if (xs_tile && sx >= 0)
-            d1 = psi(d1, upd, s.m.x[1], s.mb.x[1], mxi, __ldg(s.ax.a + i), __ldg(s.ax.b + i), __ldg(s.ax.ik + i));
-          if (ys_tile && sy >= 0)
-            d2 = psi(d2, upd, s.m.y[0], s.mb.y[0], myi, __ldg(s.ay.ah + j), __ldg(s.ay.bh + j), __ldg(s.ay.ikh + j));
+          if (hx) d1 = psi(d1, upd, qx1, s.mb.x[1], mxi, xa, xb, xk);
+          if (hy) d2 = psi(d2, upd, qy0, s.mb.y[0], myi, yah, ybh, ykh);
           const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
           const float o = SO[3 * SLOT + b];
           const float n = upd ? o + dm * (d1 + d2) : o;
@@ -413,9 +395,8 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
           float d1 = (vzc - VZ0[b - 1]) * s.odx;
           float d2 = (VX1[b] - vxc) * s.odz;
           const bool upd = !edge || (m <= nz - 2 && i >= 1);
-          if (xs_tile && sx >= 0)
-            d1 = psi(d1, upd, s.m.x[2], s.mb.x[2], mxi, __ldg(s.ax.a + i), __ldg(s.ax.b + i), __ldg(s.ax.ik + i));
-          if (zs) d2 = psi(d2, upd, s.m.z[0], s.mb.z[0], mzi, zah, zbh, zkh);
+          if (hx) d1 = psi(d1, upd, qx2, s.mb.x[2], mxi, xa, xb, xk);
+          if (zs) d2 = psi(d2, upd, qz0, s.mb.z[0], mzi, zah, zbh, zkh);
           const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
           const float o = SO[4 * SLOT + b];
           const float n = upd ? o + dm * (d1 + d2) : o;
@@ -426,9 +407,8 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
           float d1 = (VZ0[b + BX] - vzc) * s.ody;
           float d2 = (VY1[b] - vyc) * s.odz;
           const bool upd = !edge || (m <= nz - 2 && j <= ny - 2);
-          if (ys_tile && sy >= 0)
-            d1 = psi(d1, upd, s.m.y[2], s.mb.y[2], myi, __ldg(s.ay.ah + j), __ldg(s.ay.bh + j), __ldg(s.ay.ikh + j));
-          if (zs) d2 = psi(d2, upd, s.m.z[1], s.mb.z[1], mzi, zah, zbh, zkh);
+          if (hy) d1 = psi(d1, upd, qy2, s.mb.y[2], myi, yah, ybh, ykh);
+          if (zs) d2 = psi(d2, upd, qz1, s.mb.z[1], mzi, zah, zbh, zkh);
           float dm = s.dt_mu;
           if (HET) {  // 8-point average at (i+1/2, j+1/2, k+1/2); i+1 clamped on the last column
             const int di = (i < nx - 1) ? 1 : 0;
@@ -453,14 +433,13 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
       if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false);
     }
     __syncthreads();
-    // The boxes of g(m+2) go into slots whose last reader was stress(m)
-    // (velocities of the own cells travel in registers), so they can be
-    // requested before the velocity sweep.
+    // g(m+2) goes into slots whose last reader was stress(m) (own-cell
+    // velocities travel in registers), so it is requested before velocity.
     if (tid == 0 && m + 2 <= ke) issue_group(m + 2, &bar[use & 1], false);
 
     // ======================= velocity at plane p = m - 1 ====================
     const int p = m - 1;
-    if (p >= kb && p < ke && fast_xy && p >= 1 && p <= nz - 2 && s.az.slab(p) < 0) {
+    if (p >= kb && p < ke) {
       const float* Sxx = r_sxx + (p & 1) * REG;
       const float* Syy = r_syy + (p & 1) * REG;
       const float* Sxy = r_sxy + (p & 1) * REG;
@@ -471,151 +450,155 @@ __global__ void __launch_bounds__(FNT, TY == 8 ? 3 : 2)
       const float* Syz0 = r_syz + (p & 3) * REG;
       const float* Syzm = r_syz + ((p - 1) & 3) * REG;
       const bool e_z = p >= n0 && p < nz - n0;
-      const long long cpl = (long long)p * pl + (long long)j0 * px + i0;
+      if (FAST) {
+        const long long cpl = (long long)p * pl + (long long)j0 * px + i0;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        const int r = r_own + q * 8 * RX;
-        const long long c = cpl + (long long)(ty + 8 * q) * px + tx;
-        const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
-        const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
-        float vx = cvx[q] + s.dt_over_rho * (((sxx - Sxx[r - 1]) * s.odx + (sxy - Sxy[r - RX]) * s.ody) +
-                                             (sxz - Sxzm[r]) * s.odz);
-        float vy = cvy[q] + s.dt_over_rho * (((Sxy[r + 1] - sxy) * s.odx + (Syy[r + RX] - syy) * s.ody) +
-                                             (syz - Syzm[r]) * s.odz);
-        const float vz = cvz[q] + s.dt_over_rho * (((Sxz0[r + 1] - sxz) * s.odx + (syz - Syz0[r - RX]) * s.ody) +
-                                                   (Szz1[r] - szz) * s.odz);
-        if (has_src && p == s.ksrc && oi == s.isrc && oj[q] == s.jsrc) {
-          vx += src_x;
-          vy += src_y;
-        }
-        s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
-        const float v2 = vx * vx + vy * vy + vz * vz;
-        vm2 = fmaxf(vm2, v2);
-        bad |= not_finite(v2);
-        if (e_z) {
-          ek.add(s.half_rho * v2);
-          const float exx = s.e_c1 * sxx - s.e_c2 * (syy + szz);
-          const float eyy = s.e_c1 * syy - s.e_c2 * (sxx + szz);
-          const float third = s.ep_physical ? (s.e_c1 * szz - s.e_c2 * (sxx + syy)) * szz : eyy * syy;
-          ep.add(0.5f * (exx * sxx + eyy * syy + third) + s.inv_2mu * (sxy * sxy + sxz * sxz + syz * syz));
-        }
-      }
-    } else if (p >= kb && p < ke) {
-      const float* R0 = rhs + (p & 3) * SLOT;
-      const float* R1 = rhs + ((p + 1) & 3) * SLOT;
-      const float* Sxx = r_sxx + (p & 1) * REG;
-      const float* Syy = r_syy + (p & 1) * REG;
-      const float* Sxy = r_sxy + (p & 1) * REG;
-      const float* Szz0 = r_szz + (p & 1) * REG;
-      const float* Szz1 = r_szz + ((p + 1) & 1) * REG;
-      const float* Sxz0 = r_sxz + (p & 3) * REG;
-      const float* Sxzm = r_sxz + ((p - 1) & 3) * REG;
-      const float* Syz0 = r_syz + (p & 3) * REG;
-      const float* Syzm = r_syz + ((p - 1) & 3) * REG;
-      const bool edge = edge_tile || p < 1 || p > nz - 2;
-      const bool e_z = p >= n0 && p < nz - n0;
-      const int sz = s.az.slab(p);
-      const bool zs = sz >= 0;
-      float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
-      if (zs) {
-        za = __ldg(s.az.a + p); zb = __ldg(s.az.b + p); zk = __ldg(s.az.ik + p);
-        zah = __ldg(s.az.ah + p); zbh = __ldg(s.az.bh + p); zkh = __ldg(s.az.ikh + p);
-      }
-      const long long mxp = (long long)p * ny * wx;
-      const long long myp = (long long)p * wy * px;
-      const long long mzp = (long long)sz * ny * px;
-      const long long cpl = (long long)p * pl;
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        if (!ov[q]) continue;
-        const int i = oi, j = oj[q];
-        const int b = b_own + q * 8 * BX, r = r_own + q * 8 * RX;
-        const long long c = cpl + (long long)j * px + i;
-        const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
-        const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
-        float d1 = (sxx - Sxx[r - 1]) * s.odx;   // v_x (3D:976-993)
-        float d2 = (sxy - Sxy[r - RX]) * s.ody;
-        float d3 = (sxz - Sxzm[r]) * s.odz;
-        float e1 = (Sxy[r + 1] - sxy) * s.odx;   // v_y (3D:995-1014)
-        float e2 = (Syy[r + RX] - syy) * s.ody;
-        float e3 = (syz - Syzm[r]) * s.odz;
-        float f1 = (Sxz0[r + 1] - sxz) * s.odx;  // v_z (3D:1031-1052)
-        float f2 = (syz - Syz0[r - RX]) * s.ody;
-        float f3 = (Szz1[r] - szz) * s.odz;
-        const bool ux = !edge || (p >= 1 && j >= 1 && i >= 1);
-        const bool uy = !edge || (p >= 1 && j <= ny - 2 && i <= nx - 2);
-        const bool uz = !edge || (p <= nz - 2 && j >= 1 && i <= nx - 2);
-        // in-place memory variables of the velocity sweep (only the owner
-        // touches them): updated where the component is
-        auto psi = [&](float d, bool upd, float* mm, long long mi, float a_, float b_, float k_) {
-          float nw = mm[mi];
-          if (upd) { nw = b_ * nw + a_ * d; mm[mi] = nw; }
-          return d * k_ + nw;
-        };
-        if (xs_tile && osx >= 0) {
-          const long long mi = mxp + (long long)j * wx + osx;
-          const float a_ = __ldg(s.ax.a + i), b_ = __ldg(s.ax.b + i), k_ = __ldg(s.ax.ik + i);
-          const float ah_ = __ldg(s.ax.ah + i), bh_ = __ldg(s.ax.bh + i), kh_ = __ldg(s.ax.ikh + i);
-          d1 = psi(d1, ux, s.m.x[3], mi, a_, b_, k_);
-          e1 = psi(e1, uy, s.m.x[4], mi, ah_, bh_, kh_);
-          f1 = psi(f1, uz, s.m.x[5], mi, ah_, bh_, kh_);
-        }
-        if (ys_tile && osy[q] >= 0) {
-          const long long mi = myp + (long long)osy[q] * px + i;
-          const float a_ = __ldg(s.ay.a + j), b_ = __ldg(s.ay.b + j), k_ = __ldg(s.ay.ik + j);
-          const float ah_ = __ldg(s.ay.ah + j), bh_ = __ldg(s.ay.bh + j), kh_ = __ldg(s.ay.ikh + j);
-          d2 = psi(d2, ux, s.m.y[3], mi, a_, b_, k_);
-          e2 = psi(e2, uy, s.m.y[4], mi, ah_, bh_, kh_);
-          f2 = psi(f2, uz, s.m.y[5], mi, a_, b_, k_);
-        }
-        if (zs) {
-          const long long mi = mzp + (long long)j * px + i;
-          d3 = psi(d3, ux, s.m.z[3], mi, za, zb, zk);
-          e3 = psi(e3, uy, s.m.z[4], mi, za, zb, zk);
-          f3 = psi(f3, uz, s.m.z[5], mi, zah, zbh, zkh);
-        }
-        float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
-        if (HET) {
-          fx = s.dt / R0[b];
-          fy = s.dt / (0.25f * (R0[b] + R0[b + 1] + R0[b + 1 + BX] + R0[b + BX]));
-          fz = s.dt / (0.25f * (R0[b] + R0[b + 1] + R1[b + 1] + R1[b]));
-        }
-        const float ox = cvx[q], oy = cvy[q], oz = cvz[q];
-        float vx = ox + fx * (d1 + d2 + d3);
-        float vy = oy + fy * (e1 + e2 + e3);
-        float vz = oz + fz * (f1 + f2 + f3);
-        if (edge) {
-          if (!ux) vx = ox;
-          if (!uy) vy = oy;
-          if (!uz) vz = oz;
-        }
-        if (has_src && p == s.ksrc && i == s.isrc && j == s.jsrc) {  // 3D:1080-1081
-          vx += src_x;
-          vy += src_y;
-        }
-        if (edge && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || p == 0 || p == nz - 1)) {
-          vx = 0.f; vy = 0.f; vz = 0.f;  // rigid faces (3D:1087-1121)
-        }
-        s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
-        const float v2 = vx * vx + vy * vy + vz * vz;
-        vm2 = fmaxf(vm2, v2);
-        bad |= not_finite(v2);
-        if (e_z && oe[q]) {  // energy interior (3D:1136-1143)
-          float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
-          if (HET) {
-            const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
-            const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
-            hr = 0.5f * R0[b];
-            c1 = 2.0f * (l + mu) * den;
-            c2 = l * den;
-            i2m = 1.0f / (2.0f * mu);
+        for (int q = 0; q < NQ; ++q) {
+          const int r = r_own + q * 8 * RX;
+          const long long c = cpl + (long long)(ty + 8 * q) * px + tx;
+          const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
+          const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
+          float vx = cvx[q] + s.dt_over_rho * (((sxx - Sxx[r - 1]) * s.odx + (sxy - Sxy[r - RX]) * s.ody) +
+                                               (sxz - Sxzm[r]) * s.odz);
+          float vy = cvy[q] + s.dt_over_rho * (((Sxy[r + 1] - sxy) * s.odx + (Syy[r + RX] - syy) * s.ody) +
+                                               (syz - Syzm[r]) * s.odz);
+          const float vz = cvz[q] + s.dt_over_rho * (((Sxz0[r + 1] - sxz) * s.odx + (syz - Syz0[r - RX]) * s.ody) +
+                                                     (Szz1[r] - szz) * s.odz);
+          if (has_src && p == s.ksrc && oi == s.isrc && oj[q] == s.jsrc) {
+            vx += src_x;
+            vy += src_y;
           }
-          ek.add(hr * v2);
-          const float exx = c1 * sxx - c2 * (syy + szz);
-          const float eyy = c1 * syy - c2 * (sxx + szz);
-          // the reference adds eps_yy*sigma_yy twice and no zz term (3D:1170-1171)
-          const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
-          ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
+          s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
+          const float v2 = vx * vx + vy * vy + vz * vz;
+          vm2 = fmaxf(vm2, v2);
+          bad |= not_finite(v2);
+          if (e_z) {
+            ek.add(s.half_rho * v2);
+            const float exx = s.e_c1 * sxx - s.e_c2 * (syy + szz);
+            const float eyy = s.e_c1 * syy - s.e_c2 * (sxx + szz);
+            const float third = s.ep_physical ? (s.e_c1 * szz - s.e_c2 * (sxx + syy)) * szz : eyy * syy;
+            ep.add(0.5f * (exx * sxx + eyy * syy + third) + s.inv_2mu * (sxy * sxy + sxz * sxz + syz * syz));
+          }
+        }
+      } else {
+        const float* R0 = rhs + (p & 3) * SLOT;
+        const float* R1 = rhs + ((p + 1) & 3) * SLOT;
+        const bool edge = edge_tile || p < 1 || p > nz - 2;
+        const int sz = s.az.slab(p);
+        const bool zs = sz >= 0;
+        float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
+        if (zs) {
+          za = __ldg(s.az.a + p); zb = __ldg(s.az.b + p); zk = __ldg(s.az.ik + p);
+          zah = __ldg(s.az.ah + p); zbh = __ldg(s.az.bh + p); zkh = __ldg(s.az.ikh + p);
+        }
+        const long long mxp = (long long)p * ny * wx;
+        const long long myp = (long long)p * wy * px;
+        const long long mzp = (long long)sz * ny * px;
+        const long long cpl = (long long)p * pl;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          if (!ov[q]) continue;
+          const int i = oi, j = oj[q];
+          const int b = b_own + q * 8 * BX, r = r_own + q * 8 * RX;
+          const long long c = cpl + (long long)j * px + i;
+          const bool hx = xs_tile && osx >= 0, hy = ys_tile && osy[q] >= 0;
+          const long long mxi = mxp + (long long)j * wx + osx;
+          const long long myi = myp + (long long)osy[q] * px + i;
+          const long long mzi = mzp + (long long)j * px + i;
+          // the velocity sweep's memory variables and coefficients, issued together
+          float qx3 = 0.f, qx4 = 0.f, qx5 = 0.f, qy3 = 0.f, qy4 = 0.f, qy5 = 0.f;
+          float qz3 = 0.f, qz4 = 0.f, qz5 = 0.f;
+          float xa = 0.f, xb = 0.f, xk = 1.f, xah = 0.f, xbh = 0.f, xkh = 1.f;
+          float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
+          if (hx) {
+            qx3 = s.m.x[3][mxi]; qx4 = s.m.x[4][mxi]; qx5 = s.m.x[5][mxi];
+            xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
+            xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
+          }
+          if (hy) {
+            qy3 = s.m.y[3][myi]; qy4 = s.m.y[4][myi]; qy5 = s.m.y[5][myi];
+            ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
+            yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
+          }
+          if (zs) { qz3 = s.m.z[3][mzi]; qz4 = s.m.z[4][mzi]; qz5 = s.m.z[5][mzi]; }
+          const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
+          const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
+          float d1 = (sxx - Sxx[r - 1]) * s.odx;   // v_x (3D:976-993)
+          float d2 = (sxy - Sxy[r - RX]) * s.ody;
+          float d3 = (sxz - Sxzm[r]) * s.odz;
+          float e1 = (Sxy[r + 1] - sxy) * s.odx;   // v_y (3D:995-1014)
+          float e2 = (Syy[r + RX] - syy) * s.ody;
+          float e3 = (syz - Syzm[r]) * s.odz;
+          float f1 = (Sxz0[r + 1] - sxz) * s.odx;  // v_z (3D:1031-1052)
+          float f2 = (syz - Syz0[r - RX]) * s.ody;
+          float f3 = (Szz1[r] - szz) * s.odz;
+          const bool ux = !edge || (p >= 1 && j >= 1 && i >= 1);
+          const bool uy = !edge || (p >= 1 && j <= ny - 2 && i <= nx - 2);
+          const bool uz = !edge || (p <= nz - 2 && j >= 1 && i <= nx - 2);
+          // in place: updated where the component is (3D:979-985 and the like)
+          auto psi = [&](float d, bool upd, float old, float* mm, long long mi, float a_, float b_, float k_) {
+            float nw = old;
+            if (upd) { nw = b_ * old + a_ * d; mm[mi] = nw; }
+            return d * k_ + nw;
+          };
+          if (hx) {
+            d1 = psi(d1, ux, qx3, s.m.x[3], mxi, xa, xb, xk);
+            e1 = psi(e1, uy, qx4, s.m.x[4], mxi, xah, xbh, xkh);
+            f1 = psi(f1, uz, qx5, s.m.x[5], mxi, xah, xbh, xkh);
+          }
+          if (hy) {
+            d2 = psi(d2, ux, qy3, s.m.y[3], myi, ya, yb, yk);
+            e2 = psi(e2, uy, qy4, s.m.y[4], myi, yah, ybh, ykh);
+            f2 = psi(f2, uz, qy5, s.m.y[5], myi, ya, yb, yk);
+          }
+          if (zs) {
+            d3 = psi(d3, ux, qz3, s.m.z[3], mzi, za, zb, zk);
+            e3 = psi(e3, uy, qz4, s.m.z[4], mzi, za, zb, zk);
+            f3 = psi(f3, uz, qz5, s.m.z[5], mzi, zah, zbh, zkh);
+          }
+          float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
+          if (HET) {
+            fx = s.dt / R0[b];
+            fy = s.dt / (0.25f * (R0[b] + R0[b + 1] + R0[b + 1 + BX] + R0[b + BX]));
+            fz = s.dt / (0.25f * (R0[b] + R0[b + 1] + R1[b + 1] + R1[b]));
+          }
+          const float ox = cvx[q], oy = cvy[q], oz = cvz[q];
+          float vx = ox + fx * (d1 + d2 + d3);
+          float vy = oy + fy * (e1 + e2 + e3);
+          float vz = oz + fz * (f1 + f2 + f3);
+          if (edge) {
+            if (!ux) vx = ox;
+            if (!uy) vy = oy;
+            if (!uz) vz = oz;
+          }
+          if (has_src && p == s.ksrc && i == s.isrc && j == s.jsrc) {  // 3D:1080-1081
+            vx += src_x;
+            vy += src_y;
+          }
+          if (edge && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || p == 0 || p == nz - 1)) {
+            vx = 0.f; vy = 0.f; vz = 0.f;  // rigid faces (3D:1087-1121)
+          }
+          s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
+          const float v2 = vx * vx + vy * vy + vz * vz;
+          vm2 = fmaxf(vm2, v2);
+          bad |= not_finite(v2);
+          if (e_z && oe[q]) {  // energy interior (3D:1136-1143)
+            float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
+            if (HET) {
+              const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
+              const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
+              hr = 0.5f * R0[b];
+              c1 = 2.0f * (l + mu) * den;
+              c2 = l * den;
+              i2m = 1.0f / (2.0f * mu);
+            }
+            ek.add(hr * v2);
+            const float exx = c1 * sxx - c2 * (syy + szz);
+            const float eyy = c1 * syy - c2 * (sxx + szz);
+            // the reference adds eps_yy*sigma_yy twice and no zz term (3D:1170-1171)
+            const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
+            ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
+          }
         }
       }
     }
@@ -674,45 +657,97 @@ static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, 
   return r == CUDA_SUCCESS;
 }
 
-template <int TY, int D, bool HET>
+template <int TY, bool FAST, bool HET>
 static cudaError_t set_smem_attr() {
-  return cudaFuncSetAttribute(fused3d_kernel<TY, D, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)Geo<TY, D, HET>::SMEM);
+  return cudaFuncSetAttribute(fused3d_kernel<TY, FAST, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)Geo<TY, HET>::SMEM);
 }
-
-// Instantiated launch shapes: (tile rows, prefetch depth).
-#define CPML_FUSED_SHAPES(X) X(8, 2) X(16, 2)
 
 struct FusedPlan {
   TmapSet maps[2];  // maps[q] reads buffer set q
   int ty, lz, depth;
   bool het;
+  const int4* items_fast;  // device item lists
+  const int4* items_gen;
+  int n_fast, n_gen;
+  cudaStream_t aux;        // second stream of the fork/join
+  cudaEvent_t fork, join;
 };
 
-static cudaError_t set_attr_for(int ty, int d, bool het) {
-#define X(T, DD) \
-  if (ty == T && d == DD) return het ? set_smem_attr<T, DD, true>() : set_smem_attr<T, DD, false>();
-  CPML_FUSED_SHAPES(X)
-#undef X
+static cudaError_t set_attr_for(int ty, bool het) {
+  cudaError_t e;
+  if (ty == 8) {
+    if ((e = set_smem_attr<8, true, false>()) != cudaSuccess) return e;
+    return het ? set_smem_attr<8, false, true>() : set_smem_attr<8, false, false>();
+  }
+  if (ty == 16) {
+    if ((e = set_smem_attr<16, true, false>()) != cudaSuccess) return e;
+    return het ? set_smem_attr<16, false, true>() : set_smem_attr<16, false, false>();
+  }
   return cudaErrorInvalidValue;
 }
 
-bool fused3d_shape_ok(int ty, int d) {
-#define X(T, DD) \
-  if (ty == T && d == DD) return true;
-  CPML_FUSED_SHAPES(X)
-#undef X
-  return false;
-}
+bool fused3d_shape_ok(int ty, int d) { return (ty == 8 || ty == 16) && d == 2; }
 
 bool fused3d_supported() { return encode_fn() != nullptr; }
 
 size_t fused3d_smem(int ty, int d, bool het) {
-#define X(T, DD) \
-  if (ty == T && d == DD) return het ? Geo<T, DD, true>::SMEM : Geo<T, DD, false>::SMEM;
-  CPML_FUSED_SHAPES(X)
-#undef X
-  return 0;
+  (void)d;
+  if (ty == 8) return het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
+  return het ? Geo<16, true>::SMEM : Geo<16, false>::SMEM;
+}
+
+// Work items of one step: every (tile, z-chunk). A chunk is interior when its
+// tile plus halo avoids every x/y slab, face and the energy boundary, and all
+// its stress planes kb-1..ke avoid the z slabs and the z faces. Interior
+// chunks are cut from the planes [zi0 + 1, zi1 - 1); the rest of each
+// column, and every other tile, is general. The z-chunk is the outermost
+// loop so concurrently resident CTAs share their halos in L2.
+void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const Axis& az, int npml,
+                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen) {
+  fast.clear();
+  gen.clear();
+  const int ntx = (nx + FTX - 1) / FTX, nty = (ny + ty - 1) / ty;
+  const int zi0 = az.lo > 1 ? az.lo : 1;                              // first interior plane
+  const int zi1 = (nz - az.hi) < (nz - 1) ? (nz - az.hi) : (nz - 1);  // one past the last
+  const int f0 = zi0 + 1, f1 = zi1 - 1;
+  auto chunks = [&](int a, int b, std::vector<int2>& out) {
+    if (b <= a) return;
+    const int n = (b - a + lz - 1) / lz;
+    for (int q = 0; q < n; ++q) {
+      const int k0 = a + (int)((long long)(b - a) * q / n);
+      const int k1 = a + (int)((long long)(b - a) * (q + 1) / n);
+      if (k1 > k0) out.push_back(make_int2(k0, k1));
+    }
+  };
+  auto interior_tile = [&](int i0, int j0) {
+    const bool xs = ax.width() > 0 && (i0 - 1 < ax.lo || i0 + FTX >= nx - ax.hi);
+    const bool ys = ay.width() > 0 && (j0 - 1 < ay.lo || j0 + ty >= ny - ay.hi);
+    const bool edge = i0 - 1 < 1 || i0 + FTX > nx - 2 || j0 - 1 < 1 || j0 + ty > ny - 2;
+    const bool efull = i0 >= npml && i0 + FTX <= nx - npml && j0 >= npml && j0 + ty <= ny - npml;
+    return !het && !xs && !ys && !edge && efull;
+  };
+  const bool has_inner = f1 > f0;
+  std::vector<int2> all, inner, outer;
+  chunks(0, nz, all);
+  if (has_inner) {
+    chunks(f0, f1, inner);
+    chunks(0, f0, outer);
+    chunks(f1, nz, outer);
+  }
+  for (const int2& z : inner)
+    for (int tyi = 0; tyi < nty; ++tyi)
+      for (int txi = 0; txi < ntx; ++txi)
+        if (interior_tile(txi * FTX, tyi * ty)) fast.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+  for (const int2& z : all)
+    for (int tyi = 0; tyi < nty; ++tyi)
+      for (int txi = 0; txi < ntx; ++txi)
+        if (!has_inner || !interior_tile(txi * FTX, tyi * ty))
+          gen.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+  for (const int2& z : outer)
+    for (int tyi = 0; tyi < nty; ++tyi)
+      for (int txi = 0; txi < ntx; ++txi)
+        if (interior_tile(txi * FTX, tyi * ty)) gen.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
 }
 
 // Build the tensor maps of both buffer sets. fields[q][f] = field f of set q.
@@ -723,7 +758,7 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
   P->ty = ty; P->lz = lz; P->depth = depth; P->het = het;
   // opt in to the dynamic shared memory once per configuration, outside any
   // stream capture
-  if (set_attr_for(ty, depth, het) != cudaSuccess) return false;
+  if (set_attr_for(ty, het) != cudaSuccess) return false;
   for (int q = 0; q < 2; ++q) {
     for (int f = 0; f < 9; ++f)
       if (!make_map(&P->maps[q].f[f], fields[q][f], nx, ny, nz, px, ty)) return false;
@@ -740,29 +775,49 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
   return true;
 }
 
-size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
-
-dim3 fused3d_grid(int nx, int ny, int nz, int ty, int lz) {
-  const int ntx = (nx + FTX - 1) / FTX, nty = (ny + ty - 1) / ty, nkz = (nz + lz - 1) / lz;
-  return dim3(ntx, nty * nkz, 1);
+void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, int n_gen,
+                       cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
+  FusedPlan* P = static_cast<FusedPlan*>(plan_mem);
+  P->items_fast = fast; P->n_fast = n_fast;
+  P->items_gen = gen; P->n_gen = n_gen;
+  P->aux = aux; P->fork = fork; P->join = join;
 }
 
-template <int TY, int D, bool HET>
+size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
+
+template <int TY>
 static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
-  using G = Geo<TY, D, HET>;
-  const dim3 g = fused3d_grid(s.nx, s.ny, s.nz, TY, P->lz);
-  fused3d_kernel<TY, D, HET><<<g, FNT, G::SMEM, st>>>(P->maps[parity], s, ls, P->lz);
+  const size_t smf = Geo<TY, false>::SMEM, smg = P->het ? Geo<TY, true>::SMEM : Geo<TY, false>::SMEM;
+  // the general items run on the auxiliary stream, concurrently with the
+  // interior items; exactly one of the two kernels records the receivers
+  const bool both = P->n_fast > 0 && P->n_gen > 0;
+  if (both) {
+    cudaEventRecord(P->fork, st);
+    cudaStreamWaitEvent(P->aux, P->fork, 0);
+  }
+  cudaStream_t sg = both ? P->aux : st;
+  if (P->n_gen > 0) {
+    if (P->het)
+      fused3d_kernel<TY, false, true><<<P->n_gen, FNT, smg, sg>>>(P->maps[parity], s, ls, P->items_gen,
+                                                                   P->n_fast, 1);
+    else
+      fused3d_kernel<TY, false, false><<<P->n_gen, FNT, smg, sg>>>(P->maps[parity], s, ls, P->items_gen,
+                                                                    P->n_fast, 1);
+  }
+  if (P->n_fast > 0)
+    fused3d_kernel<TY, true, false><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
+                                                                  P->n_gen > 0 ? 0 : 1);
+  if (both) {
+    cudaEventRecord(P->join, P->aux);
+    cudaStreamWaitEvent(st, P->join, 0);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st) {
   const FusedPlan* P = static_cast<const FusedPlan*>(plan_mem);
-#define X(T, DD)                                                            \
-  if (P->ty == T && P->depth == DD)                                         \
-    return P->het ? launch_t<T, DD, true>(P, s, ls, parity, st)             \
-                  : launch_t<T, DD, false>(P, s, ls, parity, st);
-  CPML_FUSED_SHAPES(X)
-#undef X
+  if (P->ty == 8) return launch_t<8>(P, s, ls, parity, st);
+  if (P->ty == 16) return launch_t<16>(P, s, ls, parity, st);
   return cudaErrorInvalidValue;
 }
 
