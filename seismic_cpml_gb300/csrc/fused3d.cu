@@ -109,7 +109,7 @@ struct Geo {
 };
 
 template <int TY, bool FAST, bool HET>
-__global__ void __launch_bounds__(FNT, FAST ? 3 : 2)
+__global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
     fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls,
                    const int4* __restrict__ items, int item_base, int record) {
   static_assert(!(FAST && HET), "the interior kernel is homogeneous only");
@@ -664,7 +664,8 @@ static cudaError_t set_smem_attr() {
 }
 
 struct FusedPlan {
-  TmapSet maps[2];  // maps[q] reads buffer set q
+  TmapSet maps[2];  // maps[q] reads buffer set q (interior kernel, ty-row boxes)
+  TmapSet gmaps[2]; // the same for the general kernel's 8-row boxes
   int ty, lz, depth;
   bool het;
   const int4* items_fast;  // device item lists
@@ -735,19 +736,24 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
     chunks(0, f0, outer);
     chunks(f1, nz, outer);
   }
+  // Interior tiles have ty rows; the general kernel always uses 8-row tiles
+  // (a smaller footprint gives it three CTAs per SM), which split every
+  // ty-row tile exactly.
   for (const int2& z : inner)
     for (int tyi = 0; tyi < nty; ++tyi)
       for (int txi = 0; txi < ntx; ++txi)
         if (interior_tile(txi * FTX, tyi * ty)) fast.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+  auto add_gen = [&](int i0, int j0, const int2& z) {
+    for (int jj = j0; jj < j0 + ty && jj < ny; jj += 8) gen.push_back(make_int4(i0, jj, z.x, z.y));
+  };
   for (const int2& z : all)
     for (int tyi = 0; tyi < nty; ++tyi)
       for (int txi = 0; txi < ntx; ++txi)
-        if (!has_inner || !interior_tile(txi * FTX, tyi * ty))
-          gen.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+        if (!has_inner || !interior_tile(txi * FTX, tyi * ty)) add_gen(txi * FTX, tyi * ty, z);
   for (const int2& z : outer)
     for (int tyi = 0; tyi < nty; ++tyi)
       for (int txi = 0; txi < ntx; ++txi)
-        if (interior_tile(txi * FTX, tyi * ty)) gen.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+        if (interior_tile(txi * FTX, tyi * ty)) add_gen(txi * FTX, tyi * ty, z);
 }
 
 // Build the tensor maps of both buffer sets. fields[q][f] = field f of set q.
@@ -758,20 +764,23 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
   P->ty = ty; P->lz = lz; P->depth = depth; P->het = het;
   // opt in to the dynamic shared memory once per configuration, outside any
   // stream capture
-  if (set_attr_for(ty, het) != cudaSuccess) return false;
-  for (int q = 0; q < 2; ++q) {
-    for (int f = 0; f < 9; ++f)
-      if (!make_map(&P->maps[q].f[f], fields[q][f], nx, ny, nz, px, ty)) return false;
-    if (het) {
-      if (!make_map(&P->maps[q].lam, lam, nx, ny, nz, px, ty)) return false;
-      if (!make_map(&P->maps[q].mu, mu, nx, ny, nz, px, ty)) return false;
-      if (!make_map(&P->maps[q].rho, rho, nx, ny, nz, px, ty)) return false;
-    } else {
-      P->maps[q].lam = P->maps[q].f[0];
-      P->maps[q].mu = P->maps[q].f[0];
-      P->maps[q].rho = P->maps[q].f[0];
+  if (set_attr_for(ty, het) != cudaSuccess || set_attr_for(8, het) != cudaSuccess) return false;
+  for (int q = 0; q < 2; ++q)
+    for (int pass = 0; pass < 2; ++pass) {
+      TmapSet& M = pass == 0 ? P->maps[q] : P->gmaps[q];
+      const int rows = pass == 0 ? ty : 8;
+      for (int f = 0; f < 9; ++f)
+        if (!make_map(&M.f[f], fields[q][f], nx, ny, nz, px, rows)) return false;
+      if (het) {
+        if (!make_map(&M.lam, lam, nx, ny, nz, px, rows)) return false;
+        if (!make_map(&M.mu, mu, nx, ny, nz, px, rows)) return false;
+        if (!make_map(&M.rho, rho, nx, ny, nz, px, rows)) return false;
+      } else {
+        M.lam = M.f[0];
+        M.mu = M.f[0];
+        M.rho = M.f[0];
+      }
     }
-  }
   return true;
 }
 
@@ -787,7 +796,7 @@ size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
 
 template <int TY>
 static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
-  const size_t smf = Geo<TY, false>::SMEM, smg = P->het ? Geo<TY, true>::SMEM : Geo<TY, false>::SMEM;
+  const size_t smf = Geo<TY, false>::SMEM, smg = P->het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
   // the general items run on the auxiliary stream, concurrently with the
   // interior items; exactly one of the two kernels records the receivers
   const bool both = P->n_fast > 0 && P->n_gen > 0;
@@ -798,11 +807,11 @@ static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int p
   cudaStream_t sg = both ? P->aux : st;
   if (P->n_gen > 0) {
     if (P->het)
-      fused3d_kernel<TY, false, true><<<P->n_gen, FNT, smg, sg>>>(P->maps[parity], s, ls, P->items_gen,
-                                                                   P->n_fast, 1);
+      fused3d_kernel<8, false, true><<<P->n_gen, FNT, smg, sg>>>(P->gmaps[parity], s, ls, P->items_gen,
+                                                                  P->n_fast, 1);
     else
-      fused3d_kernel<TY, false, false><<<P->n_gen, FNT, smg, sg>>>(P->maps[parity], s, ls, P->items_gen,
-                                                                    P->n_fast, 1);
+      fused3d_kernel<8, false, false><<<P->n_gen, FNT, smg, sg>>>(P->gmaps[parity], s, ls, P->items_gen,
+                                                                   P->n_fast, 1);
   }
   if (P->n_fast > 0)
     fused3d_kernel<TY, true, false><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
