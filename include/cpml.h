@@ -196,6 +196,26 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
 void cpml_destroy(cpml_handle* h);
 const char* cpml_strerror(int status);
 
+/* ---- batched 2D shots ---------------------------------------------------
+   Many independent runs of the 2D program (2D:550-735), each with its own
+   grid, model, source, receivers, DELTAT and NSTEP, advanced together in one
+   persistent cooperative kernel launch captured in a CUDA graph. A shot's
+   seismograms and fields are bit-identical to a single-shot handle running
+   the same parameters (same per-cell arithmetic). No counterpart in the
+   reference, which runs one shot per program execution; energy is not
+   recorded by the batched engine. */
+typedef struct cpml_batch cpml_batch;
+int cpml_batch_create(int nshots, const cpml_params* params, cpml_batch** out);
+int cpml_batch_set_model(cpml_batch* b, int shot, const float* lambda, const float* mu,
+                         const float* rho);
+int cpml_batch_set_receivers(cpml_batch* b, int shot, int nrec, const int* ix, const int* iy);
+/* Zero every shot and run each to its own NSTEP. */
+int cpml_batch_run(cpml_batch* b);
+int cpml_batch_get_seismograms(cpml_batch* b, int shot, double* vx, double* vy);
+int cpml_batch_get_field(cpml_batch* b, int shot, int field, float* out);
+int cpml_batch_last_run_ms(cpml_batch* b, double* ms);
+void cpml_batch_destroy(cpml_batch* b);
+
 /* Kinetic and potential energy (the 3D program's formulas, 3D:1131-1180) of
    nine caller-owned FP32 device wavefields, allocating no device memory.
    No counterpart in the reference: it serves callers that cannot allocate

@@ -1,0 +1,85 @@
+"""Python mirror of the batched multi-shot 2D engine (cpml_batch_* in
+include/cpml.h): many independent 2D shots in one persistent launch."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import lib as _L
+from .params import CpmlParams, FIELDS
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class Batch:
+    def __init__(self, params, models=None, receivers=None):
+        self.L = _L.load()
+        self.params = [p.copy() for p in params]
+        arr = (CpmlParams * len(self.params))(*self.params)
+        h = ctypes.c_void_p()
+        _L.check(self.L.cpml_batch_create(len(self.params), arr, ctypes.byref(h)), "cpml_batch_create")
+        self.h = h
+        self.receivers = [[] for _ in self.params]
+        if models is not None:
+            for s, m in enumerate(models):
+                if m is not None:
+                    self.set_model(s, *m)
+        if receivers is not None:
+            for s, r in enumerate(receivers):
+                self.set_receivers(s, r)
+
+    def set_model(self, shot, lam, mu, rho):
+        a = [np.ascontiguousarray(x, dtype=np.float32) for x in (lam, mu, rho)]
+        _L.check(self.L.cpml_batch_set_model(self.h, shot, *[x.ctypes.data_as(_fp) for x in a]),
+                 "cpml_batch_set_model")
+
+    def set_receivers(self, shot, rec):
+        rec = [tuple(int(v) for v in r) for r in rec]
+        ix = np.array([r[0] for r in rec] or [0], np.int32)
+        iy = np.array([r[1] for r in rec] or [0], np.int32)
+        _L.check(self.L.cpml_batch_set_receivers(self.h, shot, len(rec), ix.ctypes.data_as(_ip),
+                                                 iy.ctypes.data_as(_ip)), "cpml_batch_set_receivers")
+        self.receivers[shot] = rec
+
+    def run(self) -> None:
+        _L.check(self.L.cpml_batch_run(self.h), "cpml_batch_run")
+
+    def last_run_ms(self) -> float:
+        v = ctypes.c_double()
+        _L.check(self.L.cpml_batch_last_run_ms(self.h, ctypes.byref(v)))
+        return v.value
+
+    def seismograms(self, shot):
+        n = len(self.receivers[shot])
+        ns = self.params[shot].nstep
+        vx = np.zeros((max(n, 1), ns))
+        vy = np.zeros((max(n, 1), ns))
+        _L.check(self.L.cpml_batch_get_seismograms(self.h, shot, vx.ctypes.data_as(_dp),
+                                                   vy.ctypes.data_as(_dp)))
+        return vx[:n], vy[:n]
+
+    def field(self, shot, name):
+        p = self.params[shot]
+        out = np.zeros((p.ny, p.nx), np.float32)
+        _L.check(self.L.cpml_batch_get_field(self.h, shot, FIELDS[name], out.ctypes.data_as(_fp)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cpml_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcpml.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels2d.cu", "kernels3d.cu", "fused3d.cu", "support.cu", "noalloc.cu",
-           "host.cpp"]
+           "batch2d.cu", "host.cpp"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,552 @@
+// batch2d.cu -- many 2D shots in one persistent launch.
+//
+// Each shot is a complete run of seismic_CPML_2D_isotropic_second_order.f90
+// (its own grid size, model, source, receivers, DELTAT and NSTEP). All shots
+// advance together in ONE cooperative kernel launch (captured in a CUDA
+// graph): per time step a stress phase over every (shot, tile) item of the
+// shots still running, a grid barrier, a velocity phase, a grid barrier. The
+// per-cell arithmetic is the single-shot path's (cell2d.cuh), so a shot's
+// seismograms and fields are bit-identical to running it alone.
+//
+// Shots are scheduled in decreasing NSTEP, so the items active at step t are
+// a prefix of the item table and a finished shot costs nothing. Items are
+// 32 x 8 tiles handed out round-robin over the resident CTAs, so uneven grid
+// sizes balance without a queue. Grid barriers spin with a bound (~2 s) and
+// report CPML_ERR_TIMEOUT instead of hanging.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cpml.h"
+#include "cpml_internal.cuh"
+#include "kutil.cuh"
+#include "cell2d.cuh"
+
+namespace cpml {
+
+struct ProfileArgs {
+  int n, npml, use_min, use_max;
+  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
+};
+void launch_build_profile(const ProfileArgs& P, double* out64, float* out32, cudaStream_t st);
+
+constexpr int BTX = 32, BTY = 8, BNT = BTX * BTY;
+constexpr long long kBarrierCycles = 4000000000LL;
+
+struct BatchArgs {
+  const Shot2D* shots;      // by shot id
+  const int4* items;        // (shot, i0, j0, -) in schedule order
+  const int* items_at;      // [max_nstep] items of the shots running at step t
+  const int* recs_at;       // [max_nstep] receivers of the shots running at step t
+  const int2* rec;          // (shot, padded cell) in schedule order
+  const long long* rec_off; // sample 0 of the receiver's v_x trace in seis
+  const long long* rec_offy;// sample 0 of its v_y trace
+  float* seis;
+  int max_nstep;
+  unsigned* bar;            // [0] arrivals, [1] generation
+  int* err;                 // 2 = barrier gave up, 4 = non-finite velocity
+};
+
+// Bounded grid barrier of a cooperative launch (every CTA is resident).
+__device__ __forceinline__ bool grid_sync(const BatchArgs& a) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* gen = a.bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(a.bar, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      a.bar[0] = 0u;
+      __threadfence();
+      atomicAdd(a.bar + 1, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*gen == g) {
+        if (clock64() - t0 > kBarrierCycles) { atomicOr(a.err, 2); break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*((volatile int*)a.err) & 2) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
+  const int n = a.recs_at[t];
+  for (long long r = (long long)blockIdx.x * BNT + threadIdx.x; r < n; r += (long long)gridDim.x * BNT) {
+    const int2 rc = a.rec[r];
+    const Shot2D& S = a.shots[rc.x];
+    a.seis[a.rec_off[r] + t] = S.vx[rc.y];
+    a.seis[a.rec_offy[r] + t] = S.vy[rc.y];
+  }
+}
+
+__global__ void __launch_bounds__(BNT) batch2d_kernel(BatchArgs a) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int t = 0; t < a.max_nstep; ++t) {
+    if (t > 0) record_batch(a, t - 1);
+    const int n = a.items_at[t];
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+      const int4 itm = a.items[q];
+      const Shot2D& S = a.shots[itm.x];
+      const int i = itm.y + tx, j = itm.z + ty;
+      if (i < S.nx && j < S.ny) {
+        if (S.het) stress2d_cell<true>(S, i, j);
+        else stress2d_cell<false>(S, i, j);
+      }
+    }
+    if (!grid_sync(a)) return;
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+      const int4 itm = a.items[q];
+      const Shot2D& S = a.shots[itm.x];
+      const int i = itm.y + tx, j = itm.z + ty;
+      if (i < S.nx && j < S.ny) {
+        float ek = 0.f, ep = 0.f, vm2 = 0.f;
+        int bad = 0;
+        if (S.het) velocity2d_cell<true>(S, i, j, t + 1, ek, ep, vm2, bad);
+        else velocity2d_cell<false>(S, i, j, t + 1, ek, ep, vm2, bad);
+        if (bad) atomicOr(a.err, 4);
+      }
+    }
+    if (!grid_sync(a)) return;
+  }
+  if (a.max_nstep > 0) record_batch(a, a.max_nstep - 1);
+}
+
+}  // namespace cpml
+
+using namespace cpml;
+
+namespace {
+const double kPi = 3.141592653589793238462643;
+
+double stf(const cpml_params& p, int it) {  // 2D:644-654
+  const double a = kPi * kPi * p.f0 * p.f0;
+  const double tt = double(it - 1) * p.deltat - p.t0;
+  const double tt2 = tt * tt;
+  if (p.stf == CPML_STF_GAUSSIAN) return p.factor * std::exp(-(a * tt2));
+  if (p.stf == CPML_STF_RICKER) return p.factor * (1.0 - 2.0 * a * tt2) * std::exp(-(a * tt2));
+  return -(p.factor * 2.0 * a * tt * std::exp(-(a * tt2)));
+}
+
+struct HostShot {
+  cpml_params p;
+  int px = 0;
+  Shot2D s{};
+  std::vector<int> rec;    // padded cells
+  std::vector<int> recij;  // 1-based pairs
+  double rho_src[2];
+  float* seis = nullptr;   // [2][nrec][nstep]
+  float* model = nullptr;  // [3][px*ny]
+};
+}  // namespace
+
+struct cpml_batch {
+  std::vector<HostShot> shots;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  Shot2D* d_shots = nullptr;
+  int4* d_items = nullptr;
+  int* d_items_at = nullptr;
+  int* d_recs_at = nullptr;
+  int2* d_rec = nullptr;
+  long long* d_rec_off = nullptr;
+  long long* d_rec_offy = nullptr;
+  float* d_seis = nullptr;
+  unsigned* d_bar = nullptr;
+  int* d_err = nullptr;
+  size_t seis_floats = 0;
+  int max_nstep = 0;
+  int grid = 0;
+  bool dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_ok = false;
+  BatchArgs args{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  std::vector<size_t> field_bytes;  // per shot, for reset
+};
+
+namespace {
+#define BCK(x)                                                              \
+  do {                                                                      \
+    cudaError_t e_ = (x);                                                   \
+    if (e_ != cudaSuccess) {                                                \
+      cudaGetLastError();                                                   \
+      return e_ == cudaErrorMemoryAllocation ? CPML_ERR_OOM : CPML_ERR_CUDA; \
+    }                                                                       \
+  } while (0)
+
+template <typename T>
+int balloc(cpml_batch* b, T** out, size_t n) {
+  *out = nullptr;
+  if (n == 0) return CPML_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) { cudaGetLastError(); return e == cudaErrorMemoryAllocation ? CPML_ERR_OOM : CPML_ERR_CUDA; }
+  b->allocs.push_back(p);
+  *out = (T*)p;
+  return CPML_OK;
+}
+
+// FP64 profile of one axis on the GPU, slab extents from its a / a_half.
+int shot_axis(cpml_batch* b, const cpml_params& p, int axis, int n, double delta, Axis* A) {
+  ProfileArgs P{};
+  P.n = n; P.npml = p.npoints_pml; P.use_min = p.use_pml[2 * axis]; P.use_max = p.use_pml[2 * axis + 1];
+  P.delta = delta; P.cp = p.cp; P.f0 = p.f0; P.dt = p.deltat; P.npower = p.npower; P.kmax = p.k_max_pml;
+  P.amax = p.alpha_max_pml < 0 ? 2.0 * kPi * (p.f0 / 2.0) : p.alpha_max_pml;
+  P.rcoef = p.rcoef;
+  double* d64 = nullptr;
+  float* d32 = nullptr;
+  int st;
+  if ((st = balloc(b, &d64, size_t(10) * n))) return st;
+  if ((st = balloc(b, &d32, size_t(6) * n))) return st;
+  launch_build_profile(P, d64, d32, b->stream);
+  std::vector<double> hp(size_t(10) * n);
+  BCK(cudaMemcpyAsync(hp.data(), d64, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  auto nzero = [&](int i) { return hp[3 * size_t(n) + i] != 0.0 || hp[8 * size_t(n) + i] != 0.0; };
+  int lo = 0, hi = 0;
+  for (int i = 0; i < n / 2; ++i) if (nzero(i)) lo = i + 1;
+  for (int i = n - 1; i >= n / 2; --i) if (nzero(i)) hi = n - i;
+  for (int i = lo; i < n - hi; ++i)
+    if (nzero(i)) { lo = n; hi = 0; break; }
+  A->a = d32; A->b = d32 + n; A->ik = d32 + 2 * n; A->ah = d32 + 3 * n; A->bh = d32 + 4 * n;
+  A->ikh = d32 + 5 * n; A->n = n; A->lo = lo; A->hi = hi;
+  return CPML_OK;
+}
+
+int upload_source(cpml_batch* b, HostShot& H, float** fx, float** fy) {
+  const cpml_params& p = H.p;
+  const double ang = p.angle_force * (kPi / 180.0);
+  std::vector<float> x(p.nstep), y(p.nstep);
+  for (int it = 1; it <= p.nstep; ++it) {
+    const double st = stf(p, it);
+    x[it - 1] = float(std::sin(ang) * st * p.deltat / H.rho_src[0]);
+    y[it - 1] = float(std::cos(ang) * st * p.deltat / H.rho_src[1]);
+  }
+  int st;
+  if (!*fx && (st = balloc(b, fx, p.nstep))) return st;
+  if (!*fy && (st = balloc(b, fy, p.nstep))) return st;
+  BCK(cudaMemcpyAsync(*fx, x.data(), sizeof(float) * p.nstep, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(*fy, y.data(), sizeof(float) * p.nstep, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return CPML_OK;
+}
+
+int build_schedule(cpml_batch* b) {
+  const int ns = (int)b->shots.size();
+  std::vector<int> order(ns);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->shots[x].p.nstep > b->shots[y].p.nstep; });
+  b->max_nstep = ns ? b->shots[order[0]].p.nstep : 0;
+  std::vector<int4> items;
+  std::vector<int> items_end(ns), recs_end(ns);
+  std::vector<int2> rec;
+  std::vector<long long> off, offy;
+  size_t seis_total = 0;
+  std::vector<size_t> seis_base(ns);
+  for (int s = 0; s < ns; ++s) {
+    HostShot& H = b->shots[s];
+    seis_base[s] = seis_total;
+    seis_total += size_t(2) * H.rec.size() * H.p.nstep;
+  }
+  for (int k = 0; k < ns; ++k) {
+    const int s = order[k];
+    const HostShot& H = b->shots[s];
+    for (int j0 = 0; j0 < H.p.ny; j0 += BTY)
+      for (int i0 = 0; i0 < H.p.nx; i0 += BTX) items.push_back(make_int4(s, i0, j0, 0));
+    items_end[k] = (int)items.size();
+    const size_t nr = H.rec.size();
+    for (size_t r = 0; r < nr; ++r) {
+      rec.push_back(make_int2(s, H.rec[r]));
+      off.push_back((long long)(seis_base[s] + r * H.p.nstep));
+      offy.push_back((long long)(seis_base[s] + (nr + r) * H.p.nstep));
+    }
+    recs_end[k] = (int)rec.size();
+  }
+  std::vector<int> items_at(b->max_nstep), recs_at(b->max_nstep);
+  for (int t = 0; t < b->max_nstep; ++t) {
+    int k = 0;
+    while (k < ns && b->shots[order[k]].p.nstep > t) ++k;   // shots running at step t
+    items_at[t] = k ? items_end[k - 1] : 0;
+    recs_at[t] = k ? recs_end[k - 1] : 0;
+  }
+  int st;
+  if ((st = balloc(b, &b->d_items, std::max<size_t>(items.size(), 1)))) return st;
+  if ((st = balloc(b, &b->d_items_at, std::max(b->max_nstep, 1)))) return st;
+  if ((st = balloc(b, &b->d_recs_at, std::max(b->max_nstep, 1)))) return st;
+  if ((st = balloc(b, &b->d_rec, std::max<size_t>(rec.size(), 1)))) return st;
+  if ((st = balloc(b, &b->d_rec_off, std::max<size_t>(off.size(), 1)))) return st;
+  if ((st = balloc(b, &b->d_rec_offy, std::max<size_t>(offy.size(), 1)))) return st;
+  if ((st = balloc(b, &b->d_seis, std::max<size_t>(seis_total, 1)))) return st;
+  b->seis_floats = seis_total;
+  if (!items.empty()) BCK(cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+  if (b->max_nstep) {
+    BCK(cudaMemcpy(b->d_items_at, items_at.data(), sizeof(int) * b->max_nstep, cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->d_recs_at, recs_at.data(), sizeof(int) * b->max_nstep, cudaMemcpyHostToDevice));
+  }
+  if (!rec.empty()) {
+    BCK(cudaMemcpy(b->d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->d_rec_off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->d_rec_offy, offy.data(), sizeof(long long) * offy.size(), cudaMemcpyHostToDevice));
+  }
+  for (int s = 0; s < ns; ++s) b->shots[s].seis = b->d_seis + seis_base[s];
+  // shot descriptors
+  std::vector<Shot2D> ds(ns);
+  for (int s = 0; s < ns; ++s) ds[s] = b->shots[s].s;
+  if (!b->d_shots && (st = balloc(b, &b->d_shots, std::max(ns, 1)))) return st;
+  BCK(cudaMemcpy(b->d_shots, ds.data(), sizeof(Shot2D) * ns, cudaMemcpyHostToDevice));
+  // resident grid: every CTA must be co-resident for the grid barrier
+  int dev = 0, nsm = 0, per_sm = 0;
+  BCK(cudaGetDevice(&dev));
+  BCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch2d_kernel, BNT, 0));
+  const int first = b->max_nstep ? items_at[0] : 1;
+  b->grid = std::max(1, std::min(nsm * std::max(per_sm, 1), first));
+  BatchArgs& A = b->args;
+  A.shots = b->d_shots; A.items = b->d_items; A.items_at = b->d_items_at; A.recs_at = b->d_recs_at;
+  A.rec = b->d_rec; A.rec_off = b->d_rec_off; A.rec_offy = b->d_rec_offy; A.seis = b->d_seis;
+  A.max_nstep = b->max_nstep; A.bar = b->d_bar; A.err = b->d_err;
+  b->dirty = false;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  b->graph_ok = false;
+  return CPML_OK;
+}
+
+cudaError_t launch_batch(cpml_batch* b) {
+  void* kargs[] = {&b->args};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(b->grid);
+  cfg.blockDim = dim3(BNT);
+  cfg.stream = b->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  (void)kargs;
+  return cudaLaunchKernelEx(&cfg, batch2d_kernel, b->args);
+}
+
+int zero_batch(cpml_batch* b) {
+  for (HostShot& H : b->shots) {
+    const size_t n = size_t(H.px) * H.p.ny;
+    for (float* f : {H.s.vx, H.s.vy, H.s.sxx, H.s.syy, H.s.sxy}) BCK(cudaMemsetAsync(f, 0, 4 * n, b->stream));
+    const size_t wx = H.s.ax.width(), wy = H.s.ay.width();
+    for (int v = 0; v < 4; ++v) {
+      if (H.s.mx[v]) BCK(cudaMemsetAsync(H.s.mx[v], 0, 4 * wx * H.p.ny, b->stream));
+      if (H.s.my[v]) BCK(cudaMemsetAsync(H.s.my[v], 0, 4 * wy * size_t(H.px), b->stream));
+    }
+  }
+  if (b->d_seis) BCK(cudaMemsetAsync(b->d_seis, 0, 4 * std::max<size_t>(b->seis_floats, 1), b->stream));
+  BCK(cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned), b->stream));
+  BCK(cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream));
+  return CPML_OK;
+}
+
+int validate2d(const cpml_params& p) {
+  if (p.ndim != 2 || p.nx < 3 || p.ny < 3 || p.nstep < 1 || p.npoints_pml < 1) return CPML_ERR_INVALID;
+  if (!(p.deltax > 0) || !(p.deltay > 0) || !(p.deltat > 0) || !(p.cp > 0) || !(p.cs > 0) || !(p.rho > 0))
+    return CPML_ERR_INVALID;
+  if (!(p.rcoef > 0 && p.rcoef < 1) || p.npower < 1) return CPML_ERR_INVALID;
+  if (p.isource < 1 || p.isource > p.nx - 1 || p.jsource < 1 || p.jsource > p.ny - 1) return CPML_ERR_INVALID;
+  if (cpml_courant(&p, p.cp) > 1.0) return CPML_ERR_CFL;
+  return CPML_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int cpml_batch_create(int nshots, const cpml_params* params, cpml_batch** out) {
+  if (!out || nshots < 1 || !params) return CPML_ERR_INVALID;
+  *out = nullptr;
+  for (int s = 0; s < nshots; ++s) {
+    int st = validate2d(params[s]);
+    if (st) return st;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) { cudaGetLastError(); return CPML_ERR_CUDA; }
+  cpml_batch* b = new cpml_batch();
+  auto fail = [&](int code) { cpml_batch_destroy(b); return code; };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CPML_ERR_CUDA);
+  if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) return fail(CPML_ERR_CUDA);
+  int st;
+  if ((st = balloc(b, &b->d_bar, 2))) return fail(st);
+  if ((st = balloc(b, &b->d_err, 1))) return fail(st);
+  b->shots.resize(nshots);
+  for (int s = 0; s < nshots; ++s) {
+    HostShot& H = b->shots[s];
+    H.p = params[s];
+    const cpml_params& p = H.p;
+    H.px = (p.nx + 31) / 32 * 32;
+    Shot2D& S = H.s;
+    S.nx = p.nx; S.ny = p.ny; S.px = H.px; S.npml = p.npoints_pml; S.het = 0;
+    S.odx = float(1.0 / p.deltax); S.ody = float(1.0 / p.deltay); S.dt = float(p.deltat);
+    const double lam = p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs), mu = p.rho * p.cs * p.cs;
+    S.dt_lam = float(p.deltat * lam); S.dt_mu = float(p.deltat * mu); S.dt_l2m = float(p.deltat * (lam + 2.0 * mu));
+    S.dt_over_rho = float(p.deltat / p.rho);
+    S.half_rho = float(0.5 * p.rho); S.inv_2mu = float(1.0 / (2.0 * mu));
+    const double den = 4.0 * mu * (lam + mu);
+    S.e_c1 = float((lam + 2.0 * mu) / den); S.e_c2 = float(lam / den);
+    if ((st = shot_axis(b, p, 0, p.nx, p.deltax, &S.ax))) return fail(st);
+    if ((st = shot_axis(b, p, 1, p.ny, p.deltay, &S.ay))) return fail(st);
+    const size_t n = size_t(H.px) * p.ny;
+    float* f = nullptr;
+    if ((st = balloc(b, &f, 5 * n))) return fail(st);
+    S.vx = f; S.vy = f + n; S.sxx = f + 2 * n; S.syy = f + 3 * n; S.sxy = f + 4 * n;
+    const size_t wx = S.ax.width(), wy = S.ay.width();
+    for (int v = 0; v < 4; ++v) {
+      if ((st = balloc(b, &S.mx[v], wx * p.ny))) return fail(st);
+      if ((st = balloc(b, &S.my[v], wy * size_t(H.px)))) return fail(st);
+    }
+    S.isrc = p.isource - 1; S.jsrc = p.jsource - 1;
+    H.rho_src[0] = H.rho_src[1] = p.rho;
+    float *fx = nullptr, *fy = nullptr;
+    if ((st = upload_source(b, H, &fx, &fy))) return fail(st);
+    S.src_fx = fx; S.src_fy = fy;
+  }
+  *out = b;
+  return CPML_OK;
+}
+
+int cpml_batch_set_model(cpml_batch* b, int shot, const float* lam, const float* mu, const float* rho) {
+  if (!b || shot < 0 || shot >= (int)b->shots.size() || !lam || !mu || !rho) return CPML_ERR_INVALID;
+  HostShot& H = b->shots[shot];
+  const cpml_params& p = H.p;
+  const size_t n = size_t(p.nx) * p.ny, np = size_t(H.px) * p.ny;
+  double cpm = 0.0;
+  for (size_t c = 0; c < n; ++c) {
+    if (!(rho[c] > 0) || !(mu[c] > 0) || !(lam[c] + 2 * mu[c] > 0)) return CPML_ERR_INVALID;
+    cpm = std::max(cpm, std::sqrt((double(lam[c]) + 2.0 * mu[c]) / rho[c]));
+  }
+  if (cpml_courant(&p, cpm) > 1.0) return CPML_ERR_CFL;
+  int st;
+  if (!H.model && (st = balloc(b, &H.model, 3 * np))) return st;
+  const float* src[3] = {lam, mu, rho};
+  for (int q = 0; q < 3; ++q) {
+    BCK(cudaMemset2DAsync(H.model + q * np, 4 * H.px, 0, 4 * H.px, p.ny, b->stream));
+    BCK(cudaMemcpy2DAsync(H.model + q * np, 4 * H.px, src[q], 4 * size_t(p.nx), 4 * size_t(p.nx), p.ny,
+                          cudaMemcpyHostToDevice, b->stream));
+  }
+  H.s.lam = H.model; H.s.mu = H.model + np; H.s.rho = H.model + 2 * np; H.s.het = 1;
+  const int i = p.isource, j = p.jsource;
+  auto R = [&](int i1, int j1) { return double(rho[size_t(j1 - 1) * p.nx + (i1 - 1)]); };
+  H.rho_src[0] = R(i, j);
+  H.rho_src[1] = 0.25 * (R(i, j) + R(i + 1, j) + R(i + 1, j + 1) + R(i, j + 1));  // 2D:661
+  float* fx = const_cast<float*>(H.s.src_fx);
+  float* fy = const_cast<float*>(H.s.src_fy);
+  if ((st = upload_source(b, H, &fx, &fy))) return st;
+  b->dirty = true;
+  return CPML_OK;
+}
+
+int cpml_batch_set_receivers(cpml_batch* b, int shot, int nrec, const int* ix, const int* iy) {
+  if (!b || shot < 0 || shot >= (int)b->shots.size() || nrec < 0 || (nrec > 0 && (!ix || !iy)))
+    return CPML_ERR_INVALID;
+  HostShot& H = b->shots[shot];
+  std::vector<int> cells(nrec), ij(2 * size_t(nrec));
+  for (int r = 0; r < nrec; ++r) {
+    if (ix[r] < 1 || ix[r] > H.p.nx || iy[r] < 1 || iy[r] > H.p.ny) return CPML_ERR_INVALID;
+    cells[r] = (iy[r] - 1) * H.px + (ix[r] - 1);
+    ij[2 * r] = ix[r]; ij[2 * r + 1] = iy[r];
+  }
+  H.rec = cells;
+  H.recij = ij;
+  b->dirty = true;
+  return CPML_OK;
+}
+
+int cpml_batch_run(cpml_batch* b) {
+  if (!b) return CPML_ERR_INVALID;
+  int st;
+  if (b->dirty && (st = build_schedule(b))) return st;
+  if ((st = zero_batch(b))) return st;
+  BCK(cudaEventRecord(b->ev0, b->stream));
+  if (!b->graph && !b->graph_ok) {
+    // one cooperative launch, captured once and replayed on later runs
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const cudaError_t le = launch_batch(b);
+      const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+      ok = le == cudaSuccess && ce == cudaSuccess && g &&
+           cudaGraphInstantiate(&b->graph, g, 0) == cudaSuccess;
+      if (g) cudaGraphDestroy(g);
+    }
+    if (!ok) { cudaGetLastError(); b->graph = nullptr; }
+    b->graph_ok = true;
+  }
+  if (b->graph) BCK(cudaGraphLaunch(b->graph, b->stream));
+  else BCK(launch_batch(b));
+  BCK(cudaEventRecord(b->ev1, b->stream));
+  BCK(cudaEventSynchronize(b->ev1));
+  float ms = 0;
+  BCK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->last_ms = ms;
+  int err = 0;
+  BCK(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err & 2) return CPML_ERR_TIMEOUT;
+  if (err & 4) return CPML_ERR_UNSTABLE;
+  return CPML_OK;
+}
+
+int cpml_batch_get_seismograms(cpml_batch* b, int shot, double* vx, double* vy) {
+  if (!b || shot < 0 || shot >= (int)b->shots.size()) return CPML_ERR_INVALID;
+  HostShot& H = b->shots[shot];
+  if (b->dirty || !H.seis) return CPML_ERR_NOT_READY;
+  const size_t nr = H.rec.size(), ns = H.p.nstep;
+  if (nr == 0) return CPML_OK;
+  std::vector<float> buf(2 * nr * ns);
+  BCK(cudaMemcpy(buf.data(), H.seis, sizeof(float) * buf.size(), cudaMemcpyDeviceToHost));
+  for (size_t q = 0; q < nr * ns; ++q) {
+    if (vx) vx[q] = buf[q];
+    if (vy) vy[q] = buf[nr * ns + q];
+  }
+  return CPML_OK;
+}
+
+int cpml_batch_get_field(cpml_batch* b, int shot, int field, float* out) {
+  if (!b || shot < 0 || shot >= (int)b->shots.size() || !out) return CPML_ERR_INVALID;
+  HostShot& H = b->shots[shot];
+  const float* f = nullptr;
+  switch (field) {
+    case CPML_FIELD_VX: f = H.s.vx; break;
+    case CPML_FIELD_VY: f = H.s.vy; break;
+    case CPML_FIELD_SXX: f = H.s.sxx; break;
+    case CPML_FIELD_SYY: f = H.s.syy; break;
+    case CPML_FIELD_SXY: f = H.s.sxy; break;
+    default: return CPML_ERR_INVALID;
+  }
+  BCK(cudaMemcpy2D(out, 4 * size_t(H.p.nx), f, 4 * size_t(H.px), 4 * size_t(H.p.nx), H.p.ny,
+                   cudaMemcpyDeviceToHost));
+  return CPML_OK;
+}
+
+int cpml_batch_last_run_ms(cpml_batch* b, double* ms) {
+  if (!b || !ms) return CPML_ERR_INVALID;
+  *ms = b->last_ms;
+  return CPML_OK;
+}
+
+void cpml_batch_destroy(cpml_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+}  // extern "C"

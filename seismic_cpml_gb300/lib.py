@@ -47,6 +47,14 @@ SIGNATURES = [
     ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip, _ip]),
     ("cpml_destroy", None, [_h]),
+    ("cpml_batch_create", ctypes.c_int, [ctypes.c_int, _P(CpmlParams), _P(_h)]),
+    ("cpml_batch_set_model", ctypes.c_int, [_h, ctypes.c_int, _fp, _fp, _fp]),
+    ("cpml_batch_set_receivers", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, _ip, _ip]),
+    ("cpml_batch_run", ctypes.c_int, [_h]),
+    ("cpml_batch_get_seismograms", ctypes.c_int, [_h, ctypes.c_int, _dp, _dp]),
+    ("cpml_batch_get_field", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, _fp]),
+    ("cpml_batch_last_run_ms", ctypes.c_int, [_h, _dp]),
+    ("cpml_batch_destroy", None, [_h]),
     ("cpml_energy3d_noalloc", ctypes.c_int, [_P(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_double, ctypes.c_double, ctypes.c_double,
