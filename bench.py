@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nstep", type=int, default=None, help="time steps per bench step")
-    ap.add_argument("--tuning", type=str, default=None, help="kernel,tile_y,zchunk,depth")
+    ap.add_argument("--tuning", type=str, default=None, help="kernel,tile_y,zchunk,depth (skips autotune)")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -231,6 +232,10 @@ def run_ours(args, world, rank, local, pg):
     ncell = p.nx * p.ny * p.nz
 
     s = Solver(p, rec, tuning=tuning)
+    tune = None
+    if tuning is None and not args.no_autotune:
+        tune = s.autotune(trial_steps=20)        # outside the timed region
+        tuning = s.tuning()
     stream = torch.cuda.ExternalStream(s.stream_ptr())
     for _ in range(args.warmup):
         s.reset()
@@ -265,11 +270,13 @@ def run_ours(args, world, rank, local, pg):
     achieved = bytes_step / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = None
+    traffic_tuning = None
     try:
         with open(PROFILE_TRAFFIC) as f:
             prof = json.load(f)
-        if prof.get("grid") == [p.nx, p.ny, p.nz] and list(prof.get("tuning", [])) == list(kern):
+        if prof.get("grid") == [p.nx, p.ny, p.nz] and prof.get("tuning", [None])[0] == kern[0]:
             traffic = prof.get("dram_bytes_per_launch")
+            traffic_tuning = prof.get("tuning")
     except (OSError, ValueError):
         pass
 
@@ -317,14 +324,19 @@ def run_ours(args, world, rank, local, pg):
                    "receivers": len(rec), "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (1.5 GB of wavefields)",
                    "kernel": {"kind": ["auto", "two_sweep", "fused"][kern[0]], "tile_y": kern[1],
-                              "zchunk": kern[2], "depth": kern[3]}},
+                              "zchunk": kern[2], "depth": kern[3],
+                              "autotuned": tune is not None}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": ("ncu --set full, one step, tuning %s (profiles/fused3d_276cube.md)"
+                                        % traffic_tuning) if traffic else None,
                      "peak_source": peak_kind,
                      "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 5)},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": args.steps * (p.nstep + 2 * chunks),
+        # two step kernels per time step (interior + general, or stress + velocity),
+        # plus the chunk reduction and step-counter kernels of every chunk
+        "gpu_launches": args.steps * (2 * p.nstep + 2 * chunks),
         "clocks": clk,
         "wall_s": round(wall, 3),
     }

@@ -193,6 +193,16 @@ int cpml_get_stream(cpml_handle* h, void** stream);
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth);
 int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth);
 
+/* Autotune the step kernel for this handle's grid: every candidate (one-sweep
+   kernel with tile_y in {8,16} x zchunk in {16,24,32,48,64}, and the two-sweep
+   kernel) runs 2 untimed then trial_steps timed steps (CUDA events on the
+   handle's stream); the fastest is applied. Results are cached per shape
+   class (ndim, grid, per-cell model, NPML, PML faces) for the process and,
+   when cache_path is not NULL, in that text file (one line per class). Leaves
+   the handle reset. No reference counterpart. */
+int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* kernel,
+                  int* tile_y, int* zchunk, double* ms_per_step);
+
 void cpml_destroy(cpml_handle* h);
 const char* cpml_strerror(int status);
 

@@ -14,6 +14,7 @@
 #include <map>
 #include <vector>
 #include <algorithm>
+#include <tuple>
 
 #include <cuda_runtime.h>
 
@@ -730,6 +731,91 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
   if (tile_y) *tile_y = h->tile_y;
   if (zchunk) *zchunk = h->zchunk;
   if (depth) *depth = h->depth;
+  return CPML_OK;
+}
+
+// ---- autotuner -------------------------------------------------------------
+namespace {
+struct TuneKey {
+  int ndim, nx, ny, nz, het, npml, pml_mask;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(ndim, nx, ny, nz, het, npml, pml_mask) <
+           std::tie(o.ndim, o.nx, o.ny, o.nz, o.het, o.npml, o.pml_mask);
+  }
+};
+struct TuneVal { int kernel, tile_y, zchunk, depth; double ms; };
+std::map<TuneKey, TuneVal>& tune_cache() {
+  static std::map<TuneKey, TuneVal> c;
+  return c;
+}
+TuneKey tune_key(const cpml_handle* h) {
+  int mask = 0;
+  for (int q = 0; q < 6; ++q) mask |= (h->p.use_pml[q] ? 1 : 0) << q;
+  return TuneKey{h->ndim, h->nx, h->ny, h->nz, h->het ? 1 : 0, h->p.npoints_pml, mask};
+}
+bool read_cache_file(const char* path, const TuneKey& k, TuneVal* v) {
+  FILE* f = path ? std::fopen(path, "r") : nullptr;
+  if (!f) return false;
+  TuneKey r{};
+  TuneVal x{};
+  bool found = false;
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d %d %lf", &r.ndim, &r.nx, &r.ny, &r.nz, &r.het, &r.npml,
+                     &r.pml_mask, &x.kernel, &x.tile_y, &x.zchunk, &x.depth, &x.ms) == 12)
+    if (!(r < k) && !(k < r)) { *v = x; found = true; }
+  std::fclose(f);
+  return found;
+}
+}  // namespace
+
+int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* kernel, int* tile_y,
+                  int* zchunk, double* ms_per_step) {
+  if (!h || trial_steps < 1) return CPML_ERR_INVALID;
+  if (trial_steps + 2 > h->p.nstep) trial_steps = h->p.nstep - 2;
+  if (trial_steps < 1) return CPML_ERR_RANGE;
+  const TuneKey key = tune_key(h);
+  TuneVal best{};
+  bool have = false;
+  auto it = tune_cache().find(key);
+  if (it != tune_cache().end()) { best = it->second; have = true; }
+  if (!have && read_cache_file(cache_path, key, &best)) { tune_cache()[key] = best; have = true; }
+  int st;
+  if (!have) {
+    // candidates: launch shapes of the one-sweep 3D kernel, and the two-sweep form
+    std::vector<TuneVal> cand;
+    if (h->ndim == 3 && fused3d_supported())
+      for (int ty : {8, 16})
+        for (int lz : {16, 24, 32, 48, 64}) cand.push_back(TuneVal{CPML_KERNEL_FUSED, ty, lz, 2, 0.0});
+    cand.push_back(TuneVal{CPML_KERNEL_TWO_SWEEP, 8, 32, 2, 0.0});
+    const int flags = h->p.flags;
+    h->p.flags |= CPML_FLAG_NO_STABILITY;  // time the kernels, not the host checks
+    best.ms = 1e300;
+    for (TuneVal& c : cand) {
+      if ((st = cpml_reset(h)) || (st = cpml_set_tuning(h, c.kernel, c.tile_y, c.zchunk, c.depth))) {
+        h->p.flags = flags;
+        return st;
+      }
+      if ((st = cpml_run(h, 2))) { h->p.flags = flags; return st; }       // warm-up, graphs built
+      if ((st = cpml_run(h, trial_steps))) { h->p.flags = flags; return st; }
+      c.ms = h->last_ms / trial_steps;
+      if (c.ms < best.ms) best = c;
+    }
+    h->p.flags = flags;
+    tune_cache()[key] = best;
+    if (cache_path) {
+      if (FILE* f = std::fopen(cache_path, "a")) {
+        std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d %d %.6f\n", key.ndim, key.nx, key.ny, key.nz, key.het,
+                     key.npml, key.pml_mask, best.kernel, best.tile_y, best.zchunk, best.depth, best.ms);
+        std::fclose(f);
+      }
+    }
+  }
+  if ((st = cpml_reset(h))) return st;
+  if ((st = cpml_set_tuning(h, best.kernel, best.tile_y, best.zchunk, best.depth))) return st;
+  if ((st = cpml_reset(h))) return st;
+  if (kernel) *kernel = best.kernel;
+  if (tile_y) *tile_y = best.tile_y;
+  if (zchunk) *zchunk = best.zchunk;
+  if (ms_per_step) *ms_per_step = best.ms;
   return CPML_OK;
 }
 

@@ -73,6 +73,15 @@ class Solver:
                                         ctypes.byref(d)))
         return k.value, t.value, z.value, d.value
 
+    def autotune(self, trial_steps: int = 20, cache_path: str | None = None):
+        """Time the candidate launch shapes and keep the fastest (cpml_autotune)."""
+        k, t, z = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = ctypes.c_double()
+        _L.check(self.L.cpml_autotune(self.h, int(trial_steps),
+                                      cache_path.encode() if cache_path else None, ctypes.byref(k),
+                                      ctypes.byref(t), ctypes.byref(z), ctypes.byref(ms)), "autotune")
+        return {"kernel": k.value, "tile_y": t.value, "zchunk": z.value, "ms_per_step": ms.value}
+
     # -- time loop -------------------------------------------------------
     def run(self, nsteps: int | None = None) -> None:
         it, _ = self.status()

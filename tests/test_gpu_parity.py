@@ -218,3 +218,22 @@ def test_plane_and_field_agree():
         assert np.array_equal(s.plane("vy", 2, 7), f[6])
         assert np.array_equal(s.plane("vy", 1, 5), f[:, 4, :])
         assert np.array_equal(s.plane("vy", 0, 9), f[:, :, 8])
+
+
+def test_autotune_picks_a_candidate_and_keeps_results_exact(tmp_path):
+    """The autotuner leaves the handle reset on the fastest shape; results
+    under the chosen shape still match the oracle; the cache file round-trips."""
+    p, rec = P.small_3d(n=(70, 52, 44), nstep=120)
+    cache = str(tmp_path / "tune.txt")
+    with Solver(p, rec) as s:
+        best = s.autotune(trial_steps=8, cache_path=cache)
+        assert best["kernel"] in (1, 2) and best["ms_per_step"] > 0
+        assert s.status()[0] == 0
+        s.run()
+        vx, vy, vz = s.seismograms()
+    ref = oracle_c.run(p, rec=rec)
+    assert rl2(traces(vx, vy, vz), traces(ref.sisvx, ref.sisvy, ref.sisvz)) <= TRACE_TOL
+    assert open(cache).read().split()[:4] == ["3", "70", "52", "44"]
+    with Solver(p, rec) as s2:   # second handle of the same class: served from the cache
+        again = s2.autotune(trial_steps=8, cache_path=cache)
+        assert again == best
