@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcpml.so")
+PROGRAM = os.path.join(OUT, "cpml_program")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels2d.cu", "kernels3d.cu", "fused3d.cu", "support.cu", "noalloc.cu",
            "batch2d.cu", "host.cpp"]
@@ -57,8 +58,16 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    drv = os.path.join(CSRC, "driver.cpp")
+    if not os.path.exists(PROGRAM) or os.path.getmtime(PROGRAM) < max(os.path.getmtime(drv), os.path.getmtime(LIB)):
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", drv, "-o", PROGRAM + ".tmp",
+               "-L" + OUT, "-lcpml", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(PROGRAM + ".tmp", PROGRAM)
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", PROGRAM)
     return LIB
 
 
