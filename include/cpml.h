@@ -247,6 +247,51 @@ int cpml_energy3d_noalloc(const float* const* fields, int nx, int ny, int nz, in
                           const float* lam_cell, const float* mu_cell,
                           const float* rho_cell, int flags, double* out, void* stream);
 
+/* ---- learned-surrogate network kernels -----------------------------------
+   No counterpart in the reference. The building blocks of a small
+   convolutional network that predicts 2D receiver seismograms from a
+   velocity model and a source position; shots it predicts poorly are re-run
+   by the FD solver. All pointers are device pointers; "bf16" buffers hold
+   IEEE bfloat16 values; every call is asynchronous on `stream`.
+
+   cpml_nn_gemm: C[M,N] = alpha * op(A)[M,K] op(B)[K,N] on BF16 tensor cores
+   with FP32 accumulation. ta = 0: A is [M][lda]; ta = 1: A is [K][lda].
+   tb = 0: B is [K][ldb]; tb = 1: B is [N][ldb]. Then + bias[n] (bias may be
+   NULL), + the old Cf if accum, ReLU if relu, and stores to Cf (FP32) and/or Cb
+   (bf16), row stride ldc. splits > 1 splits K; the partial sums go to `work`
+   (>= splits*M*N floats) and are added in split order. */
+int cpml_nn_gemm(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb,
+                 float* Cf, void* Cb, int ldc, const float* bias, int relu, int accum, float alpha,
+                 int splits, float* work, long long work_elems, void* stream);
+/* 3x3 stride-2 pad-1 patches of an NHWC bf16 [B][H][W][C] activation:
+   out [B*Ho*Wo][9*C] bf16, Ho = (H+1)/2, column (ky*3+kx)*C + c. */
+int cpml_nn_im2col(const void* in, void* out, int B, int H, int W, int C, void* stream);
+/* Adjoint of cpml_nn_im2col on FP32 data: out [B][H][W][C] (overwritten). */
+int cpml_nn_col2im(const float* col, float* out, int B, int H, int W, int C, void* stream);
+/* dx = dy where y > 0, else 0; to bf16 and/or FP32 (either may be NULL). */
+int cpml_nn_relu_bwd(const float* dy, const float* y, void* dx_bf16, float* dx_f32, long long n,
+                     void* stream);
+/* dst[b][r][:] = src[b][r + shift[b]][:] (L values per row) where
+   0 <= r + shift[b] < rows_src, else 0; dst has rows_dst rows per shot, to
+   FP32 and/or bf16. shift is a device int array of B entries. */
+int cpml_nn_shift_rows(const float* src, const int* shift, float* dst_f32, void* dst_bf16, int B,
+                       int rows_src, int rows_dst, int L, void* stream);
+int cpml_nn_cast(const float* x, void* y_bf16, long long n, void* stream);
+/* out[n] (+)= sum over m of x[m][n]; work >= ceil(M/256)*N floats. */
+int cpml_nn_colsum(const float* x, float* out, int M, int N, int accum, float* work,
+                   long long work_elems, void* stream);
+/* Per shot b of B rows of L values: loss[b] = ||pred-target||^2 / ||target||^2
+   and, if grad != NULL, grad = d(mean_b loss[b]) / d pred. */
+int cpml_nn_rel_l2(const float* pred, const float* target, float* grad, float* loss, int B, int L,
+                   void* stream);
+/* dh[b] = d/dh_b of weight * mean_b (h[b*ldh] - log loss[b])^2. */
+int cpml_nn_head_grad(const float* h, int ldh, const float* loss, float* dh, int B, float weight,
+                      void* stream);
+/* One Adam step (bias-corrected with `step`, 1-based; L2 weight decay wd) on
+   n FP32 master weights w, refreshing their bf16 copy wb (may be NULL). */
+int cpml_nn_adam(float* w, void* wb, const float* g, float* m, float* v, long long n, float lr,
+                 float beta1, float beta2, float eps, int step, float wd, void* stream);
+
 /* ---- reference output files (2D:738-808, 820-999; 3D:1247-1364) -------- */
 
 /* Vx_file_NNN.dat / Vy_file_NNN.dat (/ Vz_file_NNN.dat if vz != NULL), one

@@ -1,0 +1,422 @@
+// surrogate.cu -- kernels of the learned seismogram surrogate.
+//
+// A small convolutional network maps a velocity model and a source position
+// to receiver seismograms; shots it predicts poorly are re-run by the FD
+// solver. Every layer of its training and inference runs on these kernels:
+//   cpml_nn_gemm      C = alpha op(A) op(B) on BF16 tensor cores (mma.sync
+//                     m16n8k16, FP32 accumulation), optional split-K with a
+//                     fixed-order reduction, fused bias + ReLU epilogue,
+//                     FP32 and/or BF16 output, optional accumulate
+//   cpml_nn_im2col    3x3 stride-2 pad-1 patches of an NHWC BF16 activation
+//   cpml_nn_col2im    its adjoint, as a gather (fixed order, no atomics)
+//   cpml_nn_relu_bwd  dX = dY * (Y > 0), FP32 in, BF16 and/or FP32 out
+//   cpml_nn_shift_rows per-shot row shift (offset axis <-> receiver axis)
+//   cpml_nn_colsum    bias gradients: column sums in a fixed two-stage order
+//   cpml_nn_rel_l2    per-shot squared relative L2 misfit and its gradient
+//   cpml_nn_head_grad gradient of the misfit-prediction head
+//   cpml_nn_adam      FP32 Adam on master weights, refreshed BF16 copies
+//   cpml_nn_cast      FP32 -> BF16
+// No counterpart in the reference, which has no learned component.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "../../include/cpml.h"
+
+namespace {
+
+constexpr int GBM = 64, GBN = 64, GBK = 32, GKP = GBK + 8;  // tile; padded smem row
+constexpr int GT = 128;                                      // 4 warps, 2 x 2, 32 x 32 each
+
+__device__ __forceinline__ uint32_t pack2(const __nv_bfloat16* p) {
+  return *reinterpret_cast<const uint32_t*>(p);
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct Epilogue {
+  float* Cf;
+  __nv_bfloat16* Cb;
+  int ldc;
+  const float* bias;
+  int relu, accum;
+  float alpha;
+};
+
+__device__ __forceinline__ void epilogue_store(const Epilogue& e, int row, int col, float acc) {
+  float v = e.alpha * acc;
+  if (e.bias) v += e.bias[col];
+  const size_t o = (size_t)row * e.ldc + col;
+  if (e.accum && e.Cf) v += e.Cf[o];
+  if (e.relu) v = fmaxf(v, 0.f);
+  if (e.Cf) e.Cf[o] = v;
+  if (e.Cb) e.Cb[o] = __float2bfloat16(v);
+}
+
+// C[M,N] = op(A)[M,K] * op(B)[K,N].
+//   ta == 0: A is [M][lda] (k contiguous); ta == 1: A is [K][lda] (m contiguous)
+//   tb == 0: B is [K][ldb] (n contiguous); tb == 1: B is [N][ldb] (k contiguous)
+// blockIdx.z selects a K range of kchunk (a multiple of GBK). With one split
+// the epilogue is applied here; otherwise the raw partial sums go to
+// work[z][M][N] and gemm_reduce_kernel finishes.
+__global__ void __launch_bounds__(GT) gemm_bf16_kernel(int M, int N, int K, int kchunk,
+                                                       const __nv_bfloat16* __restrict__ A, int lda, int ta,
+                                                       const __nv_bfloat16* __restrict__ B, int ldb, int tb,
+                                                       Epilogue ep, float* __restrict__ work) {
+  __shared__ __align__(16) __nv_bfloat16 As[GBM][GKP];   // [m][k]
+  __shared__ __align__(16) __nv_bfloat16 Bs[GBN][GKP];   // [n][k]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * GBN;   // M tiles on x (up to 2^31 - 1)
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  const int g = lane >> 2, t4 = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  for (int k0 = kb; k0 < ke; k0 += GBK) {
+    // stage 64 x 32 tiles of A and B, coalesced along the contiguous index
+    for (int e = tid; e < GBM * GBK; e += GT) {
+      int mm, kk;
+      if (ta) { mm = e % GBM; kk = e / GBM; } else { kk = e % GBK; mm = e / GBK; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      __nv_bfloat16 v = zero;
+      if (gm < M && gk < ke) v = ta ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      As[mm][kk] = v;
+    }
+    for (int e = tid; e < GBN * GBK; e += GT) {
+      int nn, kk;
+      if (tb) { kk = e % GBK; nn = e / GBK; } else { nn = e % GBN; kk = e / GBN; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      __nv_bfloat16 v = zero;
+      if (gn < N && gk < ke) v = tb ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      Bs[nn][kk] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < GBK; ks += 16) {
+      uint32_t af[2][4], bf[4][2];
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int r = wm + a * 16 + g;
+        af[a][0] = pack2(&As[r][ks + t4 * 2]);
+        af[a][1] = pack2(&As[r + 8][ks + t4 * 2]);
+        af[a][2] = pack2(&As[r][ks + t4 * 2 + 8]);
+        af[a][3] = pack2(&As[r + 8][ks + t4 * 2 + 8]);
+      }
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int c = wn + b * 8 + g;
+        bf[b][0] = pack2(&Bs[c][ks + t4 * 2]);
+        bf[b][1] = pack2(&Bs[c][ks + t4 * 2 + 8]);
+      }
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) mma_bf16(acc[a][b], af[a], bf[b]);
+    }
+    __syncthreads();
+  }
+  // accumulator fragment layout of m16n8: rows g and g + 8, columns 2 t4 + {0,1}
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int row = m0 + wm + a * 16 + g + h * 8;
+          const int col = n0 + wn + b * 8 + t4 * 2 + q;
+          if (row >= M || col >= N) continue;
+          const float v = acc[a][b][h * 2 + q];
+          if (work)
+            work[((size_t)blockIdx.z * M + row) * N + col] = v;
+          else
+            epilogue_store(ep, row, col, v);
+        }
+}
+
+__global__ void gemm_reduce_kernel(int M, int N, int splits, const float* __restrict__ work, Epilogue ep) {
+  const long long total = (long long)M * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < splits; ++z) s += work[(size_t)z * total + e];
+    epilogue_store(ep, (int)(e / N), (int)(e % N), s);
+  }
+}
+
+// 3x3, stride 2, pad 1 patches. in: NHWC [B][H][W][C]; out row m = (b, y, x)
+// of the Ho x Wo output grid, column k = (ky*3 + kx)*C + c.
+__global__ void im2col_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int B,
+                              int H, int W, int C, int Ho, int Wo) {
+  const long long K = 9LL * C;
+  const long long total = (long long)B * Ho * Wo * K;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long m = e / K;
+    const int k = (int)(e % K);
+    const int c = k % C, kk = k / C, ky = kk / 3, kx = kk % 3;
+    const int x = (int)(m % Wo), y = (int)((m / Wo) % Ho), b = (int)(m / ((long long)Wo * Ho));
+    const int iy = 2 * y + ky - 1, ix = 2 * x + kx - 1;
+    __nv_bfloat16 v = __float2bfloat16(0.f);
+    if (iy >= 0 && iy < H && ix >= 0 && ix < W) v = in[(((long long)b * H + iy) * W + ix) * C + c];
+    out[e] = v;
+  }
+}
+
+// Adjoint of im2col as a gather: each input element sums, in a fixed order,
+// the (at most 2 x 2) patch entries that read it.
+__global__ void col2im_kernel(const float* __restrict__ col, float* __restrict__ out, int B, int H, int W, int C,
+                              int Ho, int Wo) {
+  const long long total = (long long)B * H * W * C;
+  const long long K = 9LL * C;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % C);
+    const int ix = (int)((e / C) % W), iy = (int)((e / ((long long)C * W)) % H);
+    const int b = (int)(e / ((long long)C * W * H));
+    float s = 0.f;
+    for (int ky = 0; ky < 3; ++ky) {
+      const int ty = iy + 1 - ky;
+      if (ty < 0 || (ty & 1) || (ty >> 1) >= Ho) continue;
+      const int y = ty >> 1;
+      for (int kx = 0; kx < 3; ++kx) {
+        const int tx = ix + 1 - kx;
+        if (tx < 0 || (tx & 1) || (tx >> 1) >= Wo) continue;
+        const int x = tx >> 1;
+        const long long m = ((long long)b * Ho + y) * Wo + x;
+        s += col[m * K + (ky * 3 + kx) * C + c];
+      }
+    }
+    out[e] = s;
+  }
+}
+
+__global__ void relu_bwd_kernel(const float* __restrict__ dy, const float* __restrict__ y,
+                                __nv_bfloat16* __restrict__ dx_b, float* __restrict__ dx_f, long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const float v = y[e] > 0.f ? dy[e] : 0.f;
+    if (dx_b) dx_b[e] = __float2bfloat16(v);
+    if (dx_f) dx_f[e] = v;
+  }
+}
+
+// dst[b][r][:] = src[b][r + shift[b]][:] where 0 <= r + shift[b] < rows_src,
+// else 0: moves traces between the source-centred offset axis and the
+// receiver axis (a gather in both directions, so its adjoint is one too).
+__global__ void shift_rows_kernel(const float* __restrict__ src, const int* __restrict__ shift,
+                                  float* __restrict__ dst_f, __nv_bfloat16* __restrict__ dst_b, int B, int rows_src,
+                                  int rows_dst, int L) {
+  const long long total = (long long)B * rows_dst * L;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % L);
+    const long long br = e / L;
+    const int r = (int)(br % rows_dst), b = (int)(br / rows_dst);
+    const int q = r + shift[b];
+    const float v = (q >= 0 && q < rows_src) ? src[((long long)b * rows_src + q) * L + i] : 0.f;
+    if (dst_f) dst_f[e] = v;
+    if (dst_b) dst_b[e] = __float2bfloat16(v);
+  }
+}
+
+__global__ void cast_kernel(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    y[e] = __float2bfloat16(x[e]);
+}
+
+constexpr int COLSUM_ROWS = 256;
+
+// Stage 1: part[c][n] = sum of rows [c R, (c+1) R) of column n, rows in order.
+__global__ void colsum_part_kernel(const float* __restrict__ x, float* __restrict__ part, int M, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int r0 = blockIdx.y * COLSUM_ROWS, r1 = min(M, r0 + COLSUM_ROWS);
+  float s = 0.f;
+  for (int m = r0; m < r1; ++m) s += x[(size_t)m * N + n];
+  part[(size_t)blockIdx.y * N + n] = s;
+}
+
+// Stage 2: out[n] (+)= sum over chunks in order.
+__global__ void colsum_final_kernel(const float* __restrict__ part, float* __restrict__ out, int chunks, int N,
+                                    int accum) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int c = 0; c < chunks; ++c) s += part[(size_t)c * N + n];
+  out[n] = accum ? out[n] + s : s;
+}
+
+// Per shot b: loss_b = ||p - t||^2 / (||t||^2 + tiny); grad = 2 (p - t) / (||t||^2 + tiny) / B.
+// Sums in FP64 within the block, fixed tree order.
+__global__ void rel_l2_kernel(const float* __restrict__ pred, const float* __restrict__ target,
+                              float* __restrict__ grad, float* __restrict__ loss, int B, int L) {
+  const int b = blockIdx.x;
+  __shared__ double sn[256], se[256];
+  double n2 = 0.0, e2 = 0.0;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const double t = target[(size_t)b * L + i], d = (double)pred[(size_t)b * L + i] - t;
+    n2 += t * t;
+    e2 += d * d;
+  }
+  sn[threadIdx.x] = n2;
+  se[threadIdx.x] = e2;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { sn[threadIdx.x] += sn[threadIdx.x + o]; se[threadIdx.x] += se[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  const double den = sn[0] + 1e-30;
+  if (threadIdx.x == 0) loss[b] = (float)(se[0] / den);
+  if (grad) {
+    const float s = (float)(2.0 / den / B);
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+      grad[(size_t)b * L + i] = s * (pred[(size_t)b * L + i] - target[(size_t)b * L + i]);
+  }
+}
+
+// Misfit head: h_b predicts log(loss_b); gradient of w * mean_b (h_b - log loss_b)^2.
+__global__ void head_grad_kernel(const float* __restrict__ h, int ldh, const float* __restrict__ loss,
+                                 float* __restrict__ dh, int B, float w) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const float t = logf(fmaxf(loss[b], 1e-12f));
+  dh[b] = 2.f * w * (h[(size_t)b * ldh] - t) / (float)B;
+}
+
+__global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, long long n, float lr, float b1, float b2,
+                            float eps, float c1, float c2, float wd) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const float gr = g[e] + wd * w[e];
+    const float mm = b1 * m[e] + (1.f - b1) * gr;
+    const float vv = b2 * v[e] + (1.f - b2) * gr * gr;
+    m[e] = mm;
+    v[e] = vv;
+    const float nw = w[e] - lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    w[e] = nw;
+    if (wb) wb[e] = __float2bfloat16(nw);
+  }
+}
+
+int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)(b > 8192 ? 8192 : (b < 1 ? 1 : b));
+}
+
+int status() { return cudaGetLastError() == cudaSuccess ? CPML_OK : CPML_ERR_CUDA; }
+
+}  // namespace
+
+extern "C" {
+
+int cpml_nn_gemm(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb, float* Cf,
+                 void* Cb, int ldc, const float* bias, int relu, int accum, float alpha, int splits, float* work,
+                 long long work_elems, void* stream) {
+  if (M < 0 || N < 0 || K < 0 || !A || !B || (!Cf && !Cb) || splits < 1) return CPML_ERR_INVALID;
+  if (accum && !Cf) return CPML_ERR_INVALID;
+  if (M == 0 || N == 0) return CPML_OK;
+  if ((N + GBN - 1) / GBN > 65535) return CPML_ERR_RANGE;
+  int kchunk = (K + splits - 1) / splits;
+  kchunk = ((kchunk + GBK - 1) / GBK) * GBK;
+  if (kchunk < GBK) kchunk = GBK;
+  splits = K > 0 ? (K + kchunk - 1) / kchunk : 1;
+  if (splits > 65535) return CPML_ERR_RANGE;
+  if (splits > 1 && (!work || work_elems < (long long)splits * M * N)) return CPML_ERR_INVALID;
+  const Epilogue ep{Cf, (__nv_bfloat16*)Cb, ldc, bias, relu, accum, alpha};
+  const dim3 grid((M + GBM - 1) / GBM, (N + GBN - 1) / GBN, splits);
+  cudaStream_t st = (cudaStream_t)stream;
+  gemm_bf16_kernel<<<grid, GT, 0, st>>>(M, N, K, kchunk, (const __nv_bfloat16*)A, lda, ta,
+                                        (const __nv_bfloat16*)B, ldb, tb, ep, splits > 1 ? work : nullptr);
+  if (splits > 1) gemm_reduce_kernel<<<grid_for((long long)M * N), 256, 0, st>>>(M, N, splits, work, ep);
+  return status();
+}
+
+int cpml_nn_im2col(const void* in, void* out, int B, int H, int W, int C, void* stream) {
+  if (!in || !out || B < 1 || H < 2 || W < 2 || C < 1) return CPML_ERR_INVALID;
+  const int Ho = (H + 1) / 2, Wo = (W + 1) / 2;
+  const long long n = (long long)B * Ho * Wo * 9 * C;
+  im2col_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, (__nv_bfloat16*)out, B, H,
+                                                                 W, C, Ho, Wo);
+  return status();
+}
+
+int cpml_nn_col2im(const float* col, float* out, int B, int H, int W, int C, void* stream) {
+  if (!col || !out || B < 1 || H < 2 || W < 2 || C < 1) return CPML_ERR_INVALID;
+  const int Ho = (H + 1) / 2, Wo = (W + 1) / 2;
+  const long long n = (long long)B * H * W * C;
+  col2im_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(col, out, B, H, W, C, Ho, Wo);
+  return status();
+}
+
+int cpml_nn_relu_bwd(const float* dy, const float* y, void* dx_bf16, float* dx_f32, long long n, void* stream) {
+  if (!dy || !y || n < 0 || (!dx_bf16 && !dx_f32)) return CPML_ERR_INVALID;
+  if (n == 0) return CPML_OK;
+  relu_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, y, (__nv_bfloat16*)dx_bf16, dx_f32, n);
+  return status();
+}
+
+int cpml_nn_shift_rows(const float* src, const int* shift, float* dst_f32, void* dst_bf16, int B, int rows_src,
+                       int rows_dst, int L, void* stream) {
+  if (!src || !shift || (!dst_f32 && !dst_bf16) || B < 1 || rows_src < 1 || rows_dst < 1 || L < 1)
+    return CPML_ERR_INVALID;
+  const long long n = (long long)B * rows_dst * L;
+  shift_rows_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(src, shift, dst_f32, (__nv_bfloat16*)dst_bf16, B,
+                                                                    rows_src, rows_dst, L);
+  return status();
+}
+
+int cpml_nn_cast(const float* x, void* y, long long n, void* stream) {
+  if (!x || !y || n < 0) return CPML_ERR_INVALID;
+  if (n == 0) return CPML_OK;
+  cast_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(x, (__nv_bfloat16*)y, n);
+  return status();
+}
+
+int cpml_nn_colsum(const float* x, float* out, int M, int N, int accum, float* work, long long work_elems,
+                   void* stream) {
+  if (!x || !out || M < 1 || N < 1 || !work) return CPML_ERR_INVALID;
+  const int chunks = (M + COLSUM_ROWS - 1) / COLSUM_ROWS;
+  if (chunks > 65535) return CPML_ERR_RANGE;
+  if (work_elems < (long long)chunks * N) return CPML_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  colsum_part_kernel<<<dim3((N + 127) / 128, chunks), 128, 0, st>>>(x, work, M, N);
+  colsum_final_kernel<<<(N + 127) / 128, 128, 0, st>>>(work, out, chunks, N, accum);
+  return status();
+}
+
+int cpml_nn_rel_l2(const float* pred, const float* target, float* grad, float* loss, int B, int L, void* stream) {
+  if (!pred || !target || !loss || B < 1 || L < 1) return CPML_ERR_INVALID;
+  rel_l2_kernel<<<B, 256, 0, (cudaStream_t)stream>>>(pred, target, grad, loss, B, L);
+  return status();
+}
+
+int cpml_nn_head_grad(const float* h, int ldh, const float* loss, float* dh, int B, float weight, void* stream) {
+  if (!h || !loss || !dh || B < 1 || ldh < 1) return CPML_ERR_INVALID;
+  head_grad_kernel<<<(B + 127) / 128, 128, 0, (cudaStream_t)stream>>>(h, ldh, loss, dh, B, weight);
+  return status();
+}
+
+int cpml_nn_adam(float* w, void* wb, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
+                 float eps, int step, float wd, void* stream) {
+  if (!w || !g || !m || !v || n < 0 || step < 1) return CPML_ERR_INVALID;
+  if (n == 0) return CPML_OK;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, (__nv_bfloat16*)wb, g, m, v, n, lr, b1, b2, eps,
+                                                              c1, c2, wd);
+  return status();
+}
+
+}  // extern "C"

@@ -62,6 +62,21 @@ SIGNATURES = [
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     ("cpml_strerror", ctypes.c_char_p, [ctypes.c_int]),
+    ("cpml_nn_gemm", ctypes.c_int, [ctypes.c_int] * 3 + [_vp, ctypes.c_int, ctypes.c_int] * 2
+     + [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, _vp,
+        ctypes.c_longlong, _vp]),
+    ("cpml_nn_im2col", ctypes.c_int, [_vp, _vp] + [ctypes.c_int] * 4 + [_vp]),
+    ("cpml_nn_col2im", ctypes.c_int, [_vp, _vp] + [ctypes.c_int] * 4 + [_vp]),
+    ("cpml_nn_relu_bwd", ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
+    ("cpml_nn_shift_rows", ctypes.c_int, [_vp, _vp, _vp, _vp] + [ctypes.c_int] * 4 + [_vp]),
+    ("cpml_nn_cast", ctypes.c_int, [_vp, _vp, ctypes.c_longlong, _vp]),
+    ("cpml_nn_colsum", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
+                                      ctypes.c_longlong, _vp]),
+    ("cpml_nn_rel_l2", ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    ("cpml_nn_head_grad", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_float,
+                                         _vp]),
+    ("cpml_nn_adam", ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_longlong] + [ctypes.c_float] * 4
+     + [ctypes.c_int, ctypes.c_float, _vp]),
     ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_double]),
     ("cpml_write_energy", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, ctypes.c_int, ctypes.c_double,
