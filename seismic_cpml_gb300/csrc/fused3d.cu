@@ -31,7 +31,10 @@
 //   3. computes the new velocities one plane behind (plane m-1) from the
 //      stress ring (planes m-2..m), then source, rigid faces, store to B and
 //      the energy partials;
-//   4. thread 0 waits for g(m+1); the CTA barrier that follows publishes it.
+//   4. (next iteration) every thread waits for g(m+1) on its mbarrier; the
+//      one CTA barrier of an iteration sits between its stress and velocity
+//      sweeps, and 4-plane stress rings let a warp's stress sweep of plane
+//      m+1 overlap other warps' velocity sweep of plane m-1.
 // Stress-side C-PML memory variables are ping-ponged like the fields (halo
 // cells read time-n values that their owner is overwriting); velocity-side
 // ones are updated in place (only the owner touches them).
@@ -101,9 +104,11 @@ struct Geo {
   static constexpr int RX = FTX + 2, RY = TY + 2, REG = RX * RY;  // stress ring plane
   // Power-of-two rings, a plane's slot is (m & (S-1)). Loads run two planes
   // ahead: v_x/v_y/v_z, mu and rho need at most 4 live planes, old stresses
-  // and lambda 2.
+  // and lambda 2. The six stress rings hold 4 planes each, so the stress
+  // sweep of plane m+1 never overwrites a plane the velocity sweep of plane
+  // m-1 still reads (they may overlap in time: one CTA barrier per plane).
   static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 2 + 4 + 4 : 0);
-  static constexpr int RING = 16 * REG;              // xx yy xy zz: 2 planes; xz yz: 4
+  static constexpr int RING = 24 * REG;
   static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 16 + 64;
   static constexpr int NH = 2 * FTX + 2 * TY;        // halo stress cells
 };
@@ -125,12 +130,12 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
   float* mus = lms + 2 * SLOT;
   float* rhs = mus + 4 * SLOT;
   float* ring = sm + G::NBOX * SLOT;
-  float* r_sxx = ring;                   // [2]
-  float* r_syy = r_sxx + 2 * REG;        // [2]
-  float* r_sxy = r_syy + 2 * REG;        // [2]
-  float* r_szz = r_sxy + 2 * REG;        // [2]
-  float* r_sxz = r_szz + 2 * REG;        // [4]
-  float* r_syz = r_sxz + 4 * REG;        // [4]
+  float* r_sxx = ring;                   // [4] each
+  float* r_syy = r_sxx + 4 * REG;
+  float* r_sxy = r_syy + 4 * REG;
+  float* r_szz = r_sxy + 4 * REG;
+  float* r_sxz = r_szz + 4 * REG;
+  float* r_syz = r_sxz + 4 * REG;
   uint64_t* bar = reinterpret_cast<uint64_t*>(r_syz + 4 * REG);
 
   const int tid = threadIdx.x;
@@ -186,19 +191,11 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // Only thread 0 waits on the TMA barriers; the CTA barrier that follows
-  // publishes the landed boxes to every thread, so no warp spends issue slots
-  // polling while other CTAs on the SM compute.
-  bool ok_all = true;
-  {
-    bool ok = true;
-    if (tid == 0) {
-      issue_group(kk0, &bar[0], true);
-      if (kk0 + 1 <= ke) issue_group(kk0 + 1, &bar[1], false);
-      ok = mbar_wait_bounded(&bar[0], 0);
-    }
-    if (!__syncthreads_and(ok ? 1 : 0)) ok_all = false;
+  if (tid == 0) {
+    issue_group(kk0, &bar[0], true);
+    if (kk0 + 1 <= ke) issue_group(kk0 + 1, &bar[1], false);
   }
+  bool ok_all = true;
 
   // ---- tile classification (uniform over the CTA) ---------------------------
   const int wx = s.ax.width(), wy = s.ay.width();
@@ -249,8 +246,11 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { cvx[q] = cvy[q] = cvz[q] = nvx[q] = nvy[q] = nvz[q] = 0.f; }
 
-  for (int m = kk0; ok_all && m <= ke; ++m) {
+  for (int m = kk0; m <= ke; ++m) {
     const int use = m - kk0;
+    // every thread waits for load group g(m) itself (try_wait suspends the
+    // thread in hardware), so there is one CTA barrier per plane
+    const bool landed = mbar_wait_bounded(&bar[use & 1], (uint32_t)((use >> 1) & 1));
     // ======================= stress at plane m ==============================
     const float* VX0 = vxs + (m & 3) * SLOT;
     const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
@@ -259,14 +259,16 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
     const float* VZ0 = vzs + (m & 3) * SLOT;
     const float* VZm = vzs + ((m - 1) & 3) * SLOT;
     const float* SO = sos + (m & 1) * 6 * SLOT;
-    float* Rxx = r_sxx + (m & 1) * REG;
-    float* Ryy = r_syy + (m & 1) * REG;
-    float* Rzz = r_szz + (m & 1) * REG;
-    float* Rxy = r_sxy + (m & 1) * REG;
+    float* Rxx = r_sxx + (m & 3) * REG;
+    float* Ryy = r_syy + (m & 3) * REG;
+    float* Rzz = r_szz + (m & 3) * REG;
+    float* Rxy = r_sxy + (m & 3) * REG;
     float* Rxz = r_sxz + (m & 3) * REG;
     float* Ryz = r_syz + (m & 3) * REG;
     const bool st_plane = m >= kb && m < ke;
-    if (FAST) {
+    if (!landed) {
+      // nothing to compute on boxes that did not arrive
+    } else if (FAST) {
       const long long cpl = (long long)m * pl + (long long)j0 * px + i0;
       auto cell = [&](int b, int r, int comps, bool store, long long c, float& ox, float& oy, float& oz) {
         const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
@@ -432,19 +434,20 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
         }
       if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false);
     }
-    __syncthreads();
+    if (!__syncthreads_and(landed ? 1 : 0)) { ok_all = false; break; }
     // g(m+2) goes into slots whose last reader was stress(m) (own-cell
-    // velocities travel in registers), so it is requested before velocity.
+    // velocities travel in registers; the velocity sweep reads only the
+    // stress rings and rho planes m-1, m), so it is requested before velocity.
     if (tid == 0 && m + 2 <= ke) issue_group(m + 2, &bar[use & 1], false);
 
     // ======================= velocity at plane p = m - 1 ====================
     const int p = m - 1;
     if (p >= kb && p < ke) {
-      const float* Sxx = r_sxx + (p & 1) * REG;
-      const float* Syy = r_syy + (p & 1) * REG;
-      const float* Sxy = r_sxy + (p & 1) * REG;
-      const float* Szz0 = r_szz + (p & 1) * REG;
-      const float* Szz1 = r_szz + ((p + 1) & 1) * REG;
+      const float* Sxx = r_sxx + (p & 3) * REG;
+      const float* Syy = r_syy + (p & 3) * REG;
+      const float* Sxy = r_sxy + (p & 3) * REG;
+      const float* Szz0 = r_szz + (p & 3) * REG;
+      const float* Szz1 = r_szz + ((p + 1) & 3) * REG;
       const float* Sxz0 = r_sxz + (p & 3) * REG;
       const float* Sxzm = r_sxz + ((p - 1) & 3) * REG;
       const float* Syz0 = r_syz + (p & 3) * REG;
@@ -604,9 +607,6 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
     }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) { cvx[q] = nvx[q]; cvy[q] = nvy[q]; cvz[q] = nvz[q]; }
-    bool ok = true;
-    if (tid == 0 && m + 1 <= ke) ok = mbar_wait_bounded(&bar[(use + 1) & 1], (uint32_t)(((use + 1) >> 1) & 1));
-    if (!__syncthreads_and(ok ? 1 : 0)) ok_all = false;
   }
   if (!ok_all) {
     if (tid == 0) {
