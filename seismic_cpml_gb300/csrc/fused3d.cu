@@ -14,10 +14,11 @@
 // concurrently (they share no cells and only read set A):
 //   interior items -- the tile, its one-cell halo and all planes kb-1..ke lie
 //       outside every C-PML slab and every rigid face: no memory variables,
-//       no loop-range masks; compiled lean for high occupancy;
-//   general items  -- everything else (PML slabs, faces, partial tiles, and
-//       the per-cell model), with every memory-variable load of a cell issued
-//       together before its arithmetic.
+//       no loop-range masks; compiled lean for high occupancy (a per-cell
+//       model adds lambda/mu/rho boxes to the same TMA pipeline);
+//   general items  -- everything else (PML slabs, faces, partial tiles),
+//       with every memory-variable load of a cell issued together before
+//       its arithmetic.
 // A CTA streams its planes in z (2.5D); at iteration m it
 //   1. computes the new stresses at plane m on the tile plus the halo cells
 //      the velocity update reads (left column: sigma_xx, top row: sigma_yy,
@@ -114,10 +115,9 @@ struct Geo {
 };
 
 template <int TY, bool FAST, bool HET>
-__global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
+__global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
     fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls,
                    const int4* __restrict__ items, int item_base, int record) {
-  static_assert(!(FAST && HET), "the interior kernel is homogeneous only");
   using G = Geo<TY, HET>;
   constexpr int BX = G::BX, SLOT = G::SLOT, RX = G::RX, REG = G::REG;
   constexpr int NQ = TY / 8;             // own rows per thread
@@ -270,6 +270,11 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
       // nothing to compute on boxes that did not arrive
     } else if (FAST) {
       const long long cpl = (long long)m * pl + (long long)j0 * px + i0;
+      const float* Lm = lms + (m & 1) * SLOT;
+      const float* M0 = mus + (m & 3) * SLOT;
+      const float* M1 = mus + ((m + 1) & 3) * SLOT;
+      // interior tiles never touch the last column, so the 8-point mu
+      // average of sigma_yz always takes i+1 (the general path clamps it)
       auto cell = [&](int b, int r, int comps, bool store, long long c, float& ox, float& oy, float& oz) {
         const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
         ox = vxc; oy = vyc; oz = vzc;
@@ -277,24 +282,39 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
           const float dxx = (VX0[b + 1] - vxc) * s.odx;
           const float dyy = (vyc - VY0[b - BX]) * s.ody;
           const float dzz = (vzc - VZm[b]) * s.odz;
-          const float nxx = SO[b] + (s.dt_l2m * dxx + s.dt_lam * (dyy + dzz));
-          const float nyy = SO[SLOT + b] + (s.dt_lam * (dxx + dzz) + s.dt_l2m * dyy);
-          const float nzz = SO[2 * SLOT + b] + (s.dt_lam * (dxx + dyy) + s.dt_l2m * dzz);
+          float dl = s.dt_lam, dl2m = s.dt_l2m;
+          if (HET) {
+            const float lh = 0.5f * (Lm[b + 1] + Lm[b]);
+            const float mh = 0.5f * (M0[b + 1] + M0[b]);
+            dl = s.dt * lh;
+            dl2m = s.dt * (lh + 2.0f * mh);
+          }
+          const float nxx = SO[b] + (dl2m * dxx + dl * (dyy + dzz));
+          const float nyy = SO[SLOT + b] + (dl * (dxx + dzz) + dl2m * dyy);
+          const float nzz = SO[2 * SLOT + b] + (dl * (dxx + dyy) + dl2m * dzz);
           Rxx[r] = nxx; Ryy[r] = nyy; Rzz[r] = nzz;
           if (store) { s.g.sxx[c] = nxx; s.g.syy[c] = nyy; s.g.szz[c] = nzz; }
         }
         if (comps & 2) {
-          const float n = SO[3 * SLOT + b] + s.dt_mu * ((vyc - VY0[b - 1]) * s.odx + (VX0[b + BX] - vxc) * s.ody);
+          const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
+          const float n = SO[3 * SLOT + b] + dm * ((vyc - VY0[b - 1]) * s.odx + (VX0[b + BX] - vxc) * s.ody);
           Rxy[r] = n;
           if (store) s.g.sxy[c] = n;
         }
         if (comps & 4) {
-          const float n = SO[4 * SLOT + b] + s.dt_mu * ((vzc - VZ0[b - 1]) * s.odx + (VX1[b] - vxc) * s.odz);
+          const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
+          const float n = SO[4 * SLOT + b] + dm * ((vzc - VZ0[b - 1]) * s.odx + (VX1[b] - vxc) * s.odz);
           Rxz[r] = n;
           if (store) s.g.sxz[c] = n;
         }
         if (comps & 8) {
-          const float n = SO[5 * SLOT + b] + s.dt_mu * ((VZ0[b + BX] - vzc) * s.ody + (VY1[b] - vyc) * s.odz);
+          float dm = s.dt_mu;
+          if (HET) {
+            const float sm8 = ((((((M0[b] + M0[b + 1]) + M0[b + BX]) + M0[b + BX + 1]) + M1[b]) + M1[b + 1]) +
+                               M1[b + BX]) + M1[b + BX + 1];
+            dm = s.dt * (0.125f * sm8);
+          }
+          const float n = SO[5 * SLOT + b] + dm * ((VZ0[b + BX] - vzc) * s.ody + (VY1[b] - vyc) * s.odz);
           Ryz[r] = n;
           if (store) s.g.syz[c] = n;
         }
@@ -455,18 +475,27 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
       const bool e_z = p >= n0 && p < nz - n0;
       if (FAST) {
         const long long cpl = (long long)p * pl + (long long)j0 * px + i0;
+        const float* R0 = rhs + (p & 3) * SLOT;
+        const float* R1 = rhs + ((p + 1) & 3) * SLOT;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
           const int r = r_own + q * 8 * RX;
+          const int b = b_own + q * 8 * BX;
           const long long c = cpl + (long long)(ty + 8 * q) * px + tx;
           const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
           const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
-          float vx = cvx[q] + s.dt_over_rho * (((sxx - Sxx[r - 1]) * s.odx + (sxy - Sxy[r - RX]) * s.ody) +
-                                               (sxz - Sxzm[r]) * s.odz);
-          float vy = cvy[q] + s.dt_over_rho * (((Sxy[r + 1] - sxy) * s.odx + (Syy[r + RX] - syy) * s.ody) +
-                                               (syz - Syzm[r]) * s.odz);
-          const float vz = cvz[q] + s.dt_over_rho * (((Sxz0[r + 1] - sxz) * s.odx + (syz - Syz0[r - RX]) * s.ody) +
-                                                     (Szz1[r] - szz) * s.odz);
+          float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
+          if (HET) {
+            fx = s.dt / R0[b];
+            fy = s.dt / (0.25f * (R0[b] + R0[b + 1] + R0[b + 1 + BX] + R0[b + BX]));
+            fz = s.dt / (0.25f * (R0[b] + R0[b + 1] + R1[b + 1] + R1[b]));
+          }
+          float vx = cvx[q] + fx * (((sxx - Sxx[r - 1]) * s.odx + (sxy - Sxy[r - RX]) * s.ody) +
+                                    (sxz - Sxzm[r]) * s.odz);
+          float vy = cvy[q] + fy * (((Sxy[r + 1] - sxy) * s.odx + (Syy[r + RX] - syy) * s.ody) +
+                                    (syz - Syzm[r]) * s.odz);
+          const float vz = cvz[q] + fz * (((Sxz0[r + 1] - sxz) * s.odx + (syz - Syz0[r - RX]) * s.ody) +
+                                          (Szz1[r] - szz) * s.odz);
           if (has_src && p == s.ksrc && oi == s.isrc && oj[q] == s.jsrc) {
             vx += src_x;
             vy += src_y;
@@ -476,11 +505,20 @@ __global__ void __launch_bounds__(FNT, (FAST || TY == 8) ? 3 : 2)
           vm2 = fmaxf(vm2, v2);
           bad |= not_finite(v2);
           if (e_z) {
-            ek.add(s.half_rho * v2);
-            const float exx = s.e_c1 * sxx - s.e_c2 * (syy + szz);
-            const float eyy = s.e_c1 * syy - s.e_c2 * (sxx + szz);
-            const float third = s.ep_physical ? (s.e_c1 * szz - s.e_c2 * (sxx + syy)) * szz : eyy * syy;
-            ep.add(0.5f * (exx * sxx + eyy * syy + third) + s.inv_2mu * (sxy * sxy + sxz * sxz + syz * syz));
+            float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
+            if (HET) {  // per-cell model of plane p (its smem slots may already hold later planes)
+              const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
+              const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
+              hr = 0.5f * R0[b];
+              c1 = 2.0f * (l + mu) * den;
+              c2 = l * den;
+              i2m = 1.0f / (2.0f * mu);
+            }
+            ek.add(hr * v2);
+            const float exx = c1 * sxx - c2 * (syy + szz);
+            const float eyy = c1 * syy - c2 * (sxx + szz);
+            const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
+            ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
           }
         }
       } else {
@@ -678,11 +716,11 @@ struct FusedPlan {
 static cudaError_t set_attr_for(int ty, bool het) {
   cudaError_t e;
   if (ty == 8) {
-    if ((e = set_smem_attr<8, true, false>()) != cudaSuccess) return e;
+    if ((e = het ? set_smem_attr<8, true, true>() : set_smem_attr<8, true, false>()) != cudaSuccess) return e;
     return het ? set_smem_attr<8, false, true>() : set_smem_attr<8, false, false>();
   }
   if (ty == 16) {
-    if ((e = set_smem_attr<16, true, false>()) != cudaSuccess) return e;
+    if ((e = het ? set_smem_attr<16, true, true>() : set_smem_attr<16, true, false>()) != cudaSuccess) return e;
     return het ? set_smem_attr<16, false, true>() : set_smem_attr<16, false, false>();
   }
   return cudaErrorInvalidValue;
@@ -726,7 +764,7 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
     const bool ys = ay.width() > 0 && (j0 - 1 < ay.lo || j0 + ty >= ny - ay.hi);
     const bool edge = i0 - 1 < 1 || i0 + FTX > nx - 2 || j0 - 1 < 1 || j0 + ty > ny - 2;
     const bool efull = i0 >= npml && i0 + FTX <= nx - npml && j0 >= npml && j0 + ty <= ny - npml;
-    return !het && !xs && !ys && !edge && efull;
+    return !xs && !ys && !edge && efull;
   };
   const bool has_inner = f1 > f0;
   std::vector<int2> all, inner, outer;
@@ -796,7 +834,8 @@ size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
 
 template <int TY>
 static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
-  const size_t smf = Geo<TY, false>::SMEM, smg = P->het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
+  const size_t smf = P->het ? Geo<TY, true>::SMEM : Geo<TY, false>::SMEM;
+  const size_t smg = P->het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
   // the general items run on the auxiliary stream, concurrently with the
   // interior items; exactly one of the two kernels records the receivers
   const bool both = P->n_fast > 0 && P->n_gen > 0;
@@ -813,9 +852,14 @@ static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int p
       fused3d_kernel<8, false, false><<<P->n_gen, FNT, smg, sg>>>(P->gmaps[parity], s, ls, P->items_gen,
                                                                    P->n_fast, 1);
   }
-  if (P->n_fast > 0)
-    fused3d_kernel<TY, true, false><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
-                                                                  P->n_gen > 0 ? 0 : 1);
+  if (P->n_fast > 0) {
+    if (P->het)
+      fused3d_kernel<TY, true, true><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
+                                                                   P->n_gen > 0 ? 0 : 1);
+    else
+      fused3d_kernel<TY, true, false><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
+                                                                    P->n_gen > 0 ? 0 : 1);
+  }
   if (both) {
     cudaEventRecord(P->join, P->aux);
     cudaStreamWaitEvent(st, P->join, 0);
