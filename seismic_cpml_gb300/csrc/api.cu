@@ -40,9 +40,9 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
                        bool het);
 bool fused3d_shape_ok(int ty, int depth);
 void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const Axis& az, int npml,
-                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen);
-void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, int n_gen,
-                       cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join);
+                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen, int n_cls[4]);
+void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, const int n_cls[4],
+                       const cudaStream_t aux[4], cudaEvent_t fork, const cudaEvent_t join[4]);
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st);
 }  // namespace cpml
 
@@ -76,8 +76,8 @@ struct cpml_handle {
   int kernel = 0;          // CPML_KERNEL_*
   int tile_y = 8, zchunk = 24, depth = 2;
   std::vector<unsigned char> plan;  // fused-path tensor maps and item lists
-  cudaStream_t aux = nullptr;       // second stream of the fused step's fork/join
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t aux[4] = {};         // streams of the fused step's fork/join (one per general class)
+  cudaEvent_t fork = nullptr, join[4] = {};
   int* err = nullptr;      // device error word
   float* prof32[3] = {};
   double* prof64[3] = {};
@@ -387,8 +387,9 @@ int configure_path(cpml_handle* h) {
                            h->px, h->tile_y, h->zchunk, h->depth, h->het))
       return CPML_ERR_CUDA;
     std::vector<int4> fast, gen;
+    int n_cls[4] = {0, 0, 0, 0};
     fused3d_items(h->nx, h->ny, h->nz, h->axes[0], h->axes[1], h->axes[2], h->p.npoints_pml, h->tile_y,
-                  h->zchunk, h->het, fast, gen);
+                  h->zchunk, h->het, fast, gen, n_cls);
     int4 *dfast = nullptr, *dgen = nullptr;
     if ((st = dalloc(h, &dfast, fast.size()))) return st;
     if ((st = dalloc(h, &dgen, gen.size()))) return st;
@@ -396,13 +397,14 @@ int configure_path(cpml_handle* h) {
       CK(cudaMemcpy(dfast, fast.data(), sizeof(int4) * fast.size(), cudaMemcpyHostToDevice));
     if (!gen.empty())
       CK(cudaMemcpy(dgen, gen.data(), sizeof(int4) * gen.size(), cudaMemcpyHostToDevice));
-    if (!h->aux) {
-      CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+    if (!h->fork) {
       CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
+      for (int c = 0; c < 4; ++c) {
+        CK(cudaStreamCreateWithFlags(&h->aux[c], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->join[c], cudaEventDisableTiming));
+      }
     }
-    fused3d_set_items(h->plan.data(), dfast, (int)fast.size(), dgen, (int)gen.size(), h->aux, h->fork,
-                      h->join);
+    fused3d_set_items(h->plan.data(), dfast, (int)fast.size(), dgen, n_cls, h->aux, h->fork, h->join);
     h->nblocks = int(fast.size() + gen.size());
   } else {
     StepArgs s = make_args(h);
@@ -824,10 +826,13 @@ void cpml_destroy(cpml_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graphs(h);
   for (void* p : h->allocs) cudaFree(p);
-  if (h->aux) cudaStreamSynchronize(h->aux);
+  for (int c = 0; c < 4; ++c)
+    if (h->aux[c]) cudaStreamSynchronize(h->aux[c]);
   if (h->fork) cudaEventDestroy(h->fork);
-  if (h->join) cudaEventDestroy(h->join);
-  if (h->aux) cudaStreamDestroy(h->aux);
+  for (int c = 0; c < 4; ++c) {
+    if (h->join[c]) cudaEventDestroy(h->join[c]);
+    if (h->aux[c]) cudaStreamDestroy(h->aux[c]);
+  }
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);

@@ -114,10 +114,22 @@ struct Geo {
   static constexpr int NH = 2 * FTX + 2 * TY;        // halo stress cells
 };
 
-template <int TY, bool FAST, bool HET>
-__global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
+// Item classes. Interior items take the lean path; the other four take the
+// general path, compiled per class so that a class whose items can touch
+// only one C-PML slab (and that axis's rigid faces) carries no code or
+// registers for the other two, and requests all of a plane's memory
+// variables at the top of the iteration (see below).
+enum : int { CLS_INTERIOR = 0, CLS_X = 1, CLS_Y = 2, CLS_Z = 3, CLS_GEN = 4 };
+
+template <int TY, int CLS, bool HET>
+__global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 8) ? 3 : 2))
     fused3d_kernel(const __grid_constant__ TmapSet tm, StepArgs s, int ls,
                    const int4* __restrict__ items, int item_base, int record) {
+  constexpr bool FAST = CLS == CLS_INTERIOR;
+  constexpr bool UX = CLS == CLS_X || CLS == CLS_GEN;   // x slab / x faces possible
+  constexpr bool UY = CLS == CLS_Y || CLS == CLS_GEN;
+  constexpr bool UZ = CLS == CLS_Z || CLS == CLS_GEN;
+  constexpr bool EARLY = CLS == CLS_X || CLS == CLS_Y || CLS == CLS_Z;
   using G = Geo<TY, HET>;
   constexpr int BX = G::BX, SLOT = G::SLOT, RX = G::RX, REG = G::REG;
   constexpr int NQ = TY / 8;             // own rows per thread
@@ -200,8 +212,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
   // ---- tile classification (uniform over the CTA) ---------------------------
   const int wx = s.ax.width(), wy = s.ay.width();
   const long long px = s.px, pl = s.plane;
-  const bool xs_tile = wx > 0 && (i0 - 1 < s.ax.lo || i0 + FTX >= nx - s.ax.hi);
-  const bool ys_tile = wy > 0 && (j0 - 1 < s.ay.lo || j0 + TY >= ny - s.ay.hi);
+  const bool xs_tile = UX && wx > 0 && (i0 - 1 < s.ax.lo || i0 + FTX >= nx - s.ax.hi);
+  const bool ys_tile = UY && wy > 0 && (j0 - 1 < s.ay.lo || j0 + TY >= ny - s.ay.hi);
   const bool edge_tile = i0 - 1 < 1 || i0 + FTX > nx - 2 || j0 - 1 < 1 || j0 + TY > ny - 2;
   const int n0 = s.npml;
   const bool e_full_xy = i0 >= n0 && i0 + FTX <= nx - n0 && j0 >= n0 && j0 + TY <= ny - n0;
@@ -248,6 +260,48 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
 
   for (int m = kk0; m <= ke; ++m) {
     const int use = m - kk0;
+    // Single-axis classes: every memory variable this iteration reads (own
+    // and halo stress cells at plane m, own velocity cells at plane m-1) is
+    // requested here, before the TMA wait, so one HBM round trip per plane
+    // overlaps all the work instead of three following one another.
+    float e_own[NQ][3], e_vel[NQ][3], e_halo[3];
+    if (EARLY) {
+      const int p = m - 1;
+      const bool sm_ok = m >= 0 && m < nz, vp_ok = p >= kb && p < ke;
+      const int szm = (CLS == CLS_Z && sm_ok) ? s.az.slab(m) : -1;
+      const int szp = (CLS == CLS_Z && vp_ok) ? s.az.slab(p) : -1;
+      // memory-variable index of cell (i, j, slab index sa) at plane k on the class axis
+      auto midx = [&](int k, int i, int j, int sx_, int sy_, int sz_) -> long long {
+        if (CLS == CLS_X) return (long long)k * ny * wx + (long long)j * wx + sx_;
+        if (CLS == CLS_Y) return (long long)k * wy * px + (long long)sy_ * px + i;
+        return (long long)sz_ * ny * px + (long long)j * px + i;
+      };
+      auto in_slab = [&](int sx_, int sy_, int sz_) {
+        if (CLS == CLS_X) return xs_tile && sx_ >= 0;
+        if (CLS == CLS_Y) return ys_tile && sy_ >= 0;
+        return sz_ >= 0;
+      };
+      const float* const* A = CLS == CLS_X ? s.m.x : (CLS == CLS_Y ? s.m.y : s.m.z);
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        e_own[q][0] = e_own[q][1] = e_own[q][2] = 0.f;
+        e_vel[q][0] = e_vel[q][1] = e_vel[q][2] = 0.f;
+        if (!ov[q]) continue;
+        if (sm_ok && in_slab(osx, osy[q], szm)) {
+          const long long mi = midx(m, oi, oj[q], osx, osy[q], szm);
+          e_own[q][0] = A[0][mi]; e_own[q][1] = A[1][mi]; e_own[q][2] = A[2][mi];
+        }
+        if (vp_ok && in_slab(osx, osy[q], szp)) {
+          const long long mi = midx(p, oi, oj[q], osx, osy[q], szp);
+          e_vel[q][0] = A[3][mi]; e_vel[q][1] = A[4][mi]; e_vel[q][2] = A[5][mi];
+        }
+      }
+      e_halo[0] = e_halo[1] = e_halo[2] = 0.f;
+      if (hv && sm_ok && in_slab(hsx, hsy, szm)) {
+        const long long mi = midx(m, hi, hj, hsx, hsy, szm);
+        e_halo[0] = A[0][mi]; e_halo[1] = A[1][mi]; e_halo[2] = A[2][mi];
+      }
+    }
     // every thread waits for load group g(m) itself (try_wait suspends the
     // thread in hardware), so there is one CTA barrier per plane
     const bool landed = mbar_wait_bounded(&bar[use & 1], (uint32_t)((use >> 1) & 1));
@@ -332,8 +386,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
       const float* M0 = mus + (m & 3) * SLOT;
       const float* M1 = mus + ((m + 1) & 3) * SLOT;
       const bool edge = edge_tile || m < 1 || m > nz - 2;
-      const int sz = s.az.slab(m);
-      const bool zs = sz >= 0;
+      const int sz = UZ ? s.az.slab(m) : -1;
+      const bool zs = UZ && sz >= 0;
       float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
       if (zs) {
         za = __ldg(s.az.a + m); zb = __ldg(s.az.b + m); zk = __ldg(s.az.ik + m);
@@ -346,7 +400,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
 
       // one stress cell: box/ring offsets, grid (i, j), slab indices,
       // components (1 normal, 2 xy, 4 xz, 8 yz); own = this CTA stores it
-      auto stress = [&](int b, int r, int i, int j, int sx, int sy, int comps, bool own) {
+      auto stress = [&](int b, int r, int i, int j, int sx, int sy, int comps, bool own, const float* pre) {
         const bool st = own && st_plane;
         const long long c = cpl + (long long)j * px + i;
         const bool hx = xs_tile && sx >= 0, hy = ys_tile && sy >= 0;
@@ -360,16 +414,21 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
         float xa = 0.f, xb = 0.f, xk = 1.f, xah = 0.f, xbh = 0.f, xkh = 1.f;
         float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
         if (hx) {
-          qx0 = s.m.x[0][mxi]; qx1 = s.m.x[1][mxi]; qx2 = s.m.x[2][mxi];
+          if (EARLY) { qx0 = pre[0]; qx1 = pre[1]; qx2 = pre[2]; }
+          else { qx0 = s.m.x[0][mxi]; qx1 = s.m.x[1][mxi]; qx2 = s.m.x[2][mxi]; }
           xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
           xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
         }
         if (hy) {
-          qy0 = s.m.y[0][myi]; qy1 = s.m.y[1][myi]; qy2 = s.m.y[2][myi];
+          if (EARLY) { qy0 = pre[0]; qy1 = pre[1]; qy2 = pre[2]; }
+          else { qy0 = s.m.y[0][myi]; qy1 = s.m.y[1][myi]; qy2 = s.m.y[2][myi]; }
           ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
           yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
         }
-        if (zs) { qz0 = s.m.z[0][mzi]; qz1 = s.m.z[1][mzi]; qz2 = s.m.z[2][mzi]; }
+        if (zs) {
+          if (EARLY) { qz0 = pre[0]; qz1 = pre[1]; qz2 = pre[2]; }
+          else { qz0 = s.m.z[0][mzi]; qz1 = s.m.z[1][mzi]; qz2 = s.m.z[2][mzi]; }
+        }
         // psi(n+1) = b psi(n) + a d ; d' = d / K + psi(n+1) (3D:846-852 and
         // the other sweeps); unchanged where the component is not updated
         auto psi = [&](float d, bool upd, float old, float* mB, long long mi, float a_, float b_, float k_) {
@@ -450,9 +509,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
         if (ov[q]) {
           const int b = b_own + q * 8 * BX;
           nvx[q] = VX0[b]; nvy[q] = VY0[b]; nvz[q] = VZ0[b];
-          stress(b, r_own + q * 8 * RX, oi, oj[q], osx, osy[q], 15, true);
+          stress(b, r_own + q * 8 * RX, oi, oj[q], osx, osy[q], 15, true, e_own[q]);
         }
-      if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false);
+      if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false, e_halo);
     }
     if (!__syncthreads_and(landed ? 1 : 0)) { ok_all = false; break; }
     // g(m+2) goes into slots whose last reader was stress(m) (own-cell
@@ -525,8 +584,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
         const float* R0 = rhs + (p & 3) * SLOT;
         const float* R1 = rhs + ((p + 1) & 3) * SLOT;
         const bool edge = edge_tile || p < 1 || p > nz - 2;
-        const int sz = s.az.slab(p);
-        const bool zs = sz >= 0;
+        const int sz = UZ ? s.az.slab(p) : -1;
+        const bool zs = UZ && sz >= 0;
         float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
         if (zs) {
           za = __ldg(s.az.a + p); zb = __ldg(s.az.b + p); zk = __ldg(s.az.ik + p);
@@ -552,16 +611,21 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((FAST || TY == 8) ? 3 : 2))
           float xa = 0.f, xb = 0.f, xk = 1.f, xah = 0.f, xbh = 0.f, xkh = 1.f;
           float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
           if (hx) {
-            qx3 = s.m.x[3][mxi]; qx4 = s.m.x[4][mxi]; qx5 = s.m.x[5][mxi];
+            if (EARLY) { qx3 = e_vel[q][0]; qx4 = e_vel[q][1]; qx5 = e_vel[q][2]; }
+            else { qx3 = s.m.x[3][mxi]; qx4 = s.m.x[4][mxi]; qx5 = s.m.x[5][mxi]; }
             xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
             xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
           }
           if (hy) {
-            qy3 = s.m.y[3][myi]; qy4 = s.m.y[4][myi]; qy5 = s.m.y[5][myi];
+            if (EARLY) { qy3 = e_vel[q][0]; qy4 = e_vel[q][1]; qy5 = e_vel[q][2]; }
+            else { qy3 = s.m.y[3][myi]; qy4 = s.m.y[4][myi]; qy5 = s.m.y[5][myi]; }
             ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
             yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
           }
-          if (zs) { qz3 = s.m.z[3][mzi]; qz4 = s.m.z[4][mzi]; qz5 = s.m.z[5][mzi]; }
+          if (zs) {
+            if (EARLY) { qz3 = e_vel[q][0]; qz4 = e_vel[q][1]; qz5 = e_vel[q][2]; }
+            else { qz3 = s.m.z[3][mzi]; qz4 = s.m.z[4][mzi]; qz5 = s.m.z[5][mzi]; }
+          }
           const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
           const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
           float d1 = (sxx - Sxx[r - 1]) * s.odx;   // v_x (3D:976-993)
@@ -695,36 +759,42 @@ static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, 
   return r == CUDA_SUCCESS;
 }
 
-template <int TY, bool FAST, bool HET>
+template <int TY, int CLS, bool HET>
 static cudaError_t set_smem_attr() {
-  return cudaFuncSetAttribute(fused3d_kernel<TY, FAST, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(fused3d_kernel<TY, CLS, HET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)Geo<TY, HET>::SMEM);
 }
 
 struct FusedPlan {
   TmapSet maps[2];  // maps[q] reads buffer set q (interior kernel, ty-row boxes)
-  TmapSet gmaps[2]; // the same for the general kernel's 8-row boxes
+  TmapSet gmaps[2]; // the same for the general kernels' 8-row boxes
   int ty, lz, depth;
   bool het;
   const int4* items_fast;  // device item lists
-  const int4* items_gen;
+  const int4* items_gen;   // general items, grouped by class X, Y, Z, GEN
   int n_fast, n_gen;
-  cudaStream_t aux;        // second stream of the fork/join
-  cudaEvent_t fork, join;
+  int n_cls[4];            // general items of class X, Y, Z, GEN
+  cudaStream_t aux[4];     // one stream per general class, forked from the step stream
+  cudaEvent_t fork, join[4];
 };
 
-static cudaError_t set_attr_for(int ty, bool het) {
+template <bool HET>
+static cudaError_t set_attr_het(int ty) {
   cudaError_t e;
   if (ty == 8) {
-    if ((e = het ? set_smem_attr<8, true, true>() : set_smem_attr<8, true, false>()) != cudaSuccess) return e;
-    return het ? set_smem_attr<8, false, true>() : set_smem_attr<8, false, false>();
+    if ((e = set_smem_attr<8, CLS_INTERIOR, HET>()) != cudaSuccess) return e;
+  } else if (ty == 16) {
+    if ((e = set_smem_attr<16, CLS_INTERIOR, HET>()) != cudaSuccess) return e;
+  } else {
+    return cudaErrorInvalidValue;
   }
-  if (ty == 16) {
-    if ((e = het ? set_smem_attr<16, true, true>() : set_smem_attr<16, true, false>()) != cudaSuccess) return e;
-    return het ? set_smem_attr<16, false, true>() : set_smem_attr<16, false, false>();
-  }
-  return cudaErrorInvalidValue;
+  if ((e = set_smem_attr<8, CLS_X, HET>()) != cudaSuccess) return e;
+  if ((e = set_smem_attr<8, CLS_Y, HET>()) != cudaSuccess) return e;
+  if ((e = set_smem_attr<8, CLS_Z, HET>()) != cudaSuccess) return e;
+  return set_smem_attr<8, CLS_GEN, HET>();
 }
+
+static cudaError_t set_attr_for(int ty, bool het) { return het ? set_attr_het<true>(ty) : set_attr_het<false>(ty); }
 
 bool fused3d_shape_ok(int ty, int d) { return (ty == 8 || ty == 16) && d == 2; }
 
@@ -740,10 +810,15 @@ size_t fused3d_smem(int ty, int d, bool het) {
 // tile plus halo avoids every x/y slab, face and the energy boundary, and all
 // its stress planes kb-1..ke avoid the z slabs and the z faces. Interior
 // chunks are cut from the planes [zi0 + 1, zi1 - 1); the rest of each
-// column, and every other tile, is general. The z-chunk is the outermost
-// loop so concurrently resident CTAs share their halos in L2.
+// column, and every other tile, is general, cut at the same plane bounds so
+// that a general chunk lies either inside or outside the z slabs. General
+// items are grouped by class: X, Y or Z when the only C-PML slab they can
+// touch is that axis's, GEN otherwise (n_cls gets the four counts). The
+// z-chunk is the outermost loop so concurrently resident CTAs share their
+// halos in L2.
 void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const Axis& az, int npml,
-                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen) {
+                   int ty, int lz, bool het, std::vector<int4>& fast, std::vector<int4>& gen, int n_cls[4]) {
+  (void)het;
   fast.clear();
   gen.clear();
   const int ntx = (nx + FTX - 1) / FTX, nty = (ny + ty - 1) / ty;
@@ -768,21 +843,35 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
   };
   const bool has_inner = f1 > f0;
   std::vector<int2> all, inner, outer;
-  chunks(0, nz, all);
   if (has_inner) {
+    chunks(0, f0, all);
+    chunks(f0, f1, all);
+    chunks(f1, nz, all);
     chunks(f0, f1, inner);
     chunks(0, f0, outer);
     chunks(f1, nz, outer);
+  } else {
+    chunks(0, nz, all);
   }
-  // Interior tiles have ty rows; the general kernel always uses 8-row tiles
-  // (a smaller footprint gives it three CTAs per SM), which split every
+  // Interior tiles have ty rows; the general kernels always use 8-row tiles
+  // (a smaller footprint gives them three CTAs per SM), which split every
   // ty-row tile exactly.
   for (const int2& z : inner)
     for (int tyi = 0; tyi < nty; ++tyi)
       for (int txi = 0; txi < ntx; ++txi)
         if (interior_tile(txi * FTX, tyi * ty)) fast.push_back(make_int4(txi * FTX, tyi * ty, z.x, z.y));
+  std::vector<int4> cls[4];
+  // the slab tests of the general kernel (xs_tile, ys_tile, z slab of planes kb-1..ke)
   auto add_gen = [&](int i0, int j0, const int2& z) {
-    for (int jj = j0; jj < j0 + ty && jj < ny; jj += 8) gen.push_back(make_int4(i0, jj, z.x, z.y));
+    for (int jj = j0; jj < j0 + ty && jj < ny; jj += 8) {
+      const bool xsl = ax.width() > 0 && (i0 - 1 < ax.lo || i0 + FTX >= nx - ax.hi);
+      const bool ysl = ay.width() > 0 && (jj - 1 < ay.lo || jj + 8 >= ny - ay.hi);
+      const int mlo = z.x - 1 > 0 ? z.x - 1 : 0, mhi = z.y < nz - 1 ? z.y : nz - 1;
+      const bool zsl = az.width() > 0 && (mlo < az.lo || mhi >= nz - az.hi);
+      const int k = (xsl ? 1 : 0) + (ysl ? 1 : 0) + (zsl ? 1 : 0);
+      const int c = k != 1 ? 3 : (xsl ? 0 : (ysl ? 1 : 2));
+      cls[c].push_back(make_int4(i0, jj, z.x, z.y));
+    }
   };
   for (const int2& z : all)
     for (int tyi = 0; tyi < nty; ++tyi)
@@ -792,6 +881,10 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
     for (int tyi = 0; tyi < nty; ++tyi)
       for (int txi = 0; txi < ntx; ++txi)
         if (interior_tile(txi * FTX, tyi * ty)) add_gen(txi * FTX, tyi * ty, z);
+  for (int c = 0; c < 4; ++c) {
+    n_cls[c] = (int)cls[c].size();
+    gen.insert(gen.end(), cls[c].begin(), cls[c].end());
+  }
 }
 
 // Build the tensor maps of both buffer sets. fields[q][f] = field f of set q.
@@ -822,48 +915,67 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
   return true;
 }
 
-void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, int n_gen,
-                       cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
+void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, const int n_cls[4],
+                       const cudaStream_t aux[4], cudaEvent_t fork, const cudaEvent_t join[4]) {
   FusedPlan* P = static_cast<FusedPlan*>(plan_mem);
   P->items_fast = fast; P->n_fast = n_fast;
-  P->items_gen = gen; P->n_gen = n_gen;
-  P->aux = aux; P->fork = fork; P->join = join;
+  P->items_gen = gen;
+  P->n_gen = 0;
+  for (int c = 0; c < 4; ++c) {
+    P->n_cls[c] = n_cls[c];
+    P->n_gen += n_cls[c];
+    P->aux[c] = aux[c];
+    P->join[c] = join[c];
+  }
+  P->fork = fork;
 }
 
 size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
 
+template <int TY, bool HET>
+static void launch_classes(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
+  const size_t smf = Geo<TY, HET>::SMEM, smg = Geo<8, HET>::SMEM;
+  // Every general class runs on its own auxiliary stream, concurrently with
+  // the interior items on the step stream (forked and joined with events, so
+  // a captured graph holds the same fan-out). Exactly one kernel records the
+  // receivers: the first class with items, or the interior kernel.
+  int recorder = -1;
+  for (int c = 0; c < 4 && recorder < 0; ++c)
+    if (P->n_cls[c] > 0) recorder = c;
+  if (P->n_gen > 0) {
+    cudaEventRecord(P->fork, st);
+    int off = 0;
+    for (int c = 0; c < 4; ++c) {
+      const int n = P->n_cls[c];
+      if (n > 0) {
+        cudaStreamWaitEvent(P->aux[c], P->fork, 0);
+        const int4* it = P->items_gen + off;
+        const int base = P->n_fast + off, rec = c == recorder ? 1 : 0;
+        cudaStream_t sc = P->aux[c];
+        if (c == 0) fused3d_kernel<8, CLS_X, HET><<<n, FNT, smg, sc>>>(P->gmaps[parity], s, ls, it, base, rec);
+        if (c == 1) fused3d_kernel<8, CLS_Y, HET><<<n, FNT, smg, sc>>>(P->gmaps[parity], s, ls, it, base, rec);
+        if (c == 2) fused3d_kernel<8, CLS_Z, HET><<<n, FNT, smg, sc>>>(P->gmaps[parity], s, ls, it, base, rec);
+        if (c == 3) fused3d_kernel<8, CLS_GEN, HET><<<n, FNT, smg, sc>>>(P->gmaps[parity], s, ls, it, base, rec);
+      }
+      off += n;
+    }
+  }
+  if (P->n_fast > 0)
+    fused3d_kernel<TY, CLS_INTERIOR, HET><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
+                                                                       recorder < 0 ? 1 : 0);
+  for (int c = 0; c < 4; ++c)
+    if (P->n_cls[c] > 0) {
+      cudaEventRecord(P->join[c], P->aux[c]);
+      cudaStreamWaitEvent(st, P->join[c], 0);
+    }
+}
+
 template <int TY>
 static cudaError_t launch_t(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
-  const size_t smf = P->het ? Geo<TY, true>::SMEM : Geo<TY, false>::SMEM;
-  const size_t smg = P->het ? Geo<8, true>::SMEM : Geo<8, false>::SMEM;
-  // the general items run on the auxiliary stream, concurrently with the
-  // interior items; exactly one of the two kernels records the receivers
-  const bool both = P->n_fast > 0 && P->n_gen > 0;
-  if (both) {
-    cudaEventRecord(P->fork, st);
-    cudaStreamWaitEvent(P->aux, P->fork, 0);
-  }
-  cudaStream_t sg = both ? P->aux : st;
-  if (P->n_gen > 0) {
-    if (P->het)
-      fused3d_kernel<8, false, true><<<P->n_gen, FNT, smg, sg>>>(P->gmaps[parity], s, ls, P->items_gen,
-                                                                  P->n_fast, 1);
-    else
-      fused3d_kernel<8, false, false><<<P->n_gen, FNT, smg, sg>>>(P->gmaps[parity], s, ls, P->items_gen,
-                                                                   P->n_fast, 1);
-  }
-  if (P->n_fast > 0) {
-    if (P->het)
-      fused3d_kernel<TY, true, true><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
-                                                                   P->n_gen > 0 ? 0 : 1);
-    else
-      fused3d_kernel<TY, true, false><<<P->n_fast, FNT, smf, st>>>(P->maps[parity], s, ls, P->items_fast, 0,
-                                                                    P->n_gen > 0 ? 0 : 1);
-  }
-  if (both) {
-    cudaEventRecord(P->join, P->aux);
-    cudaStreamWaitEvent(st, P->join, 0);
-  }
+  if (P->het)
+    launch_classes<TY, true>(P, s, ls, parity, st);
+  else
+    launch_classes<TY, false>(P, s, ls, parity, st);
   return cudaGetLastError();
 }
 
