@@ -173,7 +173,15 @@ def test_network_gradients_match_fp64_oracle(L):
     from seismic_cpml_gb300.surrogate import NetConfig, Surrogate, dct_basis
     cfg = NetConfig(**SMALL)
     net = Surrogate(cfg, seed=3)
-    # make the BF16 copies exact so that the oracle sees the same weights
+    # generic weights (the product's near-zero output-layer init would make
+    # the trunk gradients tiny), rounded to BF16 so the oracle sees the same
+    # values the tensor cores multiply
+    wr = np.random.default_rng(12)
+    gen = {}
+    for name, shp in cfg.param_shapes():
+        scale = np.sqrt(2.0 / shp[1]) if name.endswith("_w") else 0.05
+        gen[name] = wr.standard_normal(shp) * scale
+    net.set_params(gen)
     net.w.copy_(net.w.to(torch.bfloat16).float())
     net.refresh_bf16()
     params = net.get_params()
@@ -192,11 +200,12 @@ def test_network_gradients_match_fp64_oracle(L):
                                      cfg.modes, cfg.head_weight)
     assert np.allclose(S_["loss"][:B].cpu().numpy(), loss, rtol=3e-2)
     assert np.allclose(S_["head"][:B].cpu().numpy(), head, rtol=3e-2, atol=3e-2)
+    errs = {}
     for name, _ in cfg.param_shapes():
         got = net.G[name].cpu().double().numpy()
         ref = g[name]
-        rel = np.linalg.norm(got - ref) / (np.linalg.norm(ref) + 1e-30)
-        assert rel < 5e-2, (name, rel)
+        errs[name] = np.linalg.norm(got - ref) / (np.linalg.norm(ref) + 1e-30)
+    assert max(errs.values()) < 5e-2, errs
 
 
 def test_training_fits_a_small_problem(L):
