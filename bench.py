@@ -325,9 +325,11 @@ def run_ours(args, world, rank, local, pg):
         cores = os.cpu_count() or 1
         sample = args.cpu_sample_steps or 12
         v, dt = cpu_baseline(p, sample, cores)
+        v1, dt1 = cpu_baseline(p, 2, 1)
         cpu = {"value": round(v, 3), "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
                "sample": f"{sample} time steps of the 276^3 grid ({dt:.1f} s), FP64 C++ "
-                         "restatement of the reference time loop, OpenMP"}
+                         "restatement of the reference time loop, OpenMP",
+               "value_1core": round(v1, 3), "sample_1core": f"2 time steps on one thread ({dt1:.1f} s)"}
 
     chunks = n_chunks(p.nstep, p.it_display)
     line = {
@@ -432,12 +434,14 @@ def run_surrogate(args, world, rank, local, pg):
     clocks = ClockSampler(local)
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = net.launches
     ev0.record()
     for _ in range(args.steps):
         net.predict(Xv, Sv, out=P)
     ev1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
+    launches = net.launches - launches0
     dev_ms = ev0.elapsed_time(ev1)
     nn_rate = args.steps * args.test_shots / (dev_ms / 1e3)
     flops = surrogate_flops_per_shot(cfg)
@@ -503,7 +507,7 @@ def run_surrogate(args, world, rank, local, pg):
                      "flops_per_shot": flops},
         "cpu_baseline": None,
         "e2e": e2e,
-        "gpu_launches": args.steps * (-(-args.test_shots // 512)) * (2 * len(cfg.chans) + 4),
+        "gpu_launches": launches,
         "clocks": clk,
     }
     if rank == 0:

@@ -263,6 +263,14 @@ int cpml_energy3d_noalloc(const float* const* fields, int nx, int ny, int nz, in
 int cpml_nn_gemm(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb,
                  float* Cf, void* Cb, int ldc, const float* bias, int relu, int accum, float alpha,
                  int splits, float* work, long long work_elems, void* stream);
+/* The same contract as cpml_nn_gemm on the 5th-generation tensor cores
+   (tcgen05.mma, accumulator in tensor memory, 128 x 128 output tiles). */
+int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb,
+                    float* Cf, void* Cb, int ldc, const float* bias, int relu, int accum, float alpha,
+                    int splits, float* work, long long work_elems, void* stream);
+/* *err = whether a bounded tensor-core wait gave up since the last call
+   (1) or not (0); resets the flag. Synchronous. */
+int cpml_nn_error(int* err);
 /* 3x3 stride-2 pad-1 patches of an NHWC bf16 [B][H][W][C] activation:
    out [B*Ho*Wo][9*C] bf16, Ho = (H+1)/2, column (ky*3+kx)*C + c. */
 int cpml_nn_im2col(const void* in, void* out, int B, int H, int W, int C, void* stream);

@@ -7,6 +7,7 @@
 //                     m16n8k16, FP32 accumulation), optional split-K with a
 //                     fixed-order reduction, fused bias + ReLU epilogue,
 //                     FP32 and/or BF16 output, optional accumulate
+//   cpml_nn_gemm_tc   the same contract on tcgen05.mma with a TMEM accumulator
 //   cpml_nn_im2col    3x3 stride-2 pad-1 patches of an NHWC BF16 activation
 //   cpml_nn_col2im    its adjoint, as a gather (fixed order, no atomics)
 //   cpml_nn_relu_bwd  dX = dY * (Y > 0), FP32 in, BF16 and/or FP32 out
@@ -311,6 +312,209 @@ __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ w
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same GEMM on the 5th-generation tensor cores: tcgen05.mma with the
+// accumulator in tensor memory. A CTA of 4 warps owns a 128 x 128 output
+// tile; operand tiles of 64 k-values are staged into shared memory in the
+// canonical K-major, non-swizzled core-matrix layout (8 rows x 16 bytes per
+// core matrix, core matrices 128 B apart along k and 1 KB apart along m/n),
+// two stages deep: while the tensor core works on one stage, the threads
+// fill the other. One thread issues the MMAs (4 x K=16 per stage) and
+// commits them to the stage's mbarrier; the 128 fp32 accumulator columns are
+// read back with tcgen05.ld (warp w reads TMEM lanes 32w..32w+31 = rows).
+// ---------------------------------------------------------------------------
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 64, NT = 128, STAGES = 2;
+constexpr int TILE_BYTES = BM * BK * 2;                    // 16 KB per operand tile (BM == BN)
+constexpr int STAGE_BYTES = 2 * TILE_BYTES;
+constexpr int SMEM = STAGES * STAGE_BYTES + 64;
+constexpr uint32_t LBO = 128, SBO = 1024;                  // k- and m/n-direction core-matrix strides
+constexpr long long kWait = 2000000000LL;                  // ~1 s at 2 GHz
+
+// Instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit
+// 17, M >> 4 at bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start >> 4, LBO >> 4 at bit 16, SBO >> 4
+// at bit 32, descriptor version 1 at bit 46, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((LBO >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((SBO >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+// byte offset of element (r, k) of a staged tile
+__device__ __forceinline__ int core_off(int r, int k) {
+  return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Stage rows [r0, r0 + 128) x k-values [k0, k0 + 64) of a bf16 operand into
+// `tile`; trans == 0: element (r, k) at src[r * ld + k], else at src[k * ld + r].
+// Out-of-range elements are zero.
+__device__ __forceinline__ void stage(unsigned char* tile, const __nv_bfloat16* __restrict__ src, int ld, int trans,
+                                      int r0, int R, int k0, int ke) {
+  const int tid = threadIdx.x;
+  if (!trans) {
+    const bool vec = (ld & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    // 128 rows x 8 groups of 8 k-values; consecutive threads take consecutive groups
+    for (int e = tid; e < BM * (BK / 8); e += NT) {
+      const int r = e >> 3, g = e & 7;
+      const int gr = r0 + r, gk = k0 + g * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gr < R) {
+        if (vec && gk + 8 <= ke) {
+          v = *reinterpret_cast<const uint4*>(src + (size_t)gr * ld + gk);
+        } else {
+          __nv_bfloat16 t[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            t[q] = (gk + q < ke) ? src[(size_t)gr * ld + gk + q] : __float2bfloat16(0.f);
+          v = *reinterpret_cast<const uint4*>(t);
+        }
+      }
+      *reinterpret_cast<uint4*>(tile + core_off(r, g * 8)) = v;
+    }
+  } else {
+    // consecutive threads take consecutive rows (contiguous in memory)
+    for (int e = tid; e < BM * BK; e += NT) {
+      const int r = e & (BM - 1), k = e >> 7;
+      const int gr = r0 + r, gk = k0 + k;
+      const __nv_bfloat16 v = (gr < R && gk < ke) ? src[(size_t)gk * ld + gr] : __float2bfloat16(0.f);
+      *reinterpret_cast<__nv_bfloat16*>(tile + core_off(r, k)) = v;
+    }
+  }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWait) return false;
+  }
+}
+
+}  // namespace tc
+
+__device__ int g_nn_err;  // set when a bounded tensor-core wait gives up
+
+__global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, int kchunk,
+                                                        const __nv_bfloat16* __restrict__ A, int lda, int ta,
+                                                        const __nv_bfloat16* __restrict__ B, int ldb, int tb,
+                                                        Epilogue ep, float* __restrict__ work) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + STAGES * STAGE_BYTES + 32);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  const int nk = ke > kb ? (ke - kb + BK - 1) / BK : 0;
+
+  if (warp == 0) {  // 128 fp32 accumulator columns for the 128 x 128 tile
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(128)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&bar[s])), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  bool ok = true;
+  for (int kt = 0; kt < nk && ok; ++kt) {
+    const int s = kt & 1;
+    unsigned char* sa = smem + s * STAGE_BYTES;
+    unsigned char* sb = sa + TILE_BYTES;
+    // the MMAs that last read this stage (k-tile kt - 2) must have finished
+    if (kt >= STAGES) ok = mbar_wait(&bar[s], (uint32_t)(((kt - STAGES) >> 1) & 1));
+    if (!__syncthreads_and(ok ? 1 : 0)) { ok = false; break; }
+    const int k0 = kb + kt * BK;
+    stage(sa, A, lda, ta, m0, M, k0, ke);
+    stage(sb, B, ldb, tb ? 0 : 1, n0, N, k0, ke);
+    // make the generic-proxy stores visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int ks = 0; ks < BK / 16; ++ks) {
+        const uint64_t da = desc(smem_addr(sa) + ks * 2 * LBO);
+        const uint64_t db = desc(smem_addr(sb) + ks * 2 * LBO);
+        const uint32_t acc = (kt > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(IDESC), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_addr(&bar[s]))
+                   : "memory");
+    }
+  }
+  // all MMAs done: the last commit covers every earlier one of this thread
+  if (ok && nk > 0) ok = mbar_wait(&bar[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1));
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: tcgen05.ld below is warp-collective
+  if (!ok && tid == 0) atomicOr(&g_nn_err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  // epilogue: warp w owns rows 32w..32w+31, one row per thread
+  const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+  for (int c = 0; c < BN; c += 16) {
+    uint32_t r[16];
+    if (ok && nk > 0) {
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) r[q] = 0u;  // empty K range (or a failed wait): zero
+    }
+    if (row < M) {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int col = n0 + c + q;
+        if (col >= N) break;
+        const float v = __uint_as_float(r[q]);
+        if (work)
+          work[((size_t)blockIdx.z * M + row) * N + col] = v;
+        else
+          epilogue_store(ep, row, col, v);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
+}
+
 int grid_for(long long n) {
   long long b = (n + 255) / 256;
   return (int)(b > 8192 ? 8192 : (b < 1 ? 1 : b));
@@ -342,6 +546,42 @@ int cpml_nn_gemm(int M, int N, int K, const void* A, int lda, int ta, const void
                                         (const __nv_bfloat16*)B, ldb, tb, ep, splits > 1 ? work : nullptr);
   if (splits > 1) gemm_reduce_kernel<<<grid_for((long long)M * N), 256, 0, st>>>(M, N, splits, work, ep);
   return status();
+}
+
+int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb, float* Cf,
+                    void* Cb, int ldc, const float* bias, int relu, int accum, float alpha, int splits, float* work,
+                    long long work_elems, void* stream) {
+  if (M < 0 || N < 0 || K < 0 || !A || !B || (!Cf && !Cb) || splits < 1) return CPML_ERR_INVALID;
+  if (accum && !Cf) return CPML_ERR_INVALID;
+  if (M == 0 || N == 0) return CPML_OK;
+  if ((N + tc::BN - 1) / tc::BN > 65535) return CPML_ERR_RANGE;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM) != cudaSuccess)
+      return CPML_ERR_CUDA;
+    attr = true;
+  }
+  int kchunk = (K + splits - 1) / splits;
+  kchunk = ((kchunk + tc::BK - 1) / tc::BK) * tc::BK;
+  if (kchunk < tc::BK) kchunk = tc::BK;
+  splits = K > 0 ? (K + kchunk - 1) / kchunk : 1;
+  if (splits > 65535) return CPML_ERR_RANGE;
+  if (splits > 1 && (!work || work_elems < (long long)splits * M * N)) return CPML_ERR_INVALID;
+  const Epilogue ep{Cf, (__nv_bfloat16*)Cb, ldc, bias, relu, accum, alpha};
+  const dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN, splits);
+  cudaStream_t st = (cudaStream_t)stream;
+  gemm_tc_kernel<<<grid, tc::NT, tc::SMEM, st>>>(M, N, K, kchunk, (const __nv_bfloat16*)A, lda, ta,
+                                                  (const __nv_bfloat16*)B, ldb, tb, ep, splits > 1 ? work : nullptr);
+  if (splits > 1) gemm_reduce_kernel<<<grid_for((long long)M * N), 256, 0, st>>>(M, N, splits, work, ep);
+  return status();
+}
+
+int cpml_nn_error(int* err) {
+  if (!err) return CPML_ERR_INVALID;
+  int zero = 0;
+  if (cudaMemcpyFromSymbol(err, g_nn_err, sizeof(int)) != cudaSuccess) return CPML_ERR_CUDA;
+  if (cudaMemcpyToSymbol(g_nn_err, &zero, sizeof(int)) != cudaSuccess) return CPML_ERR_CUDA;
+  return CPML_OK;
 }
 
 int cpml_nn_im2col(const void* in, void* out, int B, int H, int W, int C, void* stream) {

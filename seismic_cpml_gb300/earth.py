@@ -54,19 +54,21 @@ def layered_model(shape, nlayers, cp_lo, cp_hi, seed, anomalies=0, amp=0.1, radi
 def layered_model_3d_device(shape, nlayers=6, cp_lo=1800.0, cp_hi=5000.0, anomalies=8, amp=0.15,
                             radius=(20.0, 80.0), seed=3, device="cuda"):
     """(lambda, mu, rho) as FP32 torch tensors on `device`, shape (nz, ny, nx):
-    `nlayers` horizontal layers stacked along z (z is up) with cp uniform in
-    [cp_lo, cp_hi], times 1 +/- amp Gaussian anomalies with radius uniform in
-    `radius` cells (each a separable product of three 1-D Gaussians), then
-    cs = cp / sqrt(3) and Gardner density. Built on the device because the
-    large workloads hold hundreds of millions of cells; the seeded parameters
-    come from numpy so the model is the same on every machine."""
+    `nlayers` horizontal layers stacked along y (the reference's vertical
+    axis) at sorted uniform depths with cp uniform in [cp_lo, cp_hi], times
+    1 +/- amp Gaussian anomalies with radius uniform in `radius` cells and
+    centres uniform in the grid (each a separable product of three 1-D
+    Gaussians), then cs = cp / sqrt(3) and Gardner density. Built on the
+    device because the large workloads hold hundreds of millions of cells; the
+    seeded parameters come from numpy (PCG64) so the model is the same on
+    every machine."""
     import torch
     rng = np.random.default_rng(seed)
     nz, ny, nx = shape
-    tops = np.sort(rng.uniform(0, nz, nlayers - 1))
+    tops = np.sort(rng.uniform(0, ny, nlayers - 1))
     vals = rng.uniform(cp_lo, cp_hi, nlayers)
-    prof = torch.tensor(vals[np.searchsorted(tops, np.arange(nz))], dtype=torch.float32, device=device)
-    cp = prof.view(nz, 1, 1).expand(nz, ny, nx).contiguous()
+    prof = torch.tensor(vals[np.searchsorted(tops, np.arange(ny))], dtype=torch.float32, device=device)
+    cp = prof.view(1, ny, 1).expand(nz, ny, nx).contiguous()
     axes = [torch.arange(n, dtype=torch.float32, device=device) for n in (nz, ny, nx)]
     for _ in range(anomalies):
         c = [rng.uniform(0, n) for n in (nz, ny, nx)]

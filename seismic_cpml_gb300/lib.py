@@ -65,6 +65,10 @@ SIGNATURES = [
     ("cpml_nn_gemm", ctypes.c_int, [ctypes.c_int] * 3 + [_vp, ctypes.c_int, ctypes.c_int] * 2
      + [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, _vp,
         ctypes.c_longlong, _vp]),
+    ("cpml_nn_gemm_tc", ctypes.c_int, [ctypes.c_int] * 3 + [_vp, ctypes.c_int, ctypes.c_int] * 2
+     + [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, _vp,
+        ctypes.c_longlong, _vp]),
+    ("cpml_nn_error", ctypes.c_int, [_ip]),
     ("cpml_nn_im2col", ctypes.c_int, [_vp, _vp] + [ctypes.c_int] * 4 + [_vp]),
     ("cpml_nn_col2im", ctypes.c_int, [_vp, _vp] + [ctypes.c_int] * 4 + [_vp]),
     ("cpml_nn_relu_bwd", ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_longlong, _vp]),

@@ -197,12 +197,13 @@ def config_3d_plain(n_interior: int = 256, nstep: int = 2500) -> tuple[CpmlParam
 
 def config_3d_large(n_interior: int = 800, nstep: int = 4000, deltat: float = 4.0e-4,
                     nrec_side: int = 201) -> tuple[CpmlParams, list]:
-    """3D large: (800 + 2*10)^3, DELTA = 5 m, Ricker f0 = 12 Hz, a
-    201 x 201 receiver grid on the top interior plane (z is up), the source
-    at the x-y centre ten cells below that plane; NSTEP = 4000. The per-cell
-    layered model comes from earth.layered_model_3d_device. DELTAT is 0.4 ms:
-    with cp up to 5000 m/s and +15 % anomalies, 0.8 ms would give a Courant
-    number of 1.39-1.59 and the reference's check (3D:712-717) would stop."""
+    """3D large: (800 + 2*10)^3, DELTA = 5 m, Ricker f0 = 12 Hz at the
+    centre, NSTEP = 4000, a 201 x 201 receiver grid on the plane one below
+    the top interior plane in y (y is the vertical axis), at i, k = 11 + 4 m.
+    The per-cell layered model comes from earth.layered_model_3d_device.
+    DELTAT is 0.4 ms: with cp up to 5000 m/s and +15 % anomalies, 0.8 ms
+    would give a Courant number of 1.39-1.59 and the reference's check
+    (3D:712-717) would stop."""
     p = default_3d()
     n = n_interior + 2 * p.npoints_pml
     p.nx = p.ny = p.nz = n
@@ -216,15 +217,12 @@ def config_3d_large(n_interior: int = 800, nstep: int = 4000, deltat: float = 4.
     p.cs = p.cp / 1.7320508075688772
     p.rho = 310.0 * p.cp ** 0.25
     c = n // 2
-    ktop = n - p.npoints_pml          # 1-based top interior plane
-    p.isource, p.jsource, p.ksource = c, c, ktop - 10
+    p.isource, p.jsource, p.ksource = c, c, c
     p.it_display = 100
-    rec = []
-    for b_ in range(nrec_side):
-        j = p.npoints_pml + 1 + int(round(b_ * (n_interior - 1) / (nrec_side - 1)))
-        for a_ in range(nrec_side):
-            i = p.npoints_pml + 1 + int(round(a_ * (n_interior - 1) / (nrec_side - 1)))
-            rec.append((i, j, ktop))
+    jr = n - p.npoints_pml - 1                       # 1-based
+    step = (n_interior - 1) / (nrec_side - 1)
+    idx = [p.npoints_pml + 1 + int(round(m * step)) for m in range(nrec_side)]
+    rec = [(i, jr, k) for k in idx for i in idx]
     return p, rec
 
 

@@ -98,28 +98,18 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-class _Checked:
-    """Calls library entry points and raises CpmlError on a non-zero status."""
-
-    def __init__(self, lib):
-        self._lib = lib
-
-    def __getattr__(self, name):
-        fn = getattr(self._lib, name)
-
-        def call(*args):
-            _L.check(fn(*args), name)
-        return call
-
-
 class Surrogate:
     """Weights, Adam state and per-batch-size work buffers on one GPU."""
 
-    def __init__(self, cfg: NetConfig = NetConfig(), seed: int = 0, device: str = "cuda"):
+    def __init__(self, cfg: NetConfig = NetConfig(), seed: int = 0, device: str = "cuda", gemm: str = "mma"):
         if not torch.cuda.is_available():
             raise RuntimeError("the surrogate needs a CUDA device")
+        if gemm not in ("mma", "tcgen05"):
+            raise ValueError("gemm is 'mma' (mma.sync) or 'tcgen05'")
         self.L = _L.load()
         self.cfg = cfg
+        self.gemm_entry = "cpml_nn_gemm_tc" if gemm == "tcgen05" else "cpml_nn_gemm"
+        self.launches = 0        # kernels this object has launched (launch accounting)
         self.dev = torch.device(device)
         self.shapes = cfg.param_shapes()
         self.off, o = {}, 0
@@ -163,7 +153,7 @@ class Surrogate:
         self.refresh_bf16()
 
     def refresh_bf16(self):
-        _L.check(self.L.cpml_nn_cast(_ptr(self.w), _ptr(self.wb), self.n, self._stream()), "cpml_nn_cast")
+        self._call("cpml_nn_cast", _ptr(self.w), _ptr(self.wb), self.n, self._stream())
 
     def get_params(self):
         return {name: self.P[name].detach().cpu().numpy().astype(np.float64) for name, _ in self.shapes}
@@ -188,18 +178,24 @@ class Surrogate:
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
+    def _call(self, name, *args, kernels=1):
+        """One library entry point; raises CpmlError on a non-zero status and
+        counts the kernels it launches."""
+        _L.check(getattr(self.L, name)(*args), name)
+        self.launches += kernels
+
     def _gemm(self, M, N, K, A, lda, ta, B, ldb, tb, Cf=None, Cb=None, ldc=None, bias=None, relu=0,
               accum=0, alpha=1.0, work=None):
-        tiles = -(-M // 64) * -(-N // 64)
+        tm = 128 if self.gemm_entry == "cpml_nn_gemm_tc" else 64
+        tiles = -(-M // tm) * -(-N // tm)
         splits = max(1, min(K // 512, -(-2 * SM_COUNT // tiles)))
         wk = work if splits > 1 else None
         if wk is not None and wk.numel() < splits * M * N:
             splits = max(1, wk.numel() // (M * N))
             wk = wk if splits > 1 else None
-        _L.check(self.L.cpml_nn_gemm(M, N, K, _ptr(A), lda, ta, _ptr(B), ldb, tb, _ptr(Cf), _ptr(Cb),
-                                     ldc if ldc is not None else N, _ptr(bias), relu, accum, alpha, splits,
-                                     _ptr(wk), wk.numel() if wk is not None else 0, self._stream()),
-                 "cpml_nn_gemm")
+        self._call(self.gemm_entry, M, N, K, _ptr(A), lda, ta, _ptr(B), ldb, tb, _ptr(Cf), _ptr(Cb),
+                   ldc if ldc is not None else N, _ptr(bias), relu, accum, alpha, splits,
+                   _ptr(wk), wk.numel() if wk is not None else 0, self._stream(), kernels=2 if splits > 1 else 1)
 
     def _buffers(self, B):
         if B in self._bufs:
@@ -247,7 +243,7 @@ class Surrogate:
         for l, (H, W, ci, co) in enumerate(c.levels()):
             Ho, Wo = (H + 1) // 2, (W + 1) // 2
             M, K = B * Ho * Wo, 9 * ci
-            _L.check(self.L.cpml_nn_im2col(_ptr(a), _ptr(S["col"][l]), B, H, W, ci, st), "cpml_nn_im2col")
+            self._call("cpml_nn_im2col", _ptr(a), _ptr(S["col"][l]), B, H, W, ci, st)
             self._gemm(M, co, K, S["col"][l], K, 0, self.Pb[f"conv{l}_w"], K, 1, Cf=S["y"][l],
                        Cb=S["a"][l], bias=self.P[f"conv{l}_b"], relu=1, work=S["work"])
             a = S["a"][l]
@@ -263,21 +259,23 @@ class Surrogate:
         # receiver r of shot b is offset r - slot_b: row r + (nrec - 1 - slot_b) of the offset traces
         torch.sub(slot[:B], c.nrec - 1, out=S["shift_neg"])
         torch.neg(S["shift_neg"], out=S["shift"])
-        _L.check(self.L.cpml_nn_shift_rows(_ptr(S["poff"]), _ptr(S["shift"]), _ptr(S["p"]), None, B, no, c.nrec,
-                                           c.nt, st), "cpml_nn_shift_rows")
+        self._call("cpml_nn_shift_rows", _ptr(S["poff"]), _ptr(S["shift"]), _ptr(S["p"]), None, B, no, c.nrec,
+                   c.nt, st)
         return S
 
     def backward(self, target, B):
         """target: FP32 [B, nrec*nt]. Writes every gradient into self.g and
         the per-shot squared relative misfits into buffer 'loss'."""
-        c, S, st, L = self.cfg, self._buffers(B), self._stream(), _Checked(self.L)
+        c, S, st = self.cfg, self._buffers(B), self._stream()
         T = c.nrec * c.nt
         R, lat, F, no = c.noff() * c.modes, c.latent, c.flat(), c.noff()
-        L.cpml_nn_rel_l2(_ptr(S["p"]), _ptr(target), _ptr(S["dp"]), _ptr(S["loss"]), B, T, st)
-        L.cpml_nn_head_grad(_ptr(S["head"]), 1, _ptr(S["loss"]), _ptr(S["dhead"]), B, c.head_weight, st)
-        L.cpml_nn_cast(_ptr(S["dhead"]), _ptr(S["dheadb"]), B, st)
+        self._call("cpml_nn_rel_l2", _ptr(S["p"]), _ptr(target), _ptr(S["dp"]), _ptr(S["loss"]), B, T, st)
+        self._call("cpml_nn_head_grad", _ptr(S["head"]), 1, _ptr(S["loss"]), _ptr(S["dhead"]), B, c.head_weight,
+                   st)
+        self._call("cpml_nn_cast", _ptr(S["dhead"]), _ptr(S["dheadb"]), B, st)
         # receiver traces back to the offset axis (offsets without a receiver get 0)
-        L.cpml_nn_shift_rows(_ptr(S["dp"]), _ptr(S["shift_neg"]), None, _ptr(S["dpoffb"]), B, c.nrec, no, c.nt, st)
+        self._call("cpml_nn_shift_rows", _ptr(S["dp"]), _ptr(S["shift_neg"]), None, _ptr(S["dpoffb"]), B, c.nrec,
+                   no, c.nt, st)
         # spectral synthesis and the coefficient layer
         self._gemm(B * no, c.modes, c.nt, S["dpoffb"], c.nt, 0, self.basis_b, c.nt, 1, Cf=S["dz"], Cb=S["dzb"],
                    work=S["work"])
@@ -288,7 +286,7 @@ class Surrogate:
         self._colsum(S["dhead"], self.G["head_b"], B, 1, S)
         # dense 1
         self._gemm(B, lat, R, S["dzb"], R, 0, self.Pb["fc2_w"], lat, 0, Cf=S["dh"], work=S["work"])
-        L.cpml_nn_relu_bwd(_ptr(S["dh"]), _ptr(S["h"]), _ptr(S["dh1b"]), _ptr(S["dh1f"]), B * lat, st)
+        self._call("cpml_nn_relu_bwd", _ptr(S["dh"]), _ptr(S["h"]), _ptr(S["dh1b"]), _ptr(S["dh1f"]), B * lat, st)
         a_last = S["a"][-1]
         self._gemm(lat, F, B, S["dh1b"], lat, 1, a_last, F, 0, Cf=self.G["fc1_w"], work=S["work"])
         self._colsum(S["dh1f"], self.G["fc1_b"], B, lat, S)
@@ -298,22 +296,21 @@ class Surrogate:
             H, W, ci, co = c.levels()[l]
             Ho, Wo = (H + 1) // 2, (W + 1) // 2
             M, K = B * Ho * Wo, 9 * ci
-            L.cpml_nn_relu_bwd(_ptr(S["da"]), _ptr(S["y"][l]), _ptr(S["dyb"]), _ptr(S["dyf"]), M * co, st)
+            self._call("cpml_nn_relu_bwd", _ptr(S["da"]), _ptr(S["y"][l]), _ptr(S["dyb"]), _ptr(S["dyf"]), M * co, st)
             self._gemm(co, K, M, S["dyb"], co, 1, S["col"][l], K, 0, Cf=self.G[f"conv{l}_w"], work=S["work"])
             self._colsum(S["dyf"], self.G[f"conv{l}_b"], M, co, S)
             if l > 0:
                 self._gemm(M, K, co, S["dyb"], co, 0, self.Pb[f"conv{l}_w"], K, 0, Cf=S["dcol"], work=S["work"])
-                L.cpml_nn_col2im(_ptr(S["dcol"]), _ptr(S["da"]), B, H, W, ci, st)
+                self._call("cpml_nn_col2im", _ptr(S["dcol"]), _ptr(S["da"]), B, H, W, ci, st)
 
     def _colsum(self, x, out, M, N, S):
-        _L.check(self.L.cpml_nn_colsum(_ptr(x), _ptr(out), M, N, 0, _ptr(S["work"]), S["work"].numel(),
-                                       self._stream()), "cpml_nn_colsum")
+        self._call("cpml_nn_colsum", _ptr(x), _ptr(out), M, N, 0, _ptr(S["work"]), S["work"].numel(),
+                   self._stream(), kernels=2)
 
     def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
         self.step_count += 1
-        _L.check(self.L.cpml_nn_adam(_ptr(self.w), _ptr(self.wb), _ptr(self.g), _ptr(self.m), _ptr(self.v),
-                                     self.n, lr, b1, b2, eps, self.step_count, wd, self._stream()),
-                 "cpml_nn_adam")
+        self._call("cpml_nn_adam", _ptr(self.w), _ptr(self.wb), _ptr(self.g), _ptr(self.m), _ptr(self.v),
+                   self.n, lr, b1, b2, eps, self.step_count, wd, self._stream())
 
     # ---- training and inference ---------------------------------------------
     def train(self, X, slot, T, epochs=1, batch=64, lr=1e-3, lr_min=1e-5, seed=0, time_budget_s=None, log=None):
@@ -368,8 +365,7 @@ class Surrogate:
         """Squared relative L2 misfit per shot, on the device (cpml_nn_rel_l2)."""
         n = P.shape[0]
         loss = torch.empty(n, dtype=torch.float32, device=self.dev)
-        _L.check(self.L.cpml_nn_rel_l2(_ptr(P), _ptr(T), None, _ptr(loss), n, P.shape[1], self._stream()),
-                 "cpml_nn_rel_l2")
+        self._call("cpml_nn_rel_l2", _ptr(P), _ptr(T), None, _ptr(loss), n, P.shape[1], self._stream())
         return loss
 
 

@@ -33,10 +33,11 @@ def stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+@pytest.mark.parametrize("fn", ["cpml_nn_gemm", "cpml_nn_gemm_tc"])
 @pytest.mark.parametrize("ta,tb", [(0, 0), (0, 1), (1, 0), (1, 1)])
 @pytest.mark.parametrize("M,N,K,splits", [(1, 1, 1, 1), (70, 33, 50, 1), (128, 192, 640, 1), (37, 65, 3000, 7),
-                                          (200, 18, 4096, 64)])
-def test_gemm_matches_fp64_reference(L, ta, tb, M, N, K, splits):
+                                          (200, 18, 4096, 64), (300, 136, 96, 1)])
+def test_gemm_matches_fp64_reference(L, fn, ta, tb, M, N, K, splits):
     g = torch.Generator(device="cpu").manual_seed(M * 7 + N * 3 + K)
     A = torch.randn(M, K, generator=g).to(torch.bfloat16)
     B = torch.randn(K, N, generator=g).to(torch.bfloat16)
@@ -52,9 +53,11 @@ def test_gemm_matches_fp64_reference(L, ta, tb, M, N, K, splits):
         Cb = torch.zeros(M, N, dtype=torch.bfloat16, device="cuda")
         work = torch.empty(splits * M * N + 1, device="cuda")
         b = bias.cuda() if use_bias else None
-        assert L.cpml_nn_gemm(M, N, K, vp(dA), lda, ta, vp(dB), ldb, tb, vp(Cf), vp(Cb), N, vp(b), relu, accum,
+        assert getattr(L, fn)(M, N, K, vp(dA), lda, ta, vp(dB), ldb, tb, vp(Cf), vp(Cb), N, vp(b), relu, accum,
                               alpha, splits, vp(work), work.numel(), stream()) == 0
         torch.cuda.synchronize()
+        err = ctypes.c_int(-1)
+        assert L.cpml_nn_error(ctypes.byref(err)) == 0 and err.value == 0
         exp = alpha * ref
         if use_bias:
             exp = exp + bias.double()
@@ -168,11 +171,12 @@ def test_adam_matches_formula(L):
 SMALL = dict(h=32, w=48, cin=3, chans=(8, 16, 16, 32, 32), latent=48, nrec=8, nt=120, modes=24, head_weight=0.2)
 
 
-def test_network_gradients_match_fp64_oracle(L):
+@pytest.mark.parametrize("gemm", ["mma", "tcgen05"])
+def test_network_gradients_match_fp64_oracle(L, gemm):
     from oracle import surrogate_np as S
     from seismic_cpml_gb300.surrogate import NetConfig, Surrogate, dct_basis
     cfg = NetConfig(**SMALL)
-    net = Surrogate(cfg, seed=3)
+    net = Surrogate(cfg, seed=3, gemm=gemm)
     # generic weights (the product's near-zero output-layer init would make
     # the trunk gradients tiny), rounded to BF16 so the oracle sees the same
     # values the tensor cores multiply
