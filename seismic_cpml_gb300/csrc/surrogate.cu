@@ -159,36 +159,56 @@ __global__ void gemm_reduce_kernel(int M, int N, int splits, const float* __rest
 }
 
 // 3x3, stride 2, pad 1 patches. in: NHWC [B][H][W][C]; out row m = (b, y, x)
-// of the Ho x Wo output grid, column k = (ky*3 + kx)*C + c.
+// of the Ho x Wo output grid, column k = (ky*3 + kx)*C + c. One thread per
+// (row m, tap, group of V channels): V = 8 moves 16 bytes per load and store
+// (C a multiple of 8), V = 1 otherwise.
+template <int V>
 __global__ void im2col_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int B,
                               int H, int W, int C, int Ho, int Wo) {
-  const long long K = 9LL * C;
-  const long long total = (long long)B * Ho * Wo * K;
+  const int CG = C / V;                                   // channel groups per tap
+  const long long total = (long long)B * Ho * Wo * 9 * CG;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const long long m = e / K;
-    const int k = (int)(e % K);
-    const int c = k % C, kk = k / C, ky = kk / 3, kx = kk % 3;
-    const int x = (int)(m % Wo), y = (int)((m / Wo) % Ho), b = (int)(m / ((long long)Wo * Ho));
-    const int iy = 2 * y + ky - 1, ix = 2 * x + kx - 1;
-    __nv_bfloat16 v = __float2bfloat16(0.f);
-    if (iy >= 0 && iy < H && ix >= 0 && ix < W) v = in[(((long long)b * H + iy) * W + ix) * C + c];
-    out[e] = v;
+    const int cg = (int)(e % CG);
+    const long long mt = e / CG;                          // (row, tap)
+    const int tap = (int)(mt % 9);
+    const long long m = mt / 9;
+    const int x = (int)(m % Wo);
+    const long long by = m / Wo;
+    const int y = (int)(by % Ho), b = (int)(by / Ho);
+    const int iy = 2 * y + tap / 3 - 1, ix = 2 * x + tap % 3 - 1;
+    const bool inside = iy >= 0 && iy < H && ix >= 0 && ix < W;
+    const long long src = (((long long)b * H + iy) * W + ix) * C + (long long)cg * V;
+    const long long dst = m * 9 * C + (long long)tap * C + (long long)cg * V;
+    if (V == 8) {
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (inside) v = *reinterpret_cast<const uint4*>(in + src);
+      *reinterpret_cast<uint4*>(out + dst) = v;
+    } else {
+      out[dst] = inside ? in[src] : __float2bfloat16(0.f);
+    }
   }
 }
 
 // Adjoint of im2col as a gather: each input element sums, in a fixed order,
-// the (at most 2 x 2) patch entries that read it.
+// the (at most 2 x 2) patch entries that read it. One thread per (pixel,
+// group of V channels); V = 4 moves 16 bytes per access (C a multiple of 4).
+template <int V>
 __global__ void col2im_kernel(const float* __restrict__ col, float* __restrict__ out, int B, int H, int W, int C,
                               int Ho, int Wo) {
-  const long long total = (long long)B * H * W * C;
+  const int CG = C / V;
+  const long long total = (long long)B * H * W * CG;
   const long long K = 9LL * C;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(e % C);
-    const int ix = (int)((e / C) % W), iy = (int)((e / ((long long)C * W)) % H);
-    const int b = (int)(e / ((long long)C * W * H));
-    float s = 0.f;
+    const int cg = (int)(e % CG);
+    const long long pix = e / CG;
+    const int ix = (int)(pix % W);
+    const long long bi = pix / W;
+    const int iy = (int)(bi % H), b = (int)(bi / H);
+    float s[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) s[q] = 0.f;
     for (int ky = 0; ky < 3; ++ky) {
       const int ty = iy + 1 - ky;
       if (ty < 0 || (ty & 1) || (ty >> 1) >= Ho) continue;
@@ -198,10 +218,22 @@ __global__ void col2im_kernel(const float* __restrict__ col, float* __restrict__
         if (tx < 0 || (tx & 1) || (tx >> 1) >= Wo) continue;
         const int x = tx >> 1;
         const long long m = ((long long)b * Ho + y) * Wo + x;
-        s += col[m * K + (ky * 3 + kx) * C + c];
+        const float* p = col + m * K + (ky * 3 + kx) * C + cg * V;
+        if (V == 4) {
+          const float4 v = *reinterpret_cast<const float4*>(p);
+          s[0] += v.x; s[1] += v.y; s[2 % V] += v.z; s[3 % V] += v.w;
+        } else {
+#pragma unroll
+          for (int q = 0; q < V; ++q) s[q] += p[q];
+        }
       }
     }
-    out[e] = s;
+    float* o = out + pix * C + cg * V;
+    if (V == 4)
+      *reinterpret_cast<float4*>(o) = make_float4(s[0], s[1 % V], s[2 % V], s[3 % V]);
+    else
+#pragma unroll
+      for (int q = 0; q < V; ++q) o[q] = s[q];
   }
 }
 
@@ -325,18 +357,24 @@ __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ w
 // ---------------------------------------------------------------------------
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, NT = 128, STAGES = 2;
-constexpr int TILE_BYTES = BM * BK * 2;                    // 16 KB per operand tile (BM == BN)
-constexpr int STAGE_BYTES = 2 * TILE_BYTES;
-constexpr int SMEM = STAGES * STAGE_BYTES + 64;
+constexpr int BM = 128, BK = 64, NT = 128, STAGES = 3;
+constexpr int A_BYTES = BM * BK * 2;                       // 16 KB A tile
 constexpr uint32_t LBO = 128, SBO = 1024;                  // k- and m/n-direction core-matrix strides
 constexpr long long kWait = 2000000000LL;                  // ~1 s at 2 GHz
 
-// Instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
-// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit
-// 17, M >> 4 at bit 24.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// Output tile width BN (32, 64 or 128: the narrowest that holds N, so thin
+// layers do not multiply zeros); BN fp32 TMEM columns hold the accumulator.
+template <int BN>
+struct Cfg {
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 64;
+  // Instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
+  // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at
+  // bit 17, M >> 4 at bit 24.
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                    ((uint32_t)(BM >> 4) << 24);
+};
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -352,16 +390,17 @@ __device__ __forceinline__ int core_off(int r, int k) {
   return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
-// Stage rows [r0, r0 + 128) x k-values [k0, k0 + 64) of a bf16 operand into
-// `tile`; trans == 0: element (r, k) at src[r * ld + k], else at src[k * ld + r].
-// Out-of-range elements are zero.
+// Stage rows [r0, r0 + ROWS) x k-values [k0, k0 + 64) of a bf16 operand
+// into `tile`; trans == 0: element (r, k) at src[r * ld + k], else at
+// src[k * ld + r]. Out-of-range elements are zero.
+template <int ROWS>
 __device__ __forceinline__ void stage(unsigned char* tile, const __nv_bfloat16* __restrict__ src, int ld, int trans,
                                       int r0, int R, int k0, int ke) {
   const int tid = threadIdx.x;
   if (!trans) {
     const bool vec = (ld & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
-    // 128 rows x 8 groups of 8 k-values; consecutive threads take consecutive groups
-    for (int e = tid; e < BM * (BK / 8); e += NT) {
+    // ROWS rows x 8 groups of 8 k-values; consecutive threads take consecutive groups
+    for (int e = tid; e < ROWS * (BK / 8); e += NT) {
       const int r = e >> 3, g = e & 7;
       const int gr = r0 + r, gk = k0 + g * 8;
       uint4 v = make_uint4(0, 0, 0, 0);
@@ -380,12 +419,34 @@ __device__ __forceinline__ void stage(unsigned char* tile, const __nv_bfloat16* 
     }
   } else {
     // consecutive threads take consecutive rows (contiguous in memory)
-    for (int e = tid; e < BM * BK; e += NT) {
-      const int r = e & (BM - 1), k = e >> 7;
+    for (int e = tid; e < ROWS * BK; e += NT) {
+      const int r = e % ROWS, k = e / ROWS;
       const int gr = r0 + r, gk = k0 + k;
       const __nv_bfloat16 v = (gr < R && gk < ke) ? src[(size_t)gk * ld + gr] : __float2bfloat16(0.f);
       *reinterpret_cast<__nv_bfloat16*>(tile + core_off(r, k)) = v;
     }
+  }
+}
+
+// Asynchronous form of stage() for a k-contiguous operand whose rows start
+// on 16-byte boundaries (ld a multiple of 8, src 16-byte aligned): every
+// 8-value group is one 16-byte cp.async straight into its core-matrix row,
+// zero-filled past the end of the row or of the matrix.
+template <int ROWS>
+__device__ __forceinline__ void stage_async(unsigned char* tile, const __nv_bfloat16* __restrict__ src, int ld,
+                                            int r0, int R, int k0, int ke) {
+  for (int e = threadIdx.x; e < ROWS * (BK / 8); e += NT) {
+    const int r = e >> 3, g = e & 7;
+    const int gr = r0 + r, gk = k0 + g * 8;
+    int bytes = 0;
+    const __nv_bfloat16* p = src;  // a valid address even when nothing is read
+    if (gr < R && gk < ke) {
+      bytes = (ke - gk >= 8 ? 8 : ke - gk) * 2;
+      p = src + (size_t)gr * ld + gk;
+    }
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(tile + core_off(r, g * 8))),
+                 "l"(p), "r"(bytes)
+                 : "memory");
   }
 }
 
@@ -409,11 +470,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 __device__ int g_nn_err;  // set when a bounded tensor-core wait gives up
 
+template <int BN>
 __global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, int kchunk,
                                                         const __nv_bfloat16* __restrict__ A, int lda, int ta,
                                                         const __nv_bfloat16* __restrict__ B, int ldb, int tb,
                                                         Epilogue ep, float* __restrict__ work) {
   using namespace tc;
+  using C = Cfg<BN>;
+  constexpr int STAGE_BYTES = C::STAGE_BYTES;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + STAGES * STAGE_BYTES + 32);
@@ -422,9 +486,9 @@ __global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, in
   const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
   const int nk = ke > kb ? (ke - kb + BK - 1) / BK : 0;
 
-  if (warp == 0) {  // 128 fp32 accumulator columns for the 128 x 128 tile
+  if (warp == 0) {  // BN fp32 accumulator columns for the 128 x BN tile
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
-                 "r"(128)
+                 "r"(BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -438,18 +502,30 @@ __global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, in
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
 
+  // k-contiguous, 16-byte-aligned operands are staged with cp.async (several
+  // stages in flight); the others with plain loads and stores
+  const bool avec = !ta && (lda & 7) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+  const bool bvec = tb && (ldb & 7) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+  auto load_stage = [&](int kt) {
+    unsigned char* sa = smem + (kt % STAGES) * STAGE_BYTES;
+    unsigned char* sb = sa + A_BYTES;
+    const int k0 = kb + kt * BK;
+    if (avec) stage_async<BM>(sa, A, lda, m0, M, k0, ke); else stage<BM>(sa, A, lda, ta, m0, M, k0, ke);
+    if (bvec) stage_async<BN>(sb, B, ldb, n0, N, k0, ke); else stage<BN>(sb, B, ldb, tb ? 0 : 1, n0, N, k0, ke);
+  };
+  // prologue: k-tiles 0 .. STAGES-2, one cp.async group each (empty if absent)
+  for (int q = 0; q < STAGES - 1; ++q) {
+    if (q < nk) load_stage(q);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   bool ok = true;
   for (int kt = 0; kt < nk && ok; ++kt) {
-    const int s = kt & 1;
+    const int s = kt % STAGES;
     unsigned char* sa = smem + s * STAGE_BYTES;
-    unsigned char* sb = sa + TILE_BYTES;
-    // the MMAs that last read this stage (k-tile kt - 2) must have finished
-    if (kt >= STAGES) ok = mbar_wait(&bar[s], (uint32_t)(((kt - STAGES) >> 1) & 1));
-    if (!__syncthreads_and(ok ? 1 : 0)) { ok = false; break; }
-    const int k0 = kb + kt * BK;
-    stage(sa, A, lda, ta, m0, M, k0, ke);
-    stage(sb, B, ldb, tb ? 0 : 1, n0, N, k0, ke);
-    // make the generic-proxy stores visible to the tensor core (async proxy)
+    unsigned char* sb = sa + A_BYTES;
+    // this thread's copies of k-tile kt have landed (later groups may not)
+    asm volatile("cp.async.wait_group %0;" ::"n"(STAGES - 2) : "memory");
+    // make the stores of this stage visible to the tensor core (async proxy)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -463,22 +539,39 @@ __global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, in
             "{\n\t.reg .pred p;\n\t"
             "setp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-            "l"(da), "l"(db), "r"(IDESC), "r"(acc)
+            "l"(da), "l"(db), "r"(C::IDESC), "r"(acc)
             : "memory");
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                        smem_addr(&bar[s]))
                    : "memory");
     }
+    // refill the stage that k-tile kt - 1 used with k-tile kt + STAGES - 1,
+    // once its MMAs have finished (the j-th commit to a stage's barrier
+    // completes its phase j)
+    const int kn = kt + STAGES - 1;
+    if (kn < nk) {
+      if (kt >= 1) ok = mbar_wait(&bar[(kt - 1) % STAGES], (uint32_t)(((kt - 1) / STAGES) & 1));
+      if (!__syncthreads_and(ok ? 1 : 0)) { ok = false; break; }
+      load_stage(kn);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   // all MMAs done: the last commit covers every earlier one of this thread
-  if (ok && nk > 0) ok = mbar_wait(&bar[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1));
+  if (ok && nk > 0) ok = mbar_wait(&bar[(nk - 1) % STAGES], (uint32_t)(((nk - 1) / STAGES) & 1));
   ok = __syncthreads_and(ok ? 1 : 0) != 0;   // uniform: tcgen05.ld below is warp-collective
   if (!ok && tid == 0) atomicOr(&g_nn_err, 1);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-  // epilogue: warp w owns rows 32w..32w+31, one row per thread
-  const int row = m0 + warp * 32 + lane;
+  // epilogue: warp w reads TMEM lanes 32w..32w+31 (tile rows, one per
+  // thread) into a padded fp32 tile in the now idle stage buffers, then the
+  // CTA writes the tile out row by row, consecutive threads on consecutive
+  // columns (coalesced)
+  float* cs = reinterpret_cast<float*>(smem);   // [BM][BN + 1]
+  constexpr int CP = BN + 1;
+  static_assert(BM * CP * 4 <= STAGES * STAGE_BYTES, "epilogue tile fits in the stage buffers");
+  const int rloc = warp * 32 + lane;
 #pragma unroll 1
   for (int c = 0; c < BN; c += 16) {
     uint32_t r[16];
@@ -496,23 +589,24 @@ __global__ void __launch_bounds__(tc::NT) gemm_tc_kernel(int M, int N, int K, in
 #pragma unroll
       for (int q = 0; q < 16; ++q) r[q] = 0u;  // empty K range (or a failed wait): zero
     }
-    if (row < M) {
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int col = n0 + c + q;
-        if (col >= N) break;
-        const float v = __uint_as_float(r[q]);
-        if (work)
-          work[((size_t)blockIdx.z * M + row) * N + col] = v;
-        else
-          epilogue_store(ep, row, col, v);
-      }
-    }
+    for (int q = 0; q < 16; ++q) cs[rloc * CP + c + q] = __uint_as_float(r[q]);
+  }
+  __syncthreads();
+  for (int e = tid; e < BM * BN; e += NT) {
+    const int rr = e / BN, cc = e % BN;
+    const int row = m0 + rr, col = n0 + cc;
+    if (row >= M || col >= N) continue;
+    const float v = cs[rr * CP + cc];
+    if (work)
+      work[((size_t)blockIdx.z * M + row) * N + col] = v;
+    else
+      epilogue_store(ep, row, col, v);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
 }
 
 int grid_for(long long n) {
@@ -554,10 +648,16 @@ int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const v
   if (M < 0 || N < 0 || K < 0 || !A || !B || (!Cf && !Cb) || splits < 1) return CPML_ERR_INVALID;
   if (accum && !Cf) return CPML_ERR_INVALID;
   if (M == 0 || N == 0) return CPML_OK;
-  if ((N + tc::BN - 1) / tc::BN > 65535) return CPML_ERR_RANGE;
+  const int bn = N <= 32 ? 32 : (N <= 64 ? 64 : 128);
+  if ((N + bn - 1) / bn > 65535) return CPML_ERR_RANGE;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM) != cudaSuccess)
+    if (cudaFuncSetAttribute(gemm_tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::Cfg<32>::SMEM) != cudaSuccess ||
+        cudaFuncSetAttribute(gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::Cfg<64>::SMEM) != cudaSuccess ||
+        cudaFuncSetAttribute(gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::Cfg<128>::SMEM) != cudaSuccess)
       return CPML_ERR_CUDA;
     attr = true;
   }
@@ -568,10 +668,16 @@ int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const v
   if (splits > 65535) return CPML_ERR_RANGE;
   if (splits > 1 && (!work || work_elems < (long long)splits * M * N)) return CPML_ERR_INVALID;
   const Epilogue ep{Cf, (__nv_bfloat16*)Cb, ldc, bias, relu, accum, alpha};
-  const dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN, splits);
+  const dim3 grid((M + tc::BM - 1) / tc::BM, (N + bn - 1) / bn, splits);
   cudaStream_t st = (cudaStream_t)stream;
-  gemm_tc_kernel<<<grid, tc::NT, tc::SMEM, st>>>(M, N, K, kchunk, (const __nv_bfloat16*)A, lda, ta,
-                                                  (const __nv_bfloat16*)B, ldb, tb, ep, splits > 1 ? work : nullptr);
+  const __nv_bfloat16 *a = (const __nv_bfloat16*)A, *b = (const __nv_bfloat16*)B;
+  float* w = splits > 1 ? work : nullptr;
+  if (bn == 32)
+    gemm_tc_kernel<32><<<grid, tc::NT, tc::Cfg<32>::SMEM, st>>>(M, N, K, kchunk, a, lda, ta, b, ldb, tb, ep, w);
+  else if (bn == 64)
+    gemm_tc_kernel<64><<<grid, tc::NT, tc::Cfg<64>::SMEM, st>>>(M, N, K, kchunk, a, lda, ta, b, ldb, tb, ep, w);
+  else
+    gemm_tc_kernel<128><<<grid, tc::NT, tc::Cfg<128>::SMEM, st>>>(M, N, K, kchunk, a, lda, ta, b, ldb, tb, ep, w);
   if (splits > 1) gemm_reduce_kernel<<<grid_for((long long)M * N), 256, 0, st>>>(M, N, splits, work, ep);
   return status();
 }
@@ -587,17 +693,28 @@ int cpml_nn_error(int* err) {
 int cpml_nn_im2col(const void* in, void* out, int B, int H, int W, int C, void* stream) {
   if (!in || !out || B < 1 || H < 2 || W < 2 || C < 1) return CPML_ERR_INVALID;
   const int Ho = (H + 1) / 2, Wo = (W + 1) / 2;
-  const long long n = (long long)B * Ho * Wo * 9 * C;
-  im2col_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, (__nv_bfloat16*)out, B, H,
-                                                                 W, C, Ho, Wo);
+  const bool vec = C % 8 == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+  const long long n = (long long)B * Ho * Wo * 9 * (vec ? C / 8 : C);
+  if (vec)
+    im2col_kernel<8><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, (__nv_bfloat16*)out, B,
+                                                                      H, W, C, Ho, Wo);
+  else
+    im2col_kernel<1><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, (__nv_bfloat16*)out, B,
+                                                                      H, W, C, Ho, Wo);
   return status();
 }
 
 int cpml_nn_col2im(const float* col, float* out, int B, int H, int W, int C, void* stream) {
   if (!col || !out || B < 1 || H < 2 || W < 2 || C < 1) return CPML_ERR_INVALID;
   const int Ho = (H + 1) / 2, Wo = (W + 1) / 2;
-  const long long n = (long long)B * H * W * C;
-  col2im_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(col, out, B, H, W, C, Ho, Wo);
+  const bool vec = C % 4 == 0 && (reinterpret_cast<uintptr_t>(col) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+  const long long n = (long long)B * H * W * (vec ? C / 4 : C);
+  if (vec)
+    col2im_kernel<4><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(col, out, B, H, W, C, Ho, Wo);
+  else
+    col2im_kernel<1><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(col, out, B, H, W, C, Ho, Wo);
   return status();
 }
 

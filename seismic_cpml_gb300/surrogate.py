@@ -9,11 +9,13 @@ the reference, which has no learned component.
 
 The network works in the source's frame, so that what it learns does not
 depend on where the source is:
-  input [B, 128, 256, 3]: the 2 x 2 mean of the 256 x 256 interior cp map,
+  input [B, 128, 256, 8]: the 2 x 2 mean of the 256 x 256 interior cp map,
         (cp - 3000) / 1000, written into a window twice as wide whose centre
         column is the source column; a channel that is 1 inside the model;
-        a channel marking the receivers (top row)
-  5 x { 3x3 stride-2 conv + bias + ReLU }: 3 -> 32 -> 64 -> 128 -> 256 -> 256
+        a channel marking the receivers (top row); five zero channels, so
+        that every pixel is 16 bytes and the first layer's patches and
+        weights take the 16-byte vector paths
+  5 x { 3x3 stride-2 conv + bias + ReLU }: 8 -> 32 -> 64 -> 128 -> 256 -> 256
   dense 4 * 8 * 256 -> latent (ReLU); dense latent -> (2 nrec - 1) x modes
         coefficients, one trace per receiver offset -(nrec-1) .. nrec-1
   spectral synthesis: coefficients x truncated cosine (DCT-II) basis
@@ -42,13 +44,14 @@ from .earth import gardner, lame_from_velocity
 from .params import STF_RICKER, default_2d
 
 SM_COUNT = 152
+IN_CHANNELS = 8   # cp, model mask, receivers + 5 zero channels
 
 
 @dataclass(frozen=True)
 class NetConfig:
     h: int = 128
     w: int = 256
-    cin: int = 3
+    cin: int = 8
     chans: tuple = (32, 64, 128, 256, 256)
     latent: int = 256
     nrec: int = 64
@@ -101,7 +104,7 @@ def _ptr(t):
 class Surrogate:
     """Weights, Adam state and per-batch-size work buffers on one GPU."""
 
-    def __init__(self, cfg: NetConfig = NetConfig(), seed: int = 0, device: str = "cuda", gemm: str = "mma"):
+    def __init__(self, cfg: NetConfig = NetConfig(), seed: int = 0, device: str = "cuda", gemm: str = "tcgen05"):
         if not torch.cuda.is_available():
             raise RuntimeError("the surrogate needs a CUDA device")
         if gemm not in ("mma", "tcgen05"):
@@ -132,6 +135,7 @@ class Surrogate:
         self.init_weights(seed)
         self.basis = torch.tensor(dct_basis(cfg.modes, cfg.nt), dtype=torch.float32, device=self.dev)
         self.basis_b = self.basis.to(torch.bfloat16)
+        self.basis_tb = self.basis_b.t().contiguous()   # [nt, modes]: k-contiguous B operand of the synthesis
         self.step_count = 0
         self._bufs = {}
 
@@ -254,7 +258,7 @@ class Surrogate:
                    work=S["work"])
         self._gemm(B, 1, lat, S["hb"], lat, 0, self.Pb["head_w"], lat, 1, Cf=S["head"], bias=self.P["head_b"],
                    work=S["work"])
-        self._gemm(B * no, c.nt, c.modes, S["zb"], c.modes, 0, self.basis_b, c.nt, 0, Cf=S["poff"],
+        self._gemm(B * no, c.nt, c.modes, S["zb"], c.modes, 0, self.basis_tb, c.modes, 1, Cf=S["poff"],
                    work=S["work"])
         # receiver r of shot b is offset r - slot_b: row r + (nrec - 1 - slot_b) of the offset traces
         torch.sub(slot[:B], c.nrec - 1, out=S["shift_neg"])
@@ -448,13 +452,13 @@ def source_slot(spec: ShotSpec, col):
 
 
 def encode_input(spec: ShotSpec, cp_inner, col):
-    """[hw, 2 hw, 3] float32 network input in the source's frame: the
+    """[hw, 2 hw, 8] float32 network input in the source's frame: the
     downsampled normalised cp map placed so that the source column lands on
-    column hw, a mask of the model window, and the receiver positions on the
-    receivers' row."""
+    column hw, a mask of the model window, the receiver positions on the
+    receivers' row, and five zero channels (16-byte pixels)."""
     f = spec.interior // spec.hw
     small = cp_inner.reshape(spec.hw, f, spec.hw, f).mean(axis=(1, 3))
-    x = np.zeros((spec.hw, 2 * spec.hw, 3), np.float32)
+    x = np.zeros((spec.hw, 2 * spec.hw, IN_CHANNELS), np.float32)
     o = spec.hw - col // f
     x[:, o:o + spec.hw, 0] = (small - 3000.0) / 1000.0
     x[:, o:o + spec.hw, 1] = 1.0
@@ -465,9 +469,9 @@ def encode_input(spec: ShotSpec, cp_inner, col):
 
 
 def make_inputs(spec: ShotSpec, seed: int, indices):
-    """Network inputs [n, hw, 2 hw, 3] float32 and source slots [n] int32 for
+    """Network inputs [n, hw, 2 hw, 8] float32 and source slots [n] int32 for
     shots (seed, index)."""
-    out = np.zeros((len(indices), spec.hw, 2 * spec.hw, 3), np.float32)
+    out = np.zeros((len(indices), spec.hw, 2 * spec.hw, IN_CHANNELS), np.float32)
     slots = np.zeros(len(indices), np.int32)
     for q, i in enumerate(indices):
         _, _, _, inner, col = make_shot(spec, seed, i)
@@ -478,12 +482,12 @@ def make_inputs(spec: ShotSpec, seed: int, indices):
 
 def fd_seismograms(spec: ShotSpec, seed: int, indices, chunk=1024, timing=None, threads=8):
     """Run shots (seed, index) through the batched FD engine and return
-    (inputs [n, hw, 2 hw, 3], source slots [n], vertical-velocity traces
+    (inputs [n, hw, 2 hw, 8], source slots [n], vertical-velocity traces
     [n, nrec, nstep/decimate]) as numpy arrays. Host threads build the next
     chunk's models while the engine runs the current one. `timing`, if a
     list, receives the engine's device milliseconds per chunk."""
     indices = list(indices)
-    X = np.zeros((len(indices), spec.hw, 2 * spec.hw, 3), np.float32)
+    X = np.zeros((len(indices), spec.hw, 2 * spec.hw, IN_CHANNELS), np.float32)
     slots = np.zeros(len(indices), np.int32)
     nt = spec.nstep // spec.decimate
     Y = np.zeros((len(indices), spec.nrec, nt), np.float32)

@@ -84,7 +84,7 @@ def test_default_network_size():
     assert cfg.flat() == 4 * 8 * 256
     assert [lv[:2] for lv in cfg.levels()] == [(128, 256), (64, 128), (32, 64), (16, 32), (8, 16)]
     assert cfg.noff() == 127
-    assert 3.0e6 < cfg.n_params() < 6.0e6
+    assert 3.0e6 < cfg.n_params() < 6.0e6 and cfg.cin == 8
 
 
 def test_shot_generator_is_seeded_and_stable():
@@ -100,7 +100,7 @@ def test_shot_generator_is_seeded_and_stable():
     assert len(a[2]) == 64 and all(21 <= r[0] <= 276 for r in a[2])
     assert 21 <= p.isource <= 276
     x = encode_input(spec, a[3], a[4])
-    assert x.shape == (128, 256, 3)
+    assert x.shape == (128, 256, 8) and not x[..., 3:].any()
     o = 128 - a[4] // 2                       # model window starts here; source column lands on 128
     assert x[..., 1].sum() == 128 * 128 and np.all(x[:, o:o + 128, 1] == 1.0)
     small = a[3].reshape(128, 2, 128, 2).mean(axis=(1, 3))
