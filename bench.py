@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["3d_plain", "3d_large", "surrogate"], default="3d_plain")
+    ap.add_argument("--workload", choices=["3d_plain", "3d_large", "2d_plain", "batch2d", "surrogate"],
+                    default="3d_plain")
     ap.add_argument("--train-shots", type=int, default=20000)
     ap.add_argument("--test-shots", type=int, default=2000)
     ap.add_argument("--train-seconds", type=float, default=600.0)
@@ -277,6 +278,7 @@ def run_ours(args, world, rank, local, pg):
     dev_ms = max_over_ranks(pg, dev_ms)
     bytes_step = s.algorithmic_bytes_per_step()
     kern = s.tuning()
+    k_step, k_chunk = s.launches_per_step()
     vx, vy, vz = s.seismograms()
     s.close()
 
@@ -352,11 +354,174 @@ def run_ours(args, world, rank, local, pg):
                      "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 5)},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        # two step kernels per time step (interior + general, or stress + velocity),
-        # plus the chunk reduction and step-counter kernels of every chunk
-        "gpu_launches": args.steps * (2 * p.nstep + 2 * chunks),
+        # the step kernels of every time step (interior + one per general class, or
+        # stress + velocity), plus the chunk reduction and step-counter kernels
+        "gpu_launches": args.steps * (k_step * p.nstep + k_chunk * chunks),
         "clocks": clk,
         "wall_s": round(wall, 3),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_2d_plain(args, world, rank, local, pg):
+    """The 2D plain workload (101 x 641, 10-point C-PML on all edges but the
+    top, homogeneous, 2000 steps, Ricker at the centre, 45 degrees, two
+    receivers): one bench step = one whole run. Its 3.8 MB working set lives
+    in L2, so the step is launch- and latency-bound: the line reports
+    Mcell-updates/s and ms per run; the roofline fraction is quoted against
+    HBM only for comparison."""
+    import torch
+    from seismic_cpml_gb300 import params as P
+    from seismic_cpml_gb300.solver import Solver
+    torch.cuda.set_device(local)
+    p, rec = P.config_2d_plain()
+    ncell = p.nx * p.ny
+    s = Solver(p, rec)
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    for _ in range(args.warmup):
+        s.reset(); s.run()
+    torch.cuda.synchronize()
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.reset(); s.run()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev_ms = max_over_ranks(pg, ev0.elapsed_time(ev1))
+    bytes_step = s.algorithmic_bytes_per_step()
+    s.close()
+    value = world * ncell * p.nstep * args.steps / (dev_ms / 1e3) / 1e6
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        with Solver(p, rec) as e:
+            e.run()
+            e.seismograms()
+            e.energy()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle_c
+        cores = os.cpu_count() or 1
+        res = {}
+        for nth in (cores, 1):
+            sess = oracle_c.Session(p, nthreads=nth)
+            sess.run(1)
+            t0 = time.perf_counter()
+            sess.run(p.nstep - 1)
+            res[nth] = ncell * (p.nstep - 1) / (time.perf_counter() - t0) / 1e6
+            sess.close()
+        cpu = {"value": round(res[cores], 3), "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
+               "sample": "the whole 2000-step run, FP64 C++ restatement, OpenMP",
+               "value_1core": round(res[1], 3)}
+    step_ms = dev_ms / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = bytes_step * p.nstep / (step_ms / 1e3) / 1e9
+    line = {
+        "metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "2d_plain_101x641", "grid": [p.nx, p.ny], "nstep": p.nstep, "receivers": len(rec),
+                   "l2": "working set (3.8 MB) is L2-resident by design of the workload"},
+        "latency_us_per_time_step": round(step_ms * 1e3 / p.nstep, 3),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "note": "L2-resident and launch-bound; the fraction is not a kernel-quality figure"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(world * ncell * p.nstep * args.steps / e2e_s / 1e6, 3), "unit": "Mcell-updates/s",
+                "h2d_bytes_per_step": 2 * 4 * p.nstep + 4 * len(rec),
+                "d2h_bytes_per_step": 2 * 4 * len(rec) * p.nstep + 2 * 8 * p.nstep},
+        "gpu_launches": args.steps * (2 * p.nstep + 2 * n_chunks(p.nstep, p.it_display)),
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch2d(args, world, rank, local, pg):
+    """Batched 2D multi-shot FD: 256 seeded shots of 240-1240 cells per side
+    (20-point C-PML), layered models, DELTAT from a Courant number of 0.5 and
+    NSTEP covering 2 s, in one persistent launch. One bench step = the whole
+    batch. `sequential` is the same shots run one after another through
+    single-shot handles (measured once, outside the timed region)."""
+    import torch
+    from seismic_cpml_gb300.batch import Batch
+    from seismic_cpml_gb300.solver import Solver
+    from seismic_cpml_gb300.workloads import batch2d_shots
+    torch.cuda.set_device(local)
+    shots = batch2d_shots()
+    cells = sum(sh[0].nx * sh[0].ny * sh[0].nstep for sh in shots)
+    b = Batch([sh[0] for sh in shots], models=[sh[1] for sh in shots], receivers=[sh[2] for sh in shots])
+    for _ in range(args.warmup):
+        b.run()
+    torch.cuda.synchronize()
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = []
+    for _ in range(args.steps):
+        b.run()
+        ms.append(b.last_run_ms())
+    clk = clocks.stop()
+    dev_ms = max_over_ranks(pg, sum(ms))
+    b.close()
+    value = world * cells * args.steps / (dev_ms / 1e3) / 1e6
+    seq_ms = 0.0
+    for sh in shots:
+        with Solver(sh[0], sh[2], model=sh[1]) as s1:
+            s1.run()
+            seq_ms += s1.last_run_ms()
+    seq = cells / (seq_ms / 1e3) / 1e6
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        with Batch([sh[0] for sh in shots], models=[sh[1] for sh in shots],
+                   receivers=[sh[2] for sh in shots]) as e:
+            e.run()
+            for q in range(len(shots)):
+                e.seismograms(q)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle_c
+        cores = os.cpu_count() or 1
+        p, m = shots[0][0], shots[0][1]
+        sess = oracle_c.Session(p, nthreads=cores, lam=m[0], mu=m[1], rho=m[2])
+        sess.run(1)
+        t0 = time.perf_counter()
+        sess.run(200)
+        dt = time.perf_counter() - t0
+        sess.close()
+        cpu = {"value": round(p.nx * p.ny * 200 / dt / 1e6, 3), "unit": "Mcell-updates/s", "cores": cores,
+               "kind": "port", "sample": f"200 time steps of shot 0 ({p.nx} x {p.ny}), FP64 C++ restatement, "
+                                         "OpenMP"}
+    bytes_cell = 52.0
+    peak, peak_kind = measured_peak()
+    achieved = value * 1e6 * bytes_cell / 1e9
+    line = {
+        "metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch2d_256_shots", "shots": len(shots), "cell_updates": cells,
+                   "l2": "inputs larger than L2 (about 4.5 GB of shot state)"},
+        "sequential_single_shot": {"value": round(seq, 3), "unit": "Mcell-updates/s",
+                                   "speedup_of_batch": round(value / seq, 3)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "bytes_per_cell_update": "52 (fields and per-cell model; C-PML memory variables not counted)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(world * cells * args.steps / e2e_s / 1e6, 3), "unit": "Mcell-updates/s",
+                "h2d_bytes_per_step": sum(12 * sh[0].nx * sh[0].ny for sh in shots),
+                "d2h_bytes_per_step": sum(2 * 8 * len(sh[2]) * sh[0].nstep for sh in shots)},
+        "gpu_launches": args.steps,
+        "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -519,6 +684,13 @@ def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
     try:
+        if args.workload in ("2d_plain", "batch2d") and args.impl != "reference":
+            return (run_2d_plain if args.workload == "2d_plain" else run_batch2d)(args, world, rank, local, pg)
+        if args.workload in ("2d_plain", "batch2d"):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement is timed inside "
+                                  "this workload's own line (cpu_baseline)"}))
+            return 0
         if args.workload == "surrogate":
             if args.impl == "reference":
                 print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned "

@@ -192,6 +192,11 @@ int cpml_get_stream(cpml_handle* h, void** stream);
    drives this. */
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth);
 int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth);
+/* Kernels one time step launches with the current tuning, and kernels per
+   chunk of steps (the FP64 reduction and the step counter); a chunk ends at
+   it = 5 and every IT_DISPLAY steps. For launch accounting; no reference
+   counterpart. */
+int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels);
 
 /* Autotune the step kernel for this handle's grid: every candidate (one-sweep
    kernel with tile_y in {8,16} x zchunk in {16,24,32,48,64}, and the two-sweep

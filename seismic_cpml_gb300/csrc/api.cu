@@ -44,6 +44,7 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
 void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4* gen, const int n_cls[4],
                        const cudaStream_t aux[4], cudaEvent_t fork, const cudaEvent_t join[4]);
 cudaError_t fused3d_launch(const void* plan_mem, const StepArgs& s, int ls, int parity, cudaStream_t st);
+int fused3d_kernels_per_step(const void* plan_mem);
 }  // namespace cpml
 
 using namespace cpml;
@@ -733,6 +734,13 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
   if (tile_y) *tile_y = h->tile_y;
   if (zchunk) *zchunk = h->zchunk;
   if (depth) *depth = h->depth;
+  return CPML_OK;
+}
+
+int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels) {
+  if (!h) return CPML_ERR_INVALID;
+  if (step_kernels) *step_kernels = h->pingpong ? fused3d_kernels_per_step(h->plan.data()) : 2;
+  if (chunk_kernels) *chunk_kernels = 2;   // chunk reduction + step counter
   return CPML_OK;
 }
 

@@ -932,6 +932,13 @@ void fused3d_set_items(void* plan_mem, const int4* fast, int n_fast, const int4*
 
 size_t fused3d_plan_bytes() { return sizeof(FusedPlan); }
 
+int fused3d_kernels_per_step(const void* plan_mem) {
+  const FusedPlan* P = static_cast<const FusedPlan*>(plan_mem);
+  int n = P->n_fast > 0 ? 1 : 0;
+  for (int c = 0; c < 4; ++c) n += P->n_cls[c] > 0 ? 1 : 0;
+  return n;
+}
+
 template <int TY, bool HET>
 static void launch_classes(const FusedPlan* P, const StepArgs& s, int ls, int parity, cudaStream_t st) {
   const size_t smf = Geo<TY, HET>::SMEM, smg = Geo<8, HET>::SMEM;

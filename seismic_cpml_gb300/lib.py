@@ -46,6 +46,7 @@ SIGNATURES = [
     ("cpml_get_stream", ctypes.c_int, [_h, _P(ctypes.c_void_p)]),
     ("cpml_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("cpml_get_tuning", ctypes.c_int, [_h, _ip, _ip, _ip, _ip]),
+    ("cpml_launches_per_step", ctypes.c_int, [_h, _ip, _ip]),
     ("cpml_autotune", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_char_p, _ip, _ip, _ip, _dp]),
     ("cpml_destroy", None, [_h]),
     ("cpml_batch_create", ctypes.c_int, [ctypes.c_int, _P(CpmlParams), _P(_h)]),

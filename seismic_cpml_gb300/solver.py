@@ -67,6 +67,12 @@ class Solver:
         _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk), int(depth)),
                  "set_tuning")
 
+    def launches_per_step(self):
+        """(kernels per time step, kernels per chunk of steps)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _L.check(self.L.cpml_launches_per_step(self.h, ctypes.byref(a), ctypes.byref(b)), "cpml_launches_per_step")
+        return a.value, b.value
+
     def tuning(self):
         k, t, z, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _L.check(self.L.cpml_get_tuning(self.h, ctypes.byref(k), ctypes.byref(t), ctypes.byref(z),

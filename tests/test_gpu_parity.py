@@ -250,3 +250,12 @@ def test_large_config_generator_at_reduced_size_vs_oracle():
     g = run_gpu(p, rec, model=(lam, mu, rho))
     ref = oracle_c.run(p, rec=rec, lam=lam, mu=mu, rho=rho)
     check(g, ref)
+
+
+def test_launch_accounting():
+    p, rec = P.small_3d()
+    with Solver(p, rec, tuning=(2, 8, 16, 2)) as s:
+        k, c = s.launches_per_step()
+        assert 2 <= k <= 5 and c == 2
+    with Solver(p, rec, tuning=(1, 8, 16, 2)) as s:
+        assert s.launches_per_step() == (2, 2)
