@@ -238,17 +238,19 @@ class Surrogate:
         return S
 
     # ---- forward / backward -------------------------------------------------
-    def forward(self, xb, slot, B):
+    def forward(self, xb, slot, B, keep=True):
         """xb: bf16 [B, h, w, cin] and slot: int32 [B] (each shot's source
         receiver slot), on the device. Leaves the traces in buffer 'p'
-        ([B, nrec*nt] FP32) and the misfit head in 'head'."""
+        ([B, nrec*nt] FP32) and the misfit head in 'head'. keep=False (pure
+        inference) skips the FP32 copies of the activations that only the
+        backward pass reads."""
         c, S, st = self.cfg, self._buffers(B), self._stream()
         a = xb
         for l, (H, W, ci, co) in enumerate(c.levels()):
             Ho, Wo = (H + 1) // 2, (W + 1) // 2
             M, K = B * Ho * Wo, 9 * ci
             self._call("cpml_nn_im2col", _ptr(a), _ptr(S["col"][l]), B, H, W, ci, st)
-            self._gemm(M, co, K, S["col"][l], K, 0, self.Pb[f"conv{l}_w"], K, 1, Cf=S["y"][l],
+            self._gemm(M, co, K, S["col"][l], K, 0, self.Pb[f"conv{l}_w"], K, 1, Cf=S["y"][l] if keep else None,
                        Cb=S["a"][l], bias=self.P[f"conv{l}_b"], relu=1, work=S["work"])
             a = S["a"][l]
         F, lat, R, no = c.flat(), c.latent, c.noff() * c.modes, c.noff()
@@ -360,7 +362,7 @@ class Surrogate:
         head = torch.empty(n, dtype=torch.float32, device=self.dev)
         for s in range(0, n, batch):
             b = min(batch, n - s)
-            S = self.forward(X[s:s + b], slot[s:s + b], b)
+            S = self.forward(X[s:s + b], slot[s:s + b], b, keep=False)
             P[s:s + b].copy_(S["p"][:b * c.nrec * c.nt].view(b, -1))
             head[s:s + b].copy_(S["head"][:b])
         return P, head
@@ -534,3 +536,33 @@ def run_with_fallback(net: Surrogate, spec: ShotSpec, seed: int, indices, X, slo
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     return P, mask, t1 - t0, t2 - t1
+
+
+def _main(argv=None):
+    """`python -m seismic_cpml_gb300.surrogate [--shots N] [--batch B] [--gemm tcgen05|mma] [--repeat R]`:
+    time inference of an untrained default network on random inputs (the
+    kernel mix of a prediction pass; the accuracy is not exercised)."""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shots", type=int, default=2048)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--gemm", choices=["tcgen05", "mma"], default="tcgen05")
+    ap.add_argument("--repeat", type=int, default=5)
+    a = ap.parse_args(argv)
+    cfg = NetConfig()
+    g = torch.Generator(device="cpu").manual_seed(0)
+    X = torch.randn(a.shots, cfg.h, cfg.w, cfg.cin, generator=g).to(torch.bfloat16).cuda()
+    S = torch.randint(0, cfg.nrec, (a.shots,), generator=g, dtype=torch.int32).cuda()
+    net = Surrogate(cfg, seed=0, gemm=a.gemm)
+    P, _ = net.predict(X, S, batch=a.batch)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(a.repeat):
+        net.predict(X, S, batch=a.batch, out=P)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t) / a.repeat
+    print(f"{a.gemm}: {a.shots / dt:.0f} shots/s ({a.shots} shots, batch {a.batch})")
+
+
+if __name__ == "__main__":
+    _main()
