@@ -12,9 +12,11 @@ depend on where the source is:
   input [B, 128, 256, 8]: the 2 x 2 mean of the 256 x 256 interior cp map,
         (cp - 3000) / 1000, written into a window twice as wide whose centre
         column is the source column; a channel that is 1 inside the model;
-        a channel marking the receivers (top row); five zero channels, so
-        that every pixel is 16 bytes and the first layer's patches and
-        weights take the 16-byte vector paths
+        a channel marking the receivers (top row); the source's offset from
+        its nearest receiver and its position inside its downsampled pixel
+        (two constant planes); three zero channels, so that every pixel is
+        16 bytes and the first layer's patches and weights take the 16-byte
+        vector paths
   5 x { 3x3 stride-2 conv + bias + ReLU }: 8 -> 32 -> 64 -> 128 -> 256 -> 256
   dense 4 * 8 * 256 -> latent (ReLU); dense latent -> (2 nrec - 1) x modes
         coefficients, one trace per receiver offset -(nrec-1) .. nrec-1
@@ -44,7 +46,7 @@ from .earth import gardner, lame_from_velocity
 from .params import STF_RICKER, default_2d
 
 SM_COUNT = 152
-IN_CHANNELS = 8   # cp, model mask, receivers + 5 zero channels
+IN_CHANNELS = 8   # cp, model mask, receivers, source offset, source sub-pixel + 3 zero channels
 
 
 @dataclass(frozen=True)
@@ -457,7 +459,11 @@ def encode_input(spec: ShotSpec, cp_inner, col):
     """[hw, 2 hw, 8] float32 network input in the source's frame: the
     downsampled normalised cp map placed so that the source column lands on
     column hw, a mask of the model window, the receiver positions on the
-    receivers' row, and five zero channels (16-byte pixels)."""
+    receivers' row, two constant planes that restore what the 2 x
+    downsampling and the receiver slots lose about the source position (the
+    source's offset from its nearest receiver in cells / 2, and the source
+    column's position inside its downsampled pixel), and three zero channels
+    (16-byte pixels)."""
     f = spec.interior // spec.hw
     small = cp_inner.reshape(spec.hw, f, spec.hw, f).mean(axis=(1, 3))
     x = np.zeros((spec.hw, 2 * spec.hw, IN_CHANNELS), np.float32)
@@ -465,8 +471,11 @@ def encode_input(spec: ShotSpec, cp_inner, col):
     x[:, o:o + spec.hw, 0] = (small - 3000.0) / 1000.0
     x[:, o:o + spec.hw, 1] = 1.0
     row = (spec.interior - 2) // f          # receivers one row below the top interior row
-    for r in range(spec.nrec):
-        x[row, o + int(round(r * (spec.interior - 1) / (spec.nrec - 1))) // f, 2] = 1.0
+    rcol = [int(round(r * (spec.interior - 1) / (spec.nrec - 1))) for r in range(spec.nrec)]
+    for c in rcol:
+        x[row, o + c // f, 2] = 1.0
+    x[:, o:o + spec.hw, 3] = (col - rcol[source_slot(spec, col)]) / 2.0
+    x[:, o:o + spec.hw, 4] = (col % f) / max(f - 1, 1)
     return x
 
 

@@ -100,7 +100,8 @@ def test_shot_generator_is_seeded_and_stable():
     assert len(a[2]) == 64 and all(21 <= r[0] <= 276 for r in a[2])
     assert 21 <= p.isource <= 276
     x = encode_input(spec, a[3], a[4])
-    assert x.shape == (128, 256, 8) and not x[..., 3:].any()
+    assert x.shape == (128, 256, 8) and not x[..., 5:].any()
+    assert np.all(np.abs(x[..., 3]) <= 1.0) and set(np.unique(x[..., 4])) <= {0.0, 1.0}
     o = 128 - a[4] // 2                       # model window starts here; source column lands on 128
     assert x[..., 1].sum() == 128 * 128 and np.all(x[:, o:o + 128, 1] == 1.0)
     small = a[3].reshape(128, 2, 128, 2).mean(axis=(1, 3))
