@@ -324,7 +324,6 @@ int build_schedule(cpml_batch* b) {
 }
 
 cudaError_t launch_batch(cpml_batch* b) {
-  void* kargs[] = {&b->args};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(b->grid);
   cfg.blockDim = dim3(BNT);
@@ -334,7 +333,6 @@ cudaError_t launch_batch(cpml_batch* b) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  (void)kargs;
   return cudaLaunchKernelEx(&cfg, batch2d_kernel, b->args);
 }
 
