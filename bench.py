@@ -348,7 +348,7 @@ def run_ours(args, world, rank, local, pg):
                               "autotuned": tune is not None}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "traffic_source": ("ncu --set full, one step, tuning %s (profiles/fused3d_276cube.md)"
+                     "traffic_source": ("ncu DRAM bytes of one step, tuning %s (profiles/fused3d_276cube.md)"
                                         % traffic_tuning) if traffic else None,
                      "peak_source": peak_kind,
                      "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 5)},
