@@ -4,7 +4,8 @@ A small convolutional network maps a 2D velocity model and a source position
 to the vertical-velocity seismograms of a line of surface receivers. It is
 trained only on shots that the batched FD engine (cpml_batch_*) computes, and
 at inference every shot whose predicted misfit is above a threshold is re-run
-by that engine, which is both the fallback and the judge. No counterpart in
+by that engine, which is both the fallback and the yardstick the misfit is
+measured against. No counterpart in
 the reference, which has no learned component.
 
 The network works in the source's frame, so that what it learns does not
