@@ -46,7 +46,6 @@ from .batch import Batch
 from .earth import gardner, lame_from_velocity
 from .params import STF_RICKER, default_2d
 
-SM_COUNT = 152
 IN_CHANNELS = 8   # cp, model mask, receivers, source offset, source sub-pixel + 3 zero channels
 
 
@@ -115,6 +114,7 @@ class Surrogate:
         self.L = _L.load()
         self.cfg = cfg
         self.gemm_entry = "cpml_nn_gemm_tc" if gemm == "tcgen05" else "cpml_nn_gemm"
+        self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.launches = 0        # kernels this object has launched (launch accounting)
         self.dev = torch.device(device)
         self.shapes = cfg.param_shapes()
@@ -195,7 +195,7 @@ class Surrogate:
               accum=0, alpha=1.0, work=None):
         tm = 128 if self.gemm_entry == "cpml_nn_gemm_tc" else 64
         tiles = -(-M // tm) * -(-N // tm)
-        splits = max(1, min(K // 512, -(-2 * SM_COUNT // tiles)))
+        splits = max(1, min(K // 512, -(-2 * self.sms // tiles)))
         wk = work if splits > 1 else None
         if wk is not None and wk.numel() < splits * M * N:
             splits = max(1, wk.numel() // (M * N))
@@ -236,7 +236,7 @@ class Surrogate:
             dcol=torch.empty(max_dcol, **f32), da=torch.empty(max_da, **f32),
             shift=torch.empty(B, dtype=torch.int32, device=self.dev),
             shift_neg=torch.empty(B, dtype=torch.int32, device=self.dev),
-            work=torch.empty(max(1 << 21, 2 * SM_COUNT * 64 * 64 * 4), **f32))
+            work=torch.empty(max(1 << 21, 2 * self.sms * 64 * 64 * 4), **f32))
         self._bufs[B] = S
         return S
 
