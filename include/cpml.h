@@ -229,6 +229,11 @@ int cpml_batch_run(cpml_batch* b);
 int cpml_batch_get_seismograms(cpml_batch* b, int shot, double* vx, double* vy);
 int cpml_batch_get_field(cpml_batch* b, int shot, int field, float* out);
 int cpml_batch_last_run_ms(cpml_batch* b, double* ms);
+/* Bound, in SM clock cycles, of one wait at the engine's grid barrier
+   (0 restores the default, about 2 s). A wait that runs out makes
+   cpml_batch_run return CPML_ERR_TIMEOUT with every CTA of the launch
+   returned; the next run starts clean. For tests of that path. */
+int cpml_batch_set_wait_limit(cpml_batch* b, long long cycles);
 void cpml_batch_destroy(cpml_batch* b);
 
 /* Kinetic and potential energy (the 3D program's formulas, 3D:1131-1180) of

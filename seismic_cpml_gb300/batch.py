@@ -47,6 +47,10 @@ class Batch:
     def run(self) -> None:
         _L.check(self.L.cpml_batch_run(self.h), "cpml_batch_run")
 
+    def set_wait_limit(self, cycles: int) -> None:
+        """Bound of one grid-barrier wait in SM cycles (0 = default)."""
+        _L.check(self.L.cpml_batch_set_wait_limit(self.h, int(cycles)), "cpml_batch_set_wait_limit")
+
     def last_run_ms(self) -> float:
         v = ctypes.c_double()
         _L.check(self.L.cpml_batch_last_run_ms(self.h, ctypes.byref(v)))

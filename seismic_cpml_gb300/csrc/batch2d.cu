@@ -49,6 +49,7 @@ struct BatchArgs {
   int max_nstep;
   unsigned* bar;            // [0] arrivals, [1] generation
   int* err;                 // 2 = barrier gave up, 4 = non-finite velocity
+  long long wait_cycles;    // bound of one grid-barrier wait
 };
 
 // Bounded grid barrier of a cooperative launch (every CTA is resident).
@@ -68,7 +69,7 @@ __device__ __forceinline__ bool grid_sync(const BatchArgs& a) {
     } else {
       const long long t0 = clock64();
       while (*gen == g) {
-        if (clock64() - t0 > kBarrierCycles) { atomicOr(a.err, 2); break; }
+        if (clock64() - t0 > a.wait_cycles) { atomicOr(a.err, 2); break; }
         __nanosleep(64);
       }
     }
@@ -167,6 +168,7 @@ struct cpml_batch {
   int max_nstep = 0;
   int grid = 0;
   bool dirty = true;
+  long long wait_cycles = 0;  // 0: the default bound of a grid-barrier wait
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
   BatchArgs args{};
@@ -317,6 +319,7 @@ int build_schedule(cpml_batch* b) {
   A.shots = b->d_shots; A.items = b->d_items; A.items_at = b->d_items_at; A.recs_at = b->d_recs_at;
   A.rec = b->d_rec; A.rec_off = b->d_rec_off; A.rec_offy = b->d_rec_offy; A.seis = b->d_seis;
   A.max_nstep = b->max_nstep; A.bar = b->d_bar; A.err = b->d_err;
+  A.wait_cycles = b->wait_cycles > 0 ? b->wait_cycles : kBarrierCycles;
   b->dirty = false;
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
   b->graph_ok = false;
@@ -527,6 +530,13 @@ int cpml_batch_get_field(cpml_batch* b, int shot, int field, float* out) {
   }
   BCK(cudaMemcpy2D(out, 4 * size_t(H.p.nx), f, 4 * size_t(H.px), 4 * size_t(H.p.nx), H.p.ny,
                    cudaMemcpyDeviceToHost));
+  return CPML_OK;
+}
+
+int cpml_batch_set_wait_limit(cpml_batch* b, long long cycles) {
+  if (!b || cycles < 0) return CPML_ERR_INVALID;
+  b->wait_cycles = cycles;
+  b->dirty = true;   // the bound travels in the captured launch arguments
   return CPML_OK;
 }
 

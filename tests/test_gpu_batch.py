@@ -55,3 +55,25 @@ def test_batch_rerun_is_deterministic():
         b.run()
         for s in range(3):
             assert np.array_equal(b.seismograms(s)[0], a[s])
+
+
+def test_barrier_timeout_is_reported_and_the_next_run_is_clean():
+    """A grid-barrier wait bound of one cycle runs out at the first barrier:
+    every CTA returns, cpml_batch_run reports CPML_ERR_TIMEOUT, and with the
+    default bound the same batch runs again to the exact results of a fresh
+    batch (the context stays usable; nothing faults or hangs)."""
+    from seismic_cpml_gb300.lib import CpmlError
+    shots = small_shots()[:3]
+    args = ([p for p, _, _ in shots], None, [r for _, _, r in shots])
+    with Batch(*args) as ref:
+        ref.run()
+        want = [ref.seismograms(s)[0].copy() for s in range(3)]
+    with Batch(*args) as b:
+        b.set_wait_limit(1)
+        with pytest.raises(CpmlError) as e:
+            b.run()
+        assert e.value.status == -5                         # CPML_ERR_TIMEOUT
+        b.set_wait_limit(0)
+        b.run()
+        for s in range(3):
+            assert np.array_equal(b.seismograms(s)[0], want[s])
