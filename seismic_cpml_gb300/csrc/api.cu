@@ -94,6 +94,8 @@ struct cpml_handle {
   int* rec_cell = nullptr;
   float* seis = nullptr;
   double* partials = nullptr;
+  int4* items_fast = nullptr;  // fused-path item lists (device copies of the plan's tables)
+  int4* items_gen = nullptr;
   int nblocks = 0;
   double *ek = nullptr, *ep = nullptr, *vmax = nullptr;
   int* bad = nullptr;
@@ -130,6 +132,31 @@ int dalloc(cpml_handle* h, T** out, size_t count) {
   if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
   h->allocs.push_back(ptr);
   *out = (T*)ptr;
+  return CPML_OK;
+}
+
+// Releases one buffer that dalloc made (no-op for nullptr). cudaFree waits for
+// the device, so no launch still reads it.
+void dfree(cpml_handle* h, void* ptr) {
+  if (!ptr) return;
+  for (size_t i = 0; i < h->allocs.size(); ++i)
+    if (h->allocs[i] == ptr) {
+      h->allocs[i] = h->allocs.back();
+      h->allocs.pop_back();
+      cudaFree(ptr);
+      return;
+    }
+}
+
+// Replaces *slot by a fresh buffer of count elements; the old buffer is
+// released only once the new one exists, so a failed call leaves *slot as it was.
+template <typename T>
+int drealloc(cpml_handle* h, T** slot, size_t count) {
+  T* fresh = nullptr;
+  int st = dalloc(h, &fresh, count);
+  if (st) return st;
+  dfree(h, *slot);
+  *slot = fresh;
   return CPML_OK;
 }
 
@@ -391,9 +418,10 @@ int configure_path(cpml_handle* h) {
     int n_cls[4] = {0, 0, 0, 0};
     fused3d_items(h->nx, h->ny, h->nz, h->axes[0], h->axes[1], h->axes[2], h->p.npoints_pml, h->tile_y,
                   h->zchunk, h->het, fast, gen, n_cls);
-    int4 *dfast = nullptr, *dgen = nullptr;
-    if ((st = dalloc(h, &dfast, fast.size()))) return st;
-    if ((st = dalloc(h, &dgen, gen.size()))) return st;
+    drop_graphs(h);  // cached graphs launch with the item lists about to be replaced
+    if ((st = drealloc(h, &h->items_fast, fast.size()))) return st;
+    if ((st = drealloc(h, &h->items_gen, gen.size()))) return st;
+    int4 *dfast = h->items_fast, *dgen = h->items_gen;
     if (!fast.empty())
       CK(cudaMemcpy(dfast, fast.data(), sizeof(int4) * fast.size(), cudaMemcpyHostToDevice));
     if (!gen.empty())
@@ -414,7 +442,8 @@ int configure_path(cpml_handle* h) {
   h->pingpong = fused;
   const size_t need = size_t(kMaxChunk) * h->nblocks * 4;
   if (need > h->partials_cap) {
-    if ((st = dalloc(h, &h->partials, need))) return st;
+    drop_graphs(h);
+    if ((st = drealloc(h, &h->partials, need))) return st;
     h->partials_cap = need;
   }
   drop_graphs(h);
@@ -538,8 +567,9 @@ int cpml_set_receivers(cpml_handle* h, int nrec, const int* ix, const int* iy, c
   if (h->it != 0) return CPML_ERR_INVALID;  // set receivers before running (or after reset)
   int st;
   if (nrec > std::max(h->nrec, 1)) {
-    if ((st = dalloc(h, &h->rec_cell, size_t(nrec)))) return st;
-    if ((st = dalloc(h, &h->seis, size_t(3) * nrec * h->p.nstep))) return st;
+    drop_graphs(h);
+    if ((st = drealloc(h, &h->rec_cell, size_t(nrec)))) return st;
+    if ((st = drealloc(h, &h->seis, size_t(3) * nrec * h->p.nstep))) return st;
   }
   h->nrec = nrec;
   h->rec_ijk = ijk;
@@ -832,10 +862,10 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
 void cpml_destroy(cpml_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  drop_graphs(h);
-  for (void* p : h->allocs) cudaFree(p);
   for (int c = 0; c < 4; ++c)
     if (h->aux[c]) cudaStreamSynchronize(h->aux[c]);
+  drop_graphs(h);
+  for (void* p : h->allocs) cudaFree(p);
   if (h->fork) cudaEventDestroy(h->fork);
   for (int c = 0; c < 4; ++c) {
     if (h->join[c]) cudaEventDestroy(h->join[c]);

@@ -199,6 +199,27 @@ int balloc(cpml_batch* b, T** out, size_t n) {
   return CPML_OK;
 }
 
+// Replaces *slot by a fresh buffer of n elements and releases the old one
+// (cudaFree waits for the device, so no launch still reads it); on failure
+// *slot is left as it was.
+template <typename T>
+int brealloc(cpml_batch* b, T** slot, size_t n) {
+  T* fresh = nullptr;
+  int st = balloc(b, &fresh, n);
+  if (st) return st;
+  if (*slot) {
+    for (size_t i = 0; i < b->allocs.size(); ++i)
+      if (b->allocs[i] == (void*)*slot) {
+        b->allocs[i] = b->allocs.back();
+        b->allocs.pop_back();
+        cudaFree((void*)*slot);
+        break;
+      }
+  }
+  *slot = fresh;
+  return CPML_OK;
+}
+
 // FP64 profile of one axis on the GPU, slab extents from its a / a_half.
 int shot_axis(cpml_batch* b, const cpml_params& p, int axis, int n, double delta, Axis* A) {
   ProfileArgs P{};
@@ -284,13 +305,13 @@ int build_schedule(cpml_batch* b) {
     recs_at[t] = k ? recs_end[k - 1] : 0;
   }
   int st;
-  if ((st = balloc(b, &b->d_items, std::max<size_t>(items.size(), 1)))) return st;
-  if ((st = balloc(b, &b->d_items_at, std::max(b->max_nstep, 1)))) return st;
-  if ((st = balloc(b, &b->d_recs_at, std::max(b->max_nstep, 1)))) return st;
-  if ((st = balloc(b, &b->d_rec, std::max<size_t>(rec.size(), 1)))) return st;
-  if ((st = balloc(b, &b->d_rec_off, std::max<size_t>(off.size(), 1)))) return st;
-  if ((st = balloc(b, &b->d_rec_offy, std::max<size_t>(offy.size(), 1)))) return st;
-  if ((st = balloc(b, &b->d_seis, std::max<size_t>(seis_total, 1)))) return st;
+  if ((st = brealloc(b, &b->d_items, std::max<size_t>(items.size(), 1)))) return st;
+  if ((st = brealloc(b, &b->d_items_at, std::max(b->max_nstep, 1)))) return st;
+  if ((st = brealloc(b, &b->d_recs_at, std::max(b->max_nstep, 1)))) return st;
+  if ((st = brealloc(b, &b->d_rec, std::max<size_t>(rec.size(), 1)))) return st;
+  if ((st = brealloc(b, &b->d_rec_off, std::max<size_t>(off.size(), 1)))) return st;
+  if ((st = brealloc(b, &b->d_rec_offy, std::max<size_t>(offy.size(), 1)))) return st;
+  if ((st = brealloc(b, &b->d_seis, std::max<size_t>(seis_total, 1)))) return st;
   b->seis_floats = seis_total;
   if (!items.empty()) BCK(cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
   if (b->max_nstep) {

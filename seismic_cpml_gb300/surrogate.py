@@ -114,9 +114,9 @@ class Surrogate:
         self.L = _L.load()
         self.cfg = cfg
         self.gemm_entry = "cpml_nn_gemm_tc" if gemm == "tcgen05" else "cpml_nn_gemm"
+        self.dev = torch.device(device)
         self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.launches = 0        # kernels this object has launched (launch accounting)
-        self.dev = torch.device(device)
         self.shapes = cfg.param_shapes()
         self.off, o = {}, 0
         for name, shp in self.shapes:
