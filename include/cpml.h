@@ -56,9 +56,14 @@ extern "C" {
 #define CPML_FLAG_NO_STABILITY  0x4  /* skip the max|v| blow-up check at IT_DISPLAY cadence      */
 
 /* ---- step kernels (cpml_set_tuning) ----------------------------------- */
-#define CPML_KERNEL_AUTO      0  /* fused one-sweep kernel in 3D, two-sweep in 2D     */
-#define CPML_KERNEL_TWO_SWEEP 1  /* stress kernel + velocity kernel, in place         */
-#define CPML_KERNEL_FUSED     2  /* 3D only: one kernel per step, two buffer sets, TMA */
+#define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: persistent when the
+                                     grid has more 32 x 8 tiles than the GPU holds
+                                     resident CTAs, else two-sweep                      */
+#define CPML_KERNEL_TWO_SWEEP  1  /* stress kernel + velocity kernel, in place          */
+#define CPML_KERNEL_FUSED      2  /* 3D only: one kernel per step, two buffer sets, TMA  */
+#define CPML_KERNEL_PERSISTENT 3  /* 2D only: the two sweeps of a whole chunk of steps in
+                                     one cooperative launch, grid barriers between them;
+                                     results bit-identical to CPML_KERNEL_TWO_SWEEP      */
 
 /* ---- fields (for cpml_get_field / cpml_get_plane) ---------------------- */
 #define CPML_FIELD_VX  0
@@ -185,9 +190,11 @@ int cpml_last_run_ms(cpml_handle* h, double* ms);
    counterpart: the reference has no device. */
 int cpml_get_stream(cpml_handle* h, void** stream);
 
-/* Select the step kernel and its launch shape: tile_y (rows of the 32-wide
-   tile), zchunk (planes per CTA in the z sweep) and depth (planes the TMA
-   loads run ahead). Supported (tile_y, depth): (8,2) (16,2). Only on a fresh or reset handle. No reference counterpart: the
+/* Select the step kernel (CPML_KERNEL_*; FUSED is 3D only, PERSISTENT 2D
+   only: CPML_ERR_INVALID otherwise) and its launch shape: tile_y (rows of the
+   32-wide tile), zchunk (planes per CTA in the z sweep) and depth (planes the
+   TMA loads run ahead); the shape only matters to the fused kernel.
+   Supported (tile_y, depth): (8,2) (16,2). Only on a fresh or reset handle. No reference counterpart: the
    reference's loop nests (3D:825-1052) have no tunables; the autotuner
    drives this. */
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth);
@@ -198,9 +205,9 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
    counterpart. */
 int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels);
 
-/* Autotune the step kernel for this handle's grid: every candidate (one-sweep
-   kernel with tile_y in {8,16} x zchunk in {16,24,32,48,64}, and the two-sweep
-   kernel) runs 2 untimed then trial_steps timed steps (CUDA events on the
+/* Autotune the step kernel for this handle's grid: every candidate (3D: the
+   one-sweep kernel with tile_y in {8,16} x zchunk in {16,24,32,48,64}; 2D: the
+   persistent kernel; both: the two-sweep kernel) runs 2 untimed then trial_steps timed steps (CUDA events on the
    handle's stream); the fastest is applied. Results are cached per shape
    class (ndim, grid, per-cell model, NPML, PML faces) for the process and,
    when cache_path is not NULL, in that text file (one line per class). Leaves

@@ -31,6 +31,9 @@ void launch_reduce_chunk(const StepArgs& s, int C, double* ek, double* ep, doubl
                          cudaStream_t st);
 void launch_step3d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
 void launch_step2d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
+int persist2d_grid(const StepArgs& s, bool het);
+cudaError_t launch_chunk2d_persistent(const StepArgs& s, int C, bool het, unsigned* bar, int grid,
+                                      cudaStream_t st);
 int blocks3d(const StepArgs& s);
 int blocks2d(const StepArgs& s);
 bool fused3d_supported();
@@ -74,6 +77,9 @@ struct cpml_handle {
   float* fld[9] = {};      // buffer set 0
   float* fld1[9] = {};     // buffer set 1 (fused 3D path: time n+1 while set 0 holds n)
   bool pingpong = false;   // fields alternate between the sets every step
+  bool persist = false;    // 2D: one cooperative launch per chunk of steps
+  int persist_grid = 0;    // its CTAs
+  unsigned* bar = nullptr; // its grid-barrier words
   int kernel = 0;          // CPML_KERNEL_*
   int tile_y = 8, zchunk = 24, depth = 2;
   std::vector<unsigned char> plan;  // fused-path tensor maps and item lists
@@ -370,7 +376,17 @@ int get_graph(cpml_handle* h, int C, cudaGraphExec_t* out) {
   if (it != h->graphs.end()) { *out = it->second; return CPML_OK; }
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int ls = 0; ls < C; ++ls) launch_step(h, h->pingpong ? ((q0 + ls) & 1) : 0, ls);
+  if (h->persist) {
+    const cudaError_t le = launch_chunk2d_persistent(make_args(h), C, h->het, h->bar, h->persist_grid, h->stream);
+    if (le != cudaSuccess) {
+      cudaStreamEndCapture(h->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return cuda_status(le);
+    }
+  } else {
+    for (int ls = 0; ls < C; ++ls) launch_step(h, h->pingpong ? ((q0 + ls) & 1) : 0, ls);
+  }
   const StepArgs s = make_args(h, h->pingpong ? ((q0 + C) & 1) : 0);  // set holding the chunk's result
   launch_reduce_chunk(s, C, h->ek, h->ep, h->vmax, h->bad, h->stream);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -438,6 +454,21 @@ int configure_path(cpml_handle* h) {
   } else {
     StepArgs s = make_args(h);
     h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
+  }
+  h->persist = false;
+  if (h->ndim == 2 && h->kernel != CPML_KERNEL_TWO_SWEEP) {
+    const StepArgs s = make_args(h);
+    h->persist_grid = persist2d_grid(s, h->het);
+    // automatic choice: persistent only when the grid has more tiles than
+    // the GPU holds resident CTAs; a grid that fits in one wave is latency-
+    // bound, and there the two kernels per step replayed from a CUDA graph
+    // measured faster than two grid barriers per step
+    if (h->persist_grid < 1) {
+      if (h->kernel == CPML_KERNEL_PERSISTENT) return CPML_ERR_CUDA;
+    } else if (h->kernel == CPML_KERNEL_PERSISTENT || h->nblocks > h->persist_grid) {
+      if (!h->bar && (st = dalloc(h, &h->bar, 2))) return st;
+      h->persist = true;
+    }
   }
   h->pingpong = fused;
   const size_t need = size_t(kMaxChunk) * h->nblocks * 4;
@@ -748,7 +779,9 @@ int cpml_last_run_ms(cpml_handle* h, double* ms) {
 }
 
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth) {
-  if (!h || kernel < 0 || kernel > 2) return CPML_ERR_INVALID;
+  if (!h || kernel < 0 || kernel > 3) return CPML_ERR_INVALID;
+  if ((kernel == CPML_KERNEL_FUSED && h->ndim != 3) || (kernel == CPML_KERNEL_PERSISTENT && h->ndim != 2))
+    return CPML_ERR_INVALID;
   if (zchunk < 2 || !fused3d_shape_ok(tile_y, depth)) return CPML_ERR_INVALID;
   if (h->it != 0) return CPML_ERR_INVALID;  // only on a fresh or reset handle
   h->kernel = kernel;
@@ -760,7 +793,8 @@ int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int dept
 
 int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth) {
   if (!h) return CPML_ERR_INVALID;
-  if (kernel) *kernel = h->pingpong ? CPML_KERNEL_FUSED : CPML_KERNEL_TWO_SWEEP;
+  if (kernel)
+    *kernel = h->pingpong ? CPML_KERNEL_FUSED : (h->persist ? CPML_KERNEL_PERSISTENT : CPML_KERNEL_TWO_SWEEP);
   if (tile_y) *tile_y = h->tile_y;
   if (zchunk) *zchunk = h->zchunk;
   if (depth) *depth = h->depth;
@@ -769,8 +803,9 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
 
 int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels) {
   if (!h) return CPML_ERR_INVALID;
-  if (step_kernels) *step_kernels = h->pingpong ? fused3d_kernels_per_step(h->plan.data()) : 2;
-  if (chunk_kernels) *chunk_kernels = 2;   // chunk reduction + step counter
+  if (step_kernels) *step_kernels = h->pingpong ? fused3d_kernels_per_step(h->plan.data()) : (h->persist ? 0 : 2);
+  // chunk reduction + step counter (+ the persistent 2D launch, which runs the chunk's steps)
+  if (chunk_kernels) *chunk_kernels = h->persist ? 3 : 2;
   return CPML_OK;
 }
 
@@ -826,6 +861,9 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
       for (int ty : {8, 16})
         for (int lz : {16, 24, 32, 48, 64}) cand.push_back(TuneVal{CPML_KERNEL_FUSED, ty, lz, 2, 0.0});
     cand.push_back(TuneVal{CPML_KERNEL_TWO_SWEEP, 8, 32, 2, 0.0});
+    if (h->ndim == 2) {
+      if (persist2d_grid(make_args(h), h->het) > 0) cand.push_back(TuneVal{CPML_KERNEL_PERSISTENT, 8, 32, 2, 0.0});
+    }
     const int flags = h->p.flags;
     h->p.flags |= CPML_FLAG_NO_STABILITY;  // time the kernels, not the host checks
     best.ms = 1e300;

@@ -47,37 +47,14 @@ struct BatchArgs {
   const long long* rec_offy;// sample 0 of its v_y trace
   float* seis;
   int max_nstep;
-  unsigned* bar;            // [0] arrivals, [1] generation
+  unsigned* bar;            // [0] grid-barrier arrivals (zeroed before each launch)
   int* err;                 // 2 = barrier gave up, 4 = non-finite velocity
   long long wait_cycles;    // bound of one grid-barrier wait
 };
 
-// Bounded grid barrier of a cooperative launch (every CTA is resident).
-__device__ __forceinline__ bool grid_sync(const BatchArgs& a) {
-  __syncthreads();
-  __shared__ int ok;
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned* gen = a.bar + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    const unsigned arrived = atomicAdd(a.bar, 1u) + 1u;
-    if (arrived == gridDim.x) {
-      a.bar[0] = 0u;
-      __threadfence();
-      atomicAdd(a.bar + 1, 1u);
-    } else {
-      const long long t0 = clock64();
-      while (*gen == g) {
-        if (clock64() - t0 > a.wait_cycles) { atomicOr(a.err, 2); break; }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    if (*((volatile int*)a.err) & 2) ok = 0;
-  }
-  __syncthreads();
-  return ok != 0;
+// nbar counts the launch's barriers so far (the arrival counter's target)
+__device__ __forceinline__ bool grid_sync(const BatchArgs& a, unsigned& nbar) {
+  return grid_barrier(a.bar, ++nbar * gridDim.x, a.err, 2, a.wait_cycles);
 }
 
 __device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
@@ -92,6 +69,7 @@ __device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
 
 __global__ void __launch_bounds__(BNT) batch2d_kernel(BatchArgs a) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  unsigned nbar = 0;
   for (int t = 0; t < a.max_nstep; ++t) {
     if (t > 0) record_batch(a, t - 1);
     const int n = a.items_at[t];
@@ -104,7 +82,7 @@ __global__ void __launch_bounds__(BNT) batch2d_kernel(BatchArgs a) {
         else stress2d_cell<false>(S, i, j);
       }
     }
-    if (!grid_sync(a)) return;
+    if (!grid_sync(a, nbar)) return;
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
       const int4 itm = a.items[q];
       const Shot2D& S = a.shots[itm.x];
@@ -117,7 +95,7 @@ __global__ void __launch_bounds__(BNT) batch2d_kernel(BatchArgs a) {
         if (bad) atomicOr(a.err, 4);
       }
     }
-    if (!grid_sync(a)) return;
+    if (!grid_sync(a, nbar)) return;
   }
   if (a.max_nstep > 0) record_batch(a, a.max_nstep - 1);
 }

@@ -76,6 +76,41 @@ __device__ __forceinline__ void block_partials(double ek, double ep, float vm2, 
   }
 }
 
+// Bounded grid barrier of a cooperative launch (every CTA resident) on one
+// monotonically increasing arrival counter: the n-th barrier of a launch
+// (n = 1, 2, ...) is passed once *count reaches target = n * CTAs. Thread 0
+// of each CTA arrives with a release add (ordering the CTA's earlier writes,
+// gathered by the __syncthreads) and polls with acquire loads; there is no
+// reset and no generation word, so the critical path is one arrival and the
+// poll that sees the last one. *count must be zero at launch. A wait longer
+// than wait_cycles SM cycles sets err_bit in *err and returns false; the CTA
+// then leaves the kernel, and every other CTA gives up at its next barrier
+// within the same bound. Wrap-safe: the counter never runs more than one
+// barrier's arrivals ahead of a waiting CTA's target.
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, int* err, int err_bit,
+                                             long long wait_cycles) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+    ok = 1;
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+    const long long t0 = clock64();
+    for (;;) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (clock64() - t0 > wait_cycles) {
+        atomicOr(err, err_bit);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 // v^2 check that also catches NaN / Inf (the reference's maxval would skip
 // NaN; flagging it is an extension).
 __device__ __forceinline__ int not_finite(float v2) { return !(v2 <= 3.0e38f); }

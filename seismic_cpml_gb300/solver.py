@@ -63,7 +63,7 @@ class Solver:
         self.receivers = rec
 
     def set_tuning(self, kernel: int = 0, tile_y: int = 8, zchunk: int = 24, depth: int = 2) -> None:
-        """Step kernel (0 auto, 1 two-sweep, 2 fused 3D) and launch shape."""
+        """Step kernel (0 auto, 1 two-sweep, 2 fused 3D, 3 persistent 2D) and launch shape."""
         _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk), int(depth)),
                  "set_tuning")
 

@@ -72,6 +72,45 @@ def test_2d_small(het):
     check(run_gpu(p, rec, model), ref, ref.fields, ref32.fields)
 
 
+@pytest.mark.parametrize("het", [False, True])
+@pytest.mark.parametrize("shape", [(48, 64, 300), (4000, 400, 120)], ids=["tile_per_cta", "tiles_per_cta"])
+def test_2d_persistent_is_bitwise_two_sweep(het, shape):
+    """The persistent 2D kernel (the steps of a chunk in one cooperative launch)
+    gives bit-identical seismograms, energies and fields to the two-sweep
+    kernels: on a grid with one tile per CTA, and on one (6250 tiles) larger
+    than the resident grid, where each CTA takes several tiles. Chunks of 5,
+    45 and 50 steps (IT_DISPLAY = 50) exercise several cached graphs."""
+    nx, ny, nstep = shape
+    p, rec = P.small_2d(nx=nx, ny=ny, nstep=nstep)
+    model = layered_2d(p, seed=5) if het else None
+    a = run_gpu(p, rec, model, tuning=(3, 8, 32, 2))
+    b = run_gpu(p, rec, model, tuning=(1, 8, 32, 2))
+    for k in ("vx", "vy", "ek", "ep"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.abs(a["vx"]).max() > 0 and a["ek"][-1] > 0
+    for n in a["fields"]:
+        assert np.array_equal(a["fields"][n], b["fields"][n]), n
+    assert a["it"] == b["it"] == nstep and a["vmax"] == b["vmax"]
+
+
+def test_2d_kernel_choice_and_launch_accounting():
+    p, rec = P.small_2d()                            # 16 tiles: one resident wave
+    with Solver(p, rec) as s:                        # automatic: two-sweep
+        assert s.tuning()[0] == 1 and s.launches_per_step() == (2, 2)
+    with Solver(p, rec, tuning=(3, 8, 32, 2)) as s:
+        assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
+    pb, recb = P.small_2d(nx=4000, ny=400, nstep=20)  # 6250 tiles: more than the resident CTAs
+    with Solver(pb, recb) as s:                      # automatic: persistent
+        assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
+    with Solver(p, rec) as s:
+        with pytest.raises(RuntimeError):
+            s.set_tuning(2, 8, 32, 2)                # the fused kernel is 3D only
+    p3, rec3 = P.small_3d()
+    with Solver(p3, rec3) as s:
+        with pytest.raises(RuntimeError):
+            s.set_tuning(3, 8, 32, 2)                # the persistent kernel is 2D only
+
+
 TUNINGS_3D = [(1, 8, 32, 2), (2, 16, 32, 2), (2, 8, 7, 2), (2, 16, 5, 2), (2, 8, 9, 2), (2, 8, 11, 2)]
 
 
@@ -250,6 +289,20 @@ def test_large_config_generator_at_reduced_size_vs_oracle():
     g = run_gpu(p, rec, model=(lam, mu, rho))
     ref = oracle_c.run(p, rec=rec, lam=lam, mu=mu, rho=rho)
     check(g, ref)
+
+
+def test_autotune_2d_times_both_kernels_and_keeps_results_exact():
+    p, rec = P.small_2d(nx=1200, ny=900, nstep=60)   # 4275 tiles: both 2D kernels are candidates
+    with Solver(p, rec) as s:
+        best = s.autotune(trial_steps=8)
+        assert best["kernel"] in (1, 3) and best["ms_per_step"] > 0
+        assert s.tuning()[0] == best["kernel"] and s.status()[0] == 0
+        s.run()
+        vx, vy, _ = s.seismograms()
+    with Solver(p, rec, tuning=(1, 8, 32, 2)) as t:
+        t.run()
+        tx, ty, _ = t.seismograms()
+    assert np.array_equal(vx, tx) and np.array_equal(vy, ty)
 
 
 def test_launch_accounting():
