@@ -9,7 +9,7 @@ if ROOT not in sys.path:
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (a GB300)")
 
 
 @pytest.fixture(scope="session")
