@@ -87,3 +87,28 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def _main(argv=None):
+    """Run a seeded batch (the batched workload's shot generator at a reduced
+    size) a few times and print each run's device time and rate."""
+    import argparse
+    from .workloads import batch2d_shots
+    ap = argparse.ArgumentParser(prog="python -m seismic_cpml_gb300.batch")
+    ap.add_argument("--shots", type=int, default=32)
+    ap.add_argument("--interior", type=int, nargs=2, default=(400, 600), help="interior cells per side, range")
+    ap.add_argument("--record-s", type=float, default=0.1, help="simulated seconds per shot")
+    ap.add_argument("--runs", type=int, default=2)
+    a = ap.parse_args(argv)
+    shots = batch2d_shots(nshots=a.shots, interior=tuple(a.interior), record_s=a.record_s)
+    cells = sum(p.nx * p.ny * p.nstep for p, _, _ in shots)
+    with Batch([p for p, _, _ in shots], models=[m for _, m, _ in shots], receivers=[r for _, _, r in shots]) as b:
+        for r in range(a.runs):
+            b.run()
+            ms = b.last_run_ms()
+            print(f"run {r}: {a.shots} shots, {cells:.3e} cell-updates, {ms:.2f} ms, "
+                  f"{cells / ms / 1e6:.1f} Gcell-updates/s")
+
+
+if __name__ == "__main__":
+    _main()

@@ -67,7 +67,10 @@ __device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
   }
 }
 
-__global__ void __launch_bounds__(BNT) batch2d_kernel(BatchArgs a) {
+// 6 resident CTAs per SM (40 registers, no spills): the kernel is bound by
+// memory latency, and 48 warps per SM hide more of it than the 40 the
+// unconstrained register count (48) allows; 8 CTAs would spill.
+__global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   unsigned nbar = 0;
   for (int t = 0; t < a.max_nstep; ++t) {
