@@ -67,18 +67,38 @@ __device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
   }
 }
 
+// The current item's shot descriptor, staged in shared memory when the item
+// belongs to another shot than the CTA's previous one (shot ids are uniform
+// over the CTA). Read through a reference into global memory, every field
+// would be a global load in front of the data load it addresses, repeated
+// after each store, since a store through one of the descriptor's pointers
+// could, for all the compiler knows, change the descriptor itself.
+__device__ __forceinline__ void stage_shot(const Shot2D* shots, int id, Shot2D& sh, int& cur) {
+  static_assert(sizeof(Shot2D) % 8 == 0 && sizeof(Shot2D) / 8 <= BNT, "descriptor copy by one pass");
+  if (id == cur) return;
+  __syncthreads();  // every thread is done with the previous descriptor
+  if (threadIdx.x < sizeof(Shot2D) / 8)
+    reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
+        reinterpret_cast<const unsigned long long*>(shots + id)[threadIdx.x];
+  __syncthreads();
+  cur = id;
+}
+
 // 6 resident CTAs per SM (40 registers, no spills): the kernel is bound by
 // memory latency, and 48 warps per SM hide more of it than the 40 the
 // unconstrained register count (48) allows; 8 CTAs would spill.
 __global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ Shot2D sh;
+  int cur = -1;
   unsigned nbar = 0;
   for (int t = 0; t < a.max_nstep; ++t) {
     if (t > 0) record_batch(a, t - 1);
     const int n = a.items_at[t];
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
       const int4 itm = a.items[q];
-      const Shot2D& S = a.shots[itm.x];
+      stage_shot(a.shots, itm.x, sh, cur);
+      const Shot2D& S = sh;
       const int i = itm.y + tx, j = itm.z + ty;
       if (i < S.nx && j < S.ny) {
         if (S.het) stress2d_cell<true>(S, i, j);
@@ -88,7 +108,8 @@ __global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
     if (!grid_sync(a, nbar)) return;
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
       const int4 itm = a.items[q];
-      const Shot2D& S = a.shots[itm.x];
+      stage_shot(a.shots, itm.x, sh, cur);
+      const Shot2D& S = sh;
       const int i = itm.y + tx, j = itm.z + ty;
       if (i < S.nx && j < S.ny) {
         float ek = 0.f, ep = 0.f, vm2 = 0.f;
