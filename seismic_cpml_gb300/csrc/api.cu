@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 #include <algorithm>
 #include <tuple>
@@ -819,9 +820,16 @@ struct TuneKey {
   }
 };
 struct TuneVal { int kernel, tile_y, zchunk, depth; double ms; };
+// Shape-class cache shared by every handle of the process; handles are
+// independent and may autotune from different threads, so every access to
+// the map and to the cache file holds tune_mutex (never the trials).
 std::map<TuneKey, TuneVal>& tune_cache() {
   static std::map<TuneKey, TuneVal> c;
   return c;
+}
+std::mutex& tune_mutex() {
+  static std::mutex m;
+  return m;
 }
 TuneKey tune_key(const cpml_handle* h) {
   int mask = 0;
@@ -850,9 +858,12 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
   const TuneKey key = tune_key(h);
   TuneVal best{};
   bool have = false;
-  auto it = tune_cache().find(key);
-  if (it != tune_cache().end()) { best = it->second; have = true; }
-  if (!have && read_cache_file(cache_path, key, &best)) { tune_cache()[key] = best; have = true; }
+  {
+    std::lock_guard<std::mutex> lock(tune_mutex());
+    auto it = tune_cache().find(key);
+    if (it != tune_cache().end()) { best = it->second; have = true; }
+    if (!have && read_cache_file(cache_path, key, &best)) { tune_cache()[key] = best; have = true; }
+  }
   int st;
   if (!have) {
     // candidates: launch shapes of the one-sweep 3D kernel, and the two-sweep form
@@ -878,6 +889,7 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
       if (c.ms < best.ms) best = c;
     }
     h->p.flags = flags;
+    std::lock_guard<std::mutex> lock(tune_mutex());
     tune_cache()[key] = best;
     if (cache_path) {
       if (FILE* f = std::fopen(cache_path, "a")) {

@@ -21,6 +21,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/cpml.h"
 
@@ -650,16 +651,24 @@ int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const v
   if (M == 0 || N == 0) return CPML_OK;
   const int bn = N <= 32 ? 32 : (N <= 64 ? 64 : 128);
   if ((N + bn - 1) / bn > 65535) return CPML_ERR_RANGE;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(gemm_tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tc::Cfg<32>::SMEM) != cudaSuccess ||
-        cudaFuncSetAttribute(gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tc::Cfg<64>::SMEM) != cudaSuccess ||
-        cudaFuncSetAttribute(gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tc::Cfg<128>::SMEM) != cudaSuccess)
-      return CPML_ERR_CUDA;
-    attr = true;
+  {
+    // the dynamic shared-memory limit is a per-device function attribute:
+    // set it once for every device this process launches the GEMM on
+    static std::mutex mu;
+    static unsigned long long done = 0;  // bit d: set on device d
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPML_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!((done >> dev) & 1ull)) {
+      if (cudaFuncSetAttribute(gemm_tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               tc::Cfg<32>::SMEM) != cudaSuccess ||
+          cudaFuncSetAttribute(gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               tc::Cfg<64>::SMEM) != cudaSuccess ||
+          cudaFuncSetAttribute(gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               tc::Cfg<128>::SMEM) != cudaSuccess)
+        return CPML_ERR_CUDA;
+      done |= 1ull << dev;
+    }
   }
   int kchunk = (K + splits - 1) / splits;
   kchunk = ((kchunk + tc::BK - 1) / tc::BK) * tc::BK;

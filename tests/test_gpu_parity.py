@@ -291,6 +291,35 @@ def test_large_config_generator_at_reduced_size_vs_oracle():
     check(g, ref)
 
 
+def test_concurrent_autotune_of_two_handles_shares_one_cache(tmp_path):
+    """Handles are independent: two threads autotune two handles of one shape
+    class at once (ctypes releases the GIL in the calls), sharing the process
+    cache and one cache file; both get a valid choice and the file stays
+    well-formed."""
+    import threading
+    p, rec = P.small_3d(n=(40, 36, 36), nstep=60)
+    cache = str(tmp_path / "tune.txt")
+    res, err = [None, None], []
+
+    def work(k):
+        try:
+            with Solver(p, rec) as s:
+                res[k] = s.autotune(trial_steps=4, cache_path=cache)
+                s.run()
+        except Exception as e:   # surfaced below: a thread's exception does not propagate
+            err.append(e)
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not err, err
+    assert all(r is not None and r["kernel"] in (1, 2) and r["ms_per_step"] > 0 for r in res)
+    lines = open(cache).read().splitlines()
+    assert 1 <= len(lines) <= 2 and all(len(ln.split()) == 12 for ln in lines)
+
+
 def test_autotune_2d_times_both_kernels_and_keeps_results_exact():
     p, rec = P.small_2d(nx=1200, ny=900, nstep=60)   # 4275 tiles: both 2D kernels are candidates
     with Solver(p, rec) as s:
