@@ -68,19 +68,20 @@ __device__ __forceinline__ void record_batch(const BatchArgs& a, int t) {
 }
 
 // The current item's shot descriptor, staged in shared memory when the item
-// belongs to another shot than the CTA's previous one (shot ids are uniform
-// over the CTA). Read through a reference into global memory, every field
-// would be a global load in front of the data load it addresses, repeated
-// after each store, since a store through one of the descriptor's pointers
-// could, for all the compiler knows, change the descriptor itself.
+// belongs to another shot than the warp's previous one. Read through a
+// reference into global memory, every field would be a global load in front
+// of the data load it addresses, repeated after each store, since a store
+// through one of the descriptor's pointers could, for all the compiler
+// knows, change the descriptor itself. Each warp (one tile row) keeps its own
+// copy, so staging needs warp synchronisation only.
 __device__ __forceinline__ void stage_shot(const Shot2D* shots, int id, Shot2D& sh, int& cur) {
-  static_assert(sizeof(Shot2D) % 8 == 0 && sizeof(Shot2D) / 8 <= BNT, "descriptor copy by one pass");
+  static_assert(sizeof(Shot2D) % 8 == 0, "descriptor copied in 8-byte words");
   if (id == cur) return;
-  __syncthreads();  // every thread is done with the previous descriptor
-  if (threadIdx.x < sizeof(Shot2D) / 8)
-    reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
-        reinterpret_cast<const unsigned long long*>(shots + id)[threadIdx.x];
-  __syncthreads();
+  __syncwarp();  // every lane is done with the previous descriptor
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(shots + id);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh);
+  for (int w = threadIdx.x & 31; w < (int)(sizeof(Shot2D) / 8); w += 32) dst[w] = src[w];
+  __syncwarp();
   cur = id;
 }
 
@@ -89,7 +90,8 @@ __device__ __forceinline__ void stage_shot(const Shot2D* shots, int id, Shot2D& 
 // unconstrained register count (48) allows; 8 CTAs would spill.
 __global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  __shared__ Shot2D sh;
+  __shared__ Shot2D shw[BNT / 32];  // one descriptor copy per warp
+  Shot2D& sh = shw[ty];
   int cur = -1;
   unsigned nbar = 0;
   for (int t = 0; t < a.max_nstep; ++t) {
