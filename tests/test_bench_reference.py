@@ -1,0 +1,44 @@
+"""bench.py's reference arm runs on the host cores only (the FP64 C++
+restatement of the 3D time loop): its JSON line keeps the benchmark
+contract's keys, checked here on a one-time-step sample, and the workloads
+whose CPU figure lives inside their own line print one `unavailable` line and
+exit 0. No GPU work."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def bench_line(*args):
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    out = subprocess.run([sys.executable, "bench.py", *args], cwd=ROOT, env=env, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    return json.loads(lines[0])
+
+
+def test_reference_arm_line_keeps_the_contract():
+    d = bench_line("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample-steps", "1")
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["metric"] == d["unit"] == "Mcell-updates/s" and d["steps"] == 1 and d["n_gpus"] == 1
+    assert d["config"]["workload"] == "3d_plain_276cube" and d["config"]["grid"] == [276, 276, 276]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+@pytest.mark.parametrize("workload", ["2d_plain", "batch2d", "surrogate", "3d_large"])
+def test_reference_arm_prints_unavailable_for_other_workloads(workload):
+    d = bench_line("--impl", "reference", "--workload", workload)
+    assert d["impl"] == "reference" and isinstance(d["unavailable"], str) and d["unavailable"]
