@@ -67,7 +67,14 @@ int read_params(const char* path, Setup& S) {
     std::string num = v;                       // Fortran double literals: 2.d-3
     for (char& c : num)
       if (c == 'd' || c == 'D') c = 'e';
-    const double d = std::strtod(num.c_str(), nullptr);
+    char* end = nullptr;
+    const double d = std::strtod(num.c_str(), &end);
+    const bool logical = vu == ".TRUE." || vu == "T" || vu == ".FALSE." || vu == "F";
+    const bool numeric = end != num.c_str() && *end == '\0';
+    if (k != "SOURCE_TIME_FUNCTION" && !logical && !numeric) {   // a number or a logical, nothing else
+      std::fprintf(stderr, "%s:%d: bad value for %s: '%s'\n", path, ln, k.c_str(), v.c_str());
+      return 1;
+    }
     S.given[k] = true;
     const int iv = (vu == ".TRUE." || vu == "T") ? 1 : (vu == ".FALSE." || vu == "F") ? 0 : (int)std::lround(d);
     cpml_params& p = S.p;

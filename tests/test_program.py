@@ -24,6 +24,24 @@ def test_courant_violation_stops_like_the_reference(program, tmp_path):
     assert "time step is too large, simulation will be unstable" in r.stdout    # 2D:516
 
 
+def test_fortran_double_literals_are_read(program, tmp_path):
+    """DELTAT = 1.6d-3 is 0.0016 s (Courant 0.75: the program goes on to the
+    device, which a CPU-only run does not have, or runs to the end on a GPU),
+    not 1.6 s, which would stop on the Courant check (2D:516)."""
+    par = tmp_path / "p.par"
+    par.write_text("NX = 60\nNY = 80\nNSTEP = 40\nIT_DISPLAY = 20\nDELTAT = 1.6d-3\n")
+    r = subprocess.run([program, "2d", str(par), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode != 3 and "too large" not in r.stdout, r.stdout
+    assert r.returncode in (0, 4), r.stdout + r.stderr
+
+
+def test_non_numeric_value_is_rejected(program, tmp_path):
+    par = tmp_path / "p.par"
+    par.write_text("NX = sixty\n")
+    r = subprocess.run([program, "2d", str(par), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 2 and "bad value for NX" in r.stderr
+
+
 def test_unknown_parameter_is_rejected(program, tmp_path):
     par = tmp_path / "p.par"
     par.write_text("NXX = 60\n")
