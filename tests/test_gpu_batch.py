@@ -4,7 +4,6 @@ handle (same per-cell arithmetic), and matches the FP64 oracle."""
 import numpy as np
 import pytest
 
-from seismic_cpml_gb300 import params as P
 from seismic_cpml_gb300.batch import Batch
 from seismic_cpml_gb300.solver import Solver
 from seismic_cpml_gb300.workloads import batch2d_shots

@@ -282,7 +282,6 @@ def test_large_config_generator_at_reduced_size_vs_oracle():
     """The 820^3 heterogeneous workload's parameters and model generator at
     140^3 (120^3 interior, same DELTA, DELTAT, source, receiver-grid layout):
     traces and energy against the FP64 oracle."""
-    import torch
     from seismic_cpml_gb300.earth import layered_model_3d_device
     p, rec = P.config_3d_large(n_interior=120, nstep=150, nrec_side=11)
     lam, mu, rho = (t.cpu().numpy() for t in layered_model_3d_device((p.nz, p.ny, p.nx), radius=(3.0, 12.0)))

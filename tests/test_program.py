@@ -1,7 +1,6 @@
 """cpml_program, the C++ host program that replaces the reference programs'
 main units: parameter file with the Fortran names, stop conditions, and the
 reference's output files."""
-import os
 import subprocess
 
 import numpy as np
