@@ -21,11 +21,12 @@ metric: Mcell-updates/s (cells x time steps / s), higher is better.
           every C-PML memory variable read and written where its a != 0)
           / average launch duration over the timed region.
   cpu_baseline: the FP64 C++ restatement of the reference time loop with
-          OpenMP on every host core, on a bounded sample of the same grid.
+          OpenMP on every host core, on a bounded sample of the same grid:
+          as many time steps as take about 10 s (and the same on one thread).
 
 --impl reference times that CPU restatement alone (the reference is Fortran
 and no Fortran compiler exists on either machine), on the same config and
-metric, each step a bounded sample of time steps.
+metric, each step a bounded sample of 40 time steps (about 2.5 s on 16 cores).
 
 Multi-GPU: the path has no exchange step in this build (one domain per GPU);
 N ranks run N independent replicas of the workload ("replicas only").
@@ -56,7 +57,8 @@ def parse():
     ap.add_argument("--nstep", type=int, default=None, help="time steps per bench step")
     ap.add_argument("--tuning", type=str, default=None, help="kernel,tile_y,zchunk,depth (skips autotune)")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--cpu-sample-steps", type=int, default=None)
+    ap.add_argument("--cpu-sample-steps", type=int, default=None,
+                    help="time steps per CPU sample (default: about 10 s of work; the reference arm: 40)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", choices=["3d_plain", "3d_large", "2d_plain", "batch2d", "surrogate"],
@@ -176,16 +178,25 @@ def n_chunks(nstep, it_display):
     return n
 
 
-def cpu_baseline(p, sample_steps, nthreads):
+def cpu_baseline(p, nthreads, sample_steps=None, target_s=10.0, max_steps=400):
+    """The FP64 C++ restatement of the time loop on `nthreads` host threads:
+    `sample_steps` timed time steps, or by default as many as take about
+    `target_s` seconds (estimated from two timed steps, at most `max_steps`).
+    Returns (Mcell-updates/s, seconds, time steps)."""
     from oracle import oracle_c
     sess = oracle_c.Session(p, nthreads=nthreads)
     sess.run(1)  # touch every page once
+    if sample_steps is None:
+        t = time.perf_counter()
+        sess.run(2)
+        per_step = max((time.perf_counter() - t) / 2, 1e-6)
+        sample_steps = int(min(max_steps, max(2, -(-target_s // per_step))))
     t = time.perf_counter()
     sess.run(sample_steps)
     dt = time.perf_counter() - t
     sess.close()
     ncell = p.nx * p.ny * p.nz
-    return ncell * sample_steps / dt / 1e6, dt
+    return ncell * sample_steps / dt / 1e6, dt, sample_steps
 
 
 # ---------------------------------------------------------------------------
@@ -195,7 +206,7 @@ def run_reference(args, world, rank, pg):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    sample = args.cpu_sample_steps or 10
+    sample = args.cpu_sample_steps or 40
     from oracle import oracle_c
     sess = oracle_c.Session(p, nthreads=cores)
     sess.run(1)
@@ -325,13 +336,12 @@ def run_ours(args, world, rank, local, pg):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and model is None:
         cores = os.cpu_count() or 1
-        sample = args.cpu_sample_steps or 12
-        v, dt = cpu_baseline(p, sample, cores)
-        v1, dt1 = cpu_baseline(p, 2, 1)
+        v, dt, n = cpu_baseline(p, cores, args.cpu_sample_steps)
+        v1, dt1, n1 = cpu_baseline(p, 1, 2 if args.cpu_sample_steps else None)
         cpu = {"value": round(v, 3), "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
-               "sample": f"{sample} time steps of the 276^3 grid ({dt:.1f} s), FP64 C++ "
+               "sample": f"{n} time steps of the 276^3 grid ({dt:.1f} s), FP64 C++ "
                          "restatement of the reference time loop, OpenMP",
-               "value_1core": round(v1, 3), "sample_1core": f"2 time steps on one thread ({dt1:.1f} s)"}
+               "value_1core": round(v1, 3), "sample_1core": f"{n1} time steps on one thread ({dt1:.1f} s)"}
 
     chunks = n_chunks(p.nstep, p.it_display)
     line = {

@@ -42,3 +42,18 @@ def test_reference_arm_line_keeps_the_contract():
 def test_reference_arm_prints_unavailable_for_other_workloads(workload):
     d = bench_line("--impl", "reference", "--workload", workload)
     assert d["impl"] == "reference" and isinstance(d["unavailable"], str) and d["unavailable"]
+
+
+def test_cpu_baseline_sample_is_sized_by_time():
+    """The GPU line's cpu_baseline helper: without a step count it times as
+    many steps as take about target_s (at least 2, at most max_steps); with
+    one it times exactly that many."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from seismic_cpml_gb300 import params as P
+    p, _ = P.small_3d(n=(40, 36, 32), nstep=500)
+    v, dt, n = bench.cpu_baseline(p, 2, target_s=0.3, max_steps=300)
+    assert 2 <= n <= 300 and dt > 0 and v > 0
+    assert dt < 3.0                       # about target_s, not the cap
+    v2, dt2, n2 = bench.cpu_baseline(p, 1, sample_steps=3)
+    assert n2 == 3 and v2 > 0
