@@ -151,7 +151,9 @@ int cpml_reset(cpml_handle* h);
 
 /* Advance nsteps time steps of the reference time loop (2D:550-735,
    3D:802-1245): stress + C-PML, velocity + C-PML, source, Dirichlet edges,
-   receivers, energy, and the max|v| check every it_display steps. */
+   receivers, energy, and the max|v| check every it_display steps.
+   CPML_ERR_NOT_READY when the handle's last re-plan (cpml_set_model or
+   cpml_set_tuning) failed part-way; a later successful one restores it. */
 int cpml_run(cpml_handle* h, int nsteps);
 
 /* Steps done so far and the last max|v| computed (2D:718, 3D:1185). */

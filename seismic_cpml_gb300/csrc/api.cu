@@ -78,6 +78,7 @@ struct cpml_handle {
   float* fld[9] = {};      // buffer set 0
   float* fld1[9] = {};     // buffer set 1 (fused 3D path: time n+1 while set 0 holds n)
   bool pingpong = false;   // fields alternate between the sets every step
+  bool plan_ok = false;    // the last re-plan (configure_path) completed; cpml_run needs it
   bool persist = false;    // 2D: one cooperative launch per chunk of steps
   int persist_grid = 0;    // its CTAs
   unsigned* bar = nullptr; // its grid-barrier words
@@ -418,7 +419,7 @@ int upload_receivers(cpml_handle* h) {
 // Choose the step kernel and (re)build what it needs: the fused one-sweep 3D
 // kernel ping-pongs two buffer sets and reads them through TMA tensor maps;
 // the two-sweep kernels update one set in place.
-int configure_path(cpml_handle* h) {
+int configure_path_impl(cpml_handle* h) {
   const bool fused = h->ndim == 3 && h->kernel != CPML_KERNEL_TWO_SWEEP && fused3d_supported();
   if (h->ndim == 3 && h->kernel == CPML_KERNEL_FUSED && !fused) return CPML_ERR_CUDA;
   int st;
@@ -435,10 +436,15 @@ int configure_path(cpml_handle* h) {
     int n_cls[4] = {0, 0, 0, 0};
     fused3d_items(h->nx, h->ny, h->nz, h->axes[0], h->axes[1], h->axes[2], h->p.npoints_pml, h->tile_y,
                   h->zchunk, h->het, fast, gen, n_cls);
+    // both new lists exist before either old one is released
+    int4 *dfast = nullptr, *dgen = nullptr;
+    if ((st = dalloc(h, &dfast, fast.size()))) return st;
+    if ((st = dalloc(h, &dgen, gen.size()))) { dfree(h, dfast); return st; }
     drop_graphs(h);  // cached graphs launch with the item lists about to be replaced
-    if ((st = drealloc(h, &h->items_fast, fast.size()))) return st;
-    if ((st = drealloc(h, &h->items_gen, gen.size()))) return st;
-    int4 *dfast = h->items_fast, *dgen = h->items_gen;
+    dfree(h, h->items_fast);
+    dfree(h, h->items_gen);
+    h->items_fast = dfast;
+    h->items_gen = dgen;
     if (!fast.empty())
       CK(cudaMemcpy(dfast, fast.data(), sizeof(int4) * fast.size(), cudaMemcpyHostToDevice));
     if (!gen.empty())
@@ -480,6 +486,15 @@ int configure_path(cpml_handle* h) {
   }
   drop_graphs(h);
   return CPML_OK;
+}
+
+// A re-plan that fails part-way leaves the handle's plan, item lists and
+// partials out of step with one another: cpml_run refuses such a handle
+// (CPML_ERR_NOT_READY) until a later re-plan succeeds.
+int configure_path(cpml_handle* h) {
+  const int st = configure_path_impl(h);
+  h->plan_ok = st == CPML_OK;
+  return st;
 }
 
 // Buffer set that holds the current time level.
@@ -599,14 +614,26 @@ int cpml_set_receivers(cpml_handle* h, int nrec, const int* ix, const int* iy, c
   if (h->it != 0) return CPML_ERR_INVALID;  // set receivers before running (or after reset)
   int st;
   if (nrec > std::max(h->nrec, 1)) {
+    // both new buffers exist before either old one is released, so a failed
+    // call leaves the previous receivers intact
+    int* cells = nullptr;
+    float* seis = nullptr;
+    if ((st = dalloc(h, &cells, size_t(nrec)))) return st;
+    if ((st = dalloc(h, &seis, size_t(3) * nrec * h->p.nstep))) { dfree(h, cells); return st; }
     drop_graphs(h);
-    if ((st = drealloc(h, &h->rec_cell, size_t(nrec)))) return st;
-    if ((st = drealloc(h, &h->seis, size_t(3) * nrec * h->p.nstep))) return st;
+    dfree(h, h->rec_cell);
+    dfree(h, h->seis);
+    h->rec_cell = cells;
+    h->seis = seis;
   }
   h->nrec = nrec;
   h->rec_ijk = ijk;
   drop_graphs(h);
-  if ((st = upload_receivers(h))) return st;
+  if ((st = upload_receivers(h))) {  // never leave indices on the device that were not uploaded
+    h->nrec = 0;
+    h->rec_ijk.clear();
+    return st;
+  }
   CK(cudaMemsetAsync(h->seis, 0, sizeof(float) * 3 * size_t(std::max(nrec, 1)) * h->p.nstep, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return CPML_OK;
@@ -619,6 +646,7 @@ int cpml_reset(cpml_handle* h) {
 
 int cpml_run(cpml_handle* h, int nsteps) {
   if (!h || nsteps < 0) return CPML_ERR_INVALID;
+  if (!h->plan_ok) return CPML_ERR_NOT_READY;
   if (h->it + nsteps > h->p.nstep) return CPML_ERR_RANGE;
   const bool check = !(h->p.flags & CPML_FLAG_NO_STABILITY);
   const int d = h->p.it_display;
