@@ -146,7 +146,8 @@ int cpml_set_model(cpml_handle* h, const float* lambda, const float* mu,
 int cpml_set_receivers(cpml_handle* h, int nrec, const int* ix, const int* iy,
                        const int* iz);
 
-/* Zero fields, memory variables, seismograms and energy; set it = 0. */
+/* Zero fields, memory variables, seismograms and energy; set it = 0 (the
+   reference's initialisation, 2D:521-544, 3D:719-757). */
 int cpml_reset(cpml_handle* h);
 
 /* Advance nsteps time steps of the reference time loop (2D:550-735,
@@ -157,6 +158,8 @@ int cpml_reset(cpml_handle* h);
 int cpml_run(cpml_handle* h, int nsteps);
 
 /* Steps done so far and the last max|v| computed (2D:718, 3D:1185). */
+/* Time steps done so far, and max |v| at the last display step (what the
+   progress print-out shows, 2D:716-723, 3D:1183-1192). */
 int cpml_status(cpml_handle* h, int* it, double* vmax);
 
 /* Seismograms recorded so far, [nrec][nstep] doubles (sisvx/sisvy,
@@ -167,7 +170,8 @@ int cpml_get_seismograms(cpml_handle* h, double* vx, double* vy, double* vz);
    3D:1131-1180; the 3D reference writes only ek+ep). Either may be NULL. */
 int cpml_get_energy(cpml_handle* h, double* ek, double* ep);
 
-/* Copy one whole field to host FP32, [k][j][i] with nx*ny*nz values. */
+/* Copy one whole field to host FP32, [k][j][i] with nx*ny*nz values. No
+   reference counterpart: the reference keeps its arrays inside the program. */
 int cpml_get_field(cpml_handle* h, int field, float* out);
 
 /* Copy one plane of a field: axis 0/1/2 = plane of constant i/j/k, index
@@ -175,16 +179,18 @@ int cpml_get_field(cpml_handle* h, int field, float* out);
    Used for the snapshots of 2D:729-732 and 3D:1236-1239 (k = NZ/2). */
 int cpml_get_plane(cpml_handle* h, int field, int axis, int index, float* out);
 
-/* Upload a whole field from host FP32 (tests and restarts). */
+/* Upload a whole field from host FP32 (tests and restarts). No reference
+   counterpart. */
 int cpml_set_field(cpml_handle* h, int field, const float* in);
 
 /* Bytes the hot path moves per time step by its compulsory count: every
    wavefield read and written once, per-cell model read once, each C-PML
-   memory variable read and written once where its coefficient a is nonzero. */
+   memory variable read and written once where its coefficient a is nonzero.
+   For roofline figures; no reference counterpart. */
 double cpml_algorithmic_bytes_per_step(cpml_handle* h);
 
 /* Milliseconds of device time of the last cpml_run (CUDA events recorded on
-   the handle's stream around it). */
+   the handle's stream around it). No reference counterpart. */
 int cpml_last_run_ms(cpml_handle* h, double* ms);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
@@ -283,7 +289,8 @@ int cpml_nn_gemm(int M, int N, int K, const void* A, int lda, int ta, const void
                  float* Cf, void* Cb, int ldc, const float* bias, int relu, int accum, float alpha,
                  int splits, float* work, long long work_elems, void* stream);
 /* The same contract as cpml_nn_gemm on the 5th-generation tensor cores
-   (tcgen05.mma, accumulator in tensor memory, 128 x 128 output tiles). */
+   (tcgen05.mma, accumulator in tensor memory; 128-row output tiles 32, 64 or
+   128 columns wide, the narrowest that covers N). */
 int cpml_nn_gemm_tc(int M, int N, int K, const void* A, int lda, int ta, const void* B, int ldb, int tb,
                     float* Cf, void* Cb, int ldc, const float* bias, int relu, int accum, float alpha,
                     int splits, float* work, long long work_elems, void* stream);
