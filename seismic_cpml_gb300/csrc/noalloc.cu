@@ -18,7 +18,9 @@
 // therefore come before any stream capture. Every call on a device uses the
 // same array: calls whose kernels overlap on the GPU race on it, so callers
 // must order them (one stream, or events). Each call writes every plane
-// slot it later reads, so nothing has to be cleared between calls.
+// slot it later reads, so nothing has to be cleared between calls. The
+// cached address belongs to the device's current context: a device or
+// context reset (cudaDeviceReset) between calls is not supported.
 #include <cuda_runtime.h>
 #include <mutex>
 
@@ -50,8 +52,8 @@ plane_energy_kernel(const float* __restrict__ vx, const float* __restrict__ vy,
                     const float* __restrict__ rho_c, int ep_physical, double* __restrict__ part) {
   const int k = blockIdx.x;
   cpml::Kahan ek, ep;
-  if (k >= npml && k < nz - npml) {
-    const int w = nx - 2 * npml, h = ny - 2 * npml;
+  const int w = nx - 2 * npml, h = ny - 2 * npml;
+  if (k >= npml && k < nz - npml && w > 0 && h > 0) {
     for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
       const int i = npml + q % w, j = npml + q / w;
       const long long c = ((long long)k * ny + j) * pitch + i;
@@ -121,6 +123,8 @@ extern "C" int cpml_energy3d_noalloc(const float* const* fields, int nx, int ny,
                                      const float* rho_cell, int flags, double* out,
                                      void* stream) {
   if (!fields || !out || nx < 1 || ny < 1 || nz < 1 || pitch < nx || npml < 0) return CPML_ERR_INVALID;
+  // the energy interior [npml, n - npml) must hold at least one cell on every axis
+  if (2 * npml >= nx || 2 * npml >= ny || 2 * npml >= nz) return CPML_ERR_INVALID;
   for (int f = 0; f < 9; ++f)
     if (!fields[f]) return CPML_ERR_INVALID;
   if ((lam_cell || mu_cell || rho_cell) && !(lam_cell && mu_cell && rho_cell)) return CPML_ERR_INVALID;
