@@ -259,6 +259,13 @@ def run_ours(args, world, rank, local, pg):
     ncell = p.nx * p.ny * p.nz
 
     s = Solver(p, rec, model=model, tuning=tuning)
+    if s.tuning()[0] != 2 and (tuning is None or tuning[0] != 1):
+        # the fused one-sweep step needs the driver's tensor-map encoder; a
+        # handle without it runs the two-sweep kernels (108 instead of 72 B
+        # per cell), which is not the path this line describes
+        s.close()
+        raise SystemExit("bench.py: the fused 3D step is unavailable on this device; "
+                         "the handle fell back to the two-sweep kernels")
     tune = None
     if tuning is None and not args.no_autotune:
         tune = s.autotune(trial_steps=20)        # outside the timed region

@@ -733,13 +733,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapFloatOOBfill);
 
 // Resolved once per process (a function-local static's initialisation is
-// thread-safe); nullptr when the driver has no tensor-map encoder.
+// thread-safe) through the runtime's versioned driver entry-point query, at
+// the ABI of CUDA 12.0 where cuTensorMapEncodeTiled first appeared; nullptr
+// when the driver has no tensor-map encoder.
 static EncodeTiledFn encode_fn() {
   static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess && p)
       return reinterpret_cast<EncodeTiledFn>(p);
     cudaGetLastError();
     return nullptr;

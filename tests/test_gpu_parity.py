@@ -186,6 +186,67 @@ def test_3d_mid_size_vs_oracle(tuning):
     check(run_gpu(p, rec, tuning=tuning), ref)
 
 
+INTERIOR_TUNINGS = [(2, 8, 16, 2), (2, 8, 48, 2), (2, 16, 24, 2), (2, 16, 64, 2)]
+
+
+@pytest.mark.parametrize("tuning", INTERIOR_TUNINGS, ids=["f8z16", "f8z48", "f16z24", "f16z64"])
+def test_3d_interior_class_vs_oracle(tuning):
+    """The lean interior kernel (homogeneous model: the class and the model
+    the 3D plain workload runs) against the FP64 oracle. At 108 x 100 x 96
+    with a 10-point C-PML the grid has interior tiles in x, y and z, so all
+    five step kernels launch (interior + X, Y, Z and mixed general classes);
+    the source and a receiver line lie inside interior tiles. 400 steps, the
+    wave crosses the grid and leaves through the C-PML (3D:836-1180)."""
+    p, _ = P.small_3d(n=(108, 100, 96), nstep=400)
+    p.npoints_pml = 10
+    c = (p.nx // 2, p.ny // 2 + 1, p.nz // 2)
+    rec = [(i, c[1], c[2]) for i in range(12, p.nx - 10, 7)] + \
+          [(c[0], j, c[2] + 3) for j in range(14, p.ny - 10, 9)] + [(7, 8, 9), (p.nx - 7, p.ny - 6, c[2] + 2)]
+    ref = oracle_c.run(p, rec=rec, keep_fields=True)
+    ref32 = oracle_c.run(p, rec=rec, keep_fields=True, double=False)
+    with Solver(p, rec, tuning=tuning) as s:
+        assert s.tuning()[0] == 2
+        assert s.launches_per_step()[0] == 5, s.launches_per_step()   # interior items exist
+        s.run()
+        vx, vy, vz = s.seismograms()
+        ek, ep = s.energy()
+        fields = {n: s.field(n) for n in ref.fields}
+    g = dict(vx=vx, vy=vy, vz=vz, ek=ek, ep=ep, fields=fields)
+    et, ee = check(g, ref, ref.fields, ref32.fields)
+    print(f"interior class {tuning}: trace rel-L2 {et:.3e}, energy rel-L2 {ee:.3e}")
+
+
+@pytest.mark.parametrize("tuning", [None, (2, 8, 48, 2), (2, 16, 32, 2)], ids=["auto", "f8z48", "f16z32"])
+def test_3d_plain_config_full_size_vs_fixture(golden, tuning):
+    """The 3D plain workload itself (276^3, 2500 steps, 64 receivers: what the
+    benchmark times) against the FP64 oracle's run of the same parameters
+    (tests/golden/config_3d_plain.npz): traces within 1e-5 and the energy
+    curve within 1e-6 relative L2 after every one of the 2500 steps."""
+    g0 = golden("config_3d_plain")
+    p, rec = P.config_3d_plain()
+    assert [tuple(r) for r in g0["rec"]] == [tuple(r) for r in rec]
+    with Solver(p, rec, tuning=tuning) as s:
+        assert s.tuning()[0] == 2                                    # the fused one-sweep step
+        assert s.launches_per_step()[0] == 5, s.launches_per_step()
+        s.run()
+        vx, vy, vz = s.seismograms()
+        ek, ep = s.energy()
+
+    class R:
+        sisvx, sisvy, sisvz, ek, ep = g0["sisvx"], g0["sisvy"], g0["sisvz"], g0["ek"], g0["ep"]
+    et, ee = check(dict(vx=vx, vy=vy, vz=vz, ek=ek, ep=ep), R)
+    print(f"3d_plain full size {tuning}: trace rel-L2 {et:.3e}, energy rel-L2 {ee:.3e}")
+
+
+def test_fused_is_the_default_3d_step():
+    """The fused step must be available (its tensor-map encoder found through
+    the runtime's versioned driver entry point): a 3D handle that silently took
+    the two-sweep kernels would move 108 instead of 72 B per cell."""
+    p, rec = P.small_3d()
+    with Solver(p, rec) as s:
+        assert s.tuning()[0] == 2
+
+
 def test_fused_equals_two_sweep_traces():
     """Both 3D step kernels agree with each other to FP32 rounding."""
     p, rec = P.small_3d(n=(40, 36, 30), nstep=150)
