@@ -55,6 +55,12 @@ extern "C" {
                                         reference's duplicated eps_yy*sigma_yy term (3D:1170-1171) */
 #define CPML_FLAG_NO_STABILITY  0x4  /* skip the max|v| blow-up check at IT_DISPLAY cadence      */
 
+/* ---- absorbing-layer schemes (cpml_params.scheme) ---------------------- */
+#define CPML_SCHEME_CPML     0   /* convolutional PML, memory variables (the default) */
+#define CPML_SCHEME_SPLIT    1   /* 2D only: classical split-field PML of Collino and
+                                    Tsogka (seismic_PML_Collino_2D_isotropic.f90),
+                                    homogeneous model, DELTAX = DELTAY, second order */
+
 /* ---- step kernels (cpml_set_tuning) ----------------------------------- */
 #define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: persistent when the
                                      grid has more 32 x 8 tiles than the GPU holds
@@ -90,7 +96,12 @@ typedef struct cpml_params {
   int32_t stf;           /* CPML_STF_*                                         */
   int32_t it_display;    /* IT_DISPLAY: cadence of the max|v| stability check */
   int32_t flags;         /* CPML_FLAG_*                                        */
-  int32_t reserved_i[4];
+  int32_t order;         /* spatial operator, 2D C-PML only: 0 or 2 = second
+                            order (2D program); 4 = fourth order with the
+                            27/24 staggered stencil (seismic_CPML_2D_isotropic_
+                            fourth_order.f90:565-637)                         */
+  int32_t scheme;        /* CPML_SCHEME_*                                      */
+  int32_t reserved_i[2];
   double deltax, deltay, deltaz;  /* DELTAX, DELTAY, DELTAZ (m)               */
   double deltat;                  /* DELTAT (s)                               */
   double cp, cs, rho;    /* homogeneous model; cp also sets the PML d0 (2D:296) */
@@ -107,6 +118,13 @@ typedef struct cpml_handle cpml_handle;
 
 /* Fill *p with the reference 2D program's parameter block (2D:138-218). */
 int cpml_params_default_2d(cpml_params* p);
+/* Fill *p with the parameter block of seismic_CPML_2D_isotropic_fourth_
+   order.f90:132-190 (order 4, DELTAT halved and NSTEP and IT_DISPLAY doubled
+   with respect to the second-order program). */
+int cpml_params_default_2d_fourth(cpml_params* p);
+/* Fill *p with the parameter block of seismic_PML_Collino_2D_isotropic.f90:
+   96-141 (scheme CPML_SCHEME_SPLIT; h = DELTAX = DELTAY = 10 m). */
+int cpml_params_default_2d_split(cpml_params* p);
 /* Fill *p with the reference 3D program's parameter block (3D:124-218),
    single-domain semantics: source and receivers on global plane k = NZ/2. */
 int cpml_params_default_3d(cpml_params* p);
@@ -122,7 +140,11 @@ int cpml_nearest_gridpoint(int nx, int ny, double deltax, double deltay,
 /* Build the 1-D C-PML profiles of one axis in FP64 on the host
    (2D:283-394 for x, 2D:396-465 for y, 3D:560-667 for z). Outputs are arrays
    of length n: d, K, alpha, a, b at grid points and at half points.
-   Exposed so callers and tests can inspect what the device kernels use. */
+   Exposed so callers and tests can inspect what the device kernels use.
+   Fourth order: the y axis's high-side origin is NY*DELTAY - thickness
+   (2D4:401). CPML_SCHEME_SPLIT: d and d_half receive the split-field damping
+   divided by two (seismic_PML_Collino_2D_isotropic.f90:180-250); K = 1,
+   alpha = a = 0 and b = 1. */
 int cpml_pml_profile(const cpml_params* p, int axis, int n,
                      double* d, double* K, double* alpha, double* a, double* b,
                      double* d_half, double* K_half, double* alpha_half,
@@ -182,6 +204,26 @@ int cpml_get_plane(cpml_handle* h, int field, int axis, int index, float* out);
 /* Upload a whole field from host FP32 (tests and restarts). No reference
    counterpart. */
 int cpml_set_field(cpml_handle* h, int field, const float* in);
+
+/* Checkpoint / restart. The state a restart of the reference's time loop
+   needs (3D:720-756, 2D:522-544 initialise it): the step counter it, the
+   wavefields, every C-PML memory variable, and what has been recorded so far
+   (seismograms, kinetic and potential energy, max|v| and the non-finite
+   flags of steps 1..it). No reference counterpart: the reference programs
+   run from it = 1 to NSTEP in one execution.
+   cpml_state_size: bytes of a snapshot at the handle's current step.
+   cpml_save_state: write the snapshot to caller-owned host memory (at least
+     cpml_state_size bytes; CPML_ERR_RANGE if smaller).
+   cpml_load_state: restore a snapshot into a handle created from the same
+     parameter block, with the same per-cell model (cpml_set_model) and the
+     same receivers (cpml_set_receivers) applied first; CPML_ERR_INVALID if
+     the snapshot's grid, parameters, model or receivers differ. The step
+     kernel may differ. Continuing the run gives bit for bit the results of
+     the uninterrupted run. The format is this library's own (native byte
+     order, a versioned header), not a portable file format. */
+int cpml_state_size(cpml_handle* h, size_t* bytes);
+int cpml_save_state(cpml_handle* h, void* buf, size_t bytes);
+int cpml_load_state(cpml_handle* h, const void* buf, size_t bytes);
 
 /* Bytes the hot path moves per time step by its compulsory count: every
    wavefield read and written once, per-cell model read once, each C-PML
@@ -258,15 +300,18 @@ void cpml_batch_destroy(cpml_batch* b);
    a fixed memory budget, where cudaMalloc would synchronise or fail).
      fields: 9 device pointers vx vy vz sxx syy szz sxy sxz syz, each
              [nz][ny][pitch] floats (pitch >= nx, in floats);
-     npml:   interior = [npml, n - npml) on every axis;
+     npml:   interior = [npml, n - npml) on every axis (CPML_ERR_INVALID
+             unless 2*npml < nx, ny and nz);
      lam/mu/rho: homogeneous model, used when the three *_cell device arrays
              (same layout as the fields) are NULL;
      flags:  CPML_FLAG_EP_PHYSICAL selects the textbook Ep;
      out:    device pointer to 2 doubles (Ek, Ep), written on `stream`.
    Scratch is a static device array of per-plane sums for at most 8192 planes
    (nz > 8192 returns CPML_ERR_RANGE). Its address is looked up on a device's
-   first call, so make that call before any stream capture. All calls share
-   that array: calls that overlap on the GPU race, so order them. */
+   first call, so make that call before any stream capture; the address is
+   kept for the life of the process, so a device or context reset between
+   calls is not supported. All calls share that array: calls that overlap
+   on the GPU race, so order them. */
 int cpml_energy3d_noalloc(const float* const* fields, int nx, int ny, int nz, int pitch,
                           int npml, double lam, double mu, double rho,
                           const float* lam_cell, const float* mu_cell,
@@ -332,6 +377,16 @@ int cpml_nn_adam(float* w, void* wb, const float* g, float* m, float* v, long lo
    "t v" line per step in Fortran list-directed REAL(4) style (2D:820-854). */
 int cpml_write_seismograms(const char* dir, const double* vx, const double* vy,
                            const double* vz, int nt, int nrec, double deltat);
+
+/* Binary receiver output for large receiver sets: seisVx.su, seisVy.su (and
+   seisVz.su if vz != NULL), the Seismic Unix layout the reference's
+   seismic_ADEPML_2D_elastic_RK4_eighth_order.f90:985-1004 writes with
+   access='stream': per receiver a 240-byte header of 120 native-order int16
+   words, all zero except word 58 = nt and word 59 = trunc(deltat*1e6)
+   (microseconds), then nt REAL(4) samples. vx/vy/vz are [nrec][nt].
+   CPML_ERR_RANGE when nt or the interval in microseconds exceeds 32767. */
+int cpml_write_seismograms_su(const char* dir, const double* vx, const double* vy,
+                              const double* vz, int nt, int nrec, double deltat);
 
 /* energy.dat: 2D writes t, Ek, Ep, Ek+Ep (2D:741-746); 3D writes t, Ek+Ep
    (3D:1253-1257). ncol selects 4 or 2. */

@@ -7,6 +7,8 @@
 //
 // It follows, loop nest by loop nest and in the reference's operation order:
 //   seismic_CPML_2D_isotropic_second_order.f90   2D:283-744
+//   seismic_CPML_2D_isotropic_fourth_order.f90   2D4:325-745 (order = 4)
+//   seismic_PML_Collino_2D_isotropic.f90         PML:180-533 (scheme = split)
 //   seismic_CPML_3D_isotropic_MPI_OpenMP.f90     3D:399-1180
 // with full-grid memory arrays as in the reference (2D:221-230, 3D:228-247)
 // and OpenMP over the outer loop index as in 3D:825. The 3D program is
@@ -45,7 +47,11 @@ struct Profile {
 };
 
 // 2D:283-394 (x), 2D:396-465 (y), 3D:560-667 (z)
+// The fourth-order program puts the high-side origin of the y profile one
+// cell further out: yorigintop = NY*DELTAY - thickness (2D4:401) where the
+// second-order program has (NY-1)*DELTAY (2D:400).
 Profile build_profile(const cpml_params* p, int axis, int n, double delta) {
+  const bool top_shift = p->ndim == 2 && p->order == 4 && axis == 1;
   Profile P;
   P.d.assign(n, 0.0); P.dh.assign(n, 0.0);
   P.K.assign(n, 1.0); P.Kh.assign(n, 1.0);
@@ -60,7 +66,7 @@ Profile build_profile(const cpml_params* p, int axis, int n, double delta) {
   const double thickness = p->npoints_pml * delta;
   const double d0 = -(npower + 1) * p->cp * std::log(p->rcoef) / (2.0 * thickness);
   const double oleft = thickness;
-  const double oright = (n - 1) * delta - thickness;
+  const double oright = (top_shift ? n : n - 1) * delta - thickness;
   for (int i = 1; i <= n; ++i) {
     const double val = delta * double(i - 1);
     const int ii = i - 1;
@@ -171,6 +177,8 @@ struct State2D {
   }
   size_t at(int i, int j) const { return size_t(j - 1) * NX + (i - 1); }  // 1-based
   void step(int it, const Out& o);
+  void step4(int it, const Out& o);
+  void advance(int it, const Out& o) { if (p->order == 4) step4(it, o); else step(it, o); }
   void fields(double* out) const {
     const std::vector<R>* F[5] = {&vx, &vy, &sxx, &syy, &sxy};
     for (int f = 0; f < 5; ++f)
@@ -286,11 +294,281 @@ void State2D<R>::step(int it, const Out& o) {
     }
   }
 
+// one pass of the fourth-order program's time loop (2D4:553-745): the same
+// sweeps with the 27/24 staggered operator, arrays 0:NX+1 x 0:NY+1 whose
+// ghost layer is never written (zero), dvx_dy corrected with K_y rather than
+// K_y_half (2D4:596), and the energy over [NPML, N-NPML+1] (2D4:696-712)
+template <typename R>
+void State2D<R>::step4(int it, const Out& o) {
+    auto G = [&](const std::vector<R>& v, int i, int j) -> R {
+      return (i < 1 || i > NX || j < 1 || j > NY) ? R(0) : v[at(i, j)];
+    };
+    const R c27 = R(27.0), dx24 = R(24.0) * DX, dy24 = R(24.0) * DY;
+    // 27/24 difference of a staggered pair: (27 f(p1) - 27 f(p0) - f(p2) + f(m1)) / (24 h)
+    auto D = [&](R p1, R p0, R p2, R m1, R h24) { return (c27 * p1 - c27 * p0 - p2 + m1) / h24; };
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j);
+        R lam_hx = R(0.5) * (lam[at(i + 1, j)] + lam[c]);
+        R mu_hx = R(0.5) * (mu[at(i + 1, j)] + mu[c]);
+        R l2m = lam_hx + R(2.0) * mu_hx;
+        R dvx_dx = D(G(vx, i + 1, j), G(vx, i, j), G(vx, i + 2, j), G(vx, i - 1, j), dx24);
+        R dvy_dy = D(G(vy, i, j), G(vy, i, j - 1), G(vy, i, j + 1), G(vy, i, j - 2), dy24);
+        m_dvx_dx[c] = X.bh[i - 1] * m_dvx_dx[c] + X.ah[i - 1] * dvx_dx;
+        m_dvy_dy[c] = Y.b[j - 1] * m_dvy_dy[c] + Y.a[j - 1] * dvy_dy;
+        dvx_dx = dvx_dx / X.Kh[i - 1] + m_dvx_dx[c];
+        dvy_dy = dvy_dy / Y.K[j - 1] + m_dvy_dy[c];
+        sxx[c] = sxx[c] + (l2m * dvx_dx + lam_hx * dvy_dy) * DT;
+        syy[c] = syy[c] + (lam_hx * dvx_dx + l2m * dvy_dy) * DT;
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j);
+        R mu_hy = R(0.5) * (mu[at(i, j + 1)] + mu[c]);
+        R dvy_dx = D(G(vy, i, j), G(vy, i - 1, j), G(vy, i + 1, j), G(vy, i - 2, j), dx24);
+        R dvx_dy = D(G(vx, i, j + 1), G(vx, i, j), G(vx, i, j + 2), G(vx, i, j - 1), dy24);
+        m_dvy_dx[c] = X.b[i - 1] * m_dvy_dx[c] + X.a[i - 1] * dvy_dx;
+        m_dvx_dy[c] = Y.bh[j - 1] * m_dvx_dy[c] + Y.ah[j - 1] * dvx_dy;
+        dvy_dx = dvy_dx / X.K[i - 1] + m_dvy_dx[c];
+        dvx_dy = dvx_dy / Y.K[j - 1] + m_dvx_dy[c];   // K_y, as 2D4:596 has it
+        sxy[c] = sxy[c] + mu_hy * (dvy_dx + dvx_dy) * DT;
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j);
+        R d1 = D(G(sxx, i, j), G(sxx, i - 1, j), G(sxx, i + 1, j), G(sxx, i - 2, j), dx24);
+        R d2 = D(G(sxy, i, j), G(sxy, i, j - 1), G(sxy, i, j + 1), G(sxy, i, j - 2), dy24);
+        m_dsxx_dx[c] = X.b[i - 1] * m_dsxx_dx[c] + X.a[i - 1] * d1;
+        m_dsxy_dy[c] = Y.b[j - 1] * m_dsxy_dy[c] + Y.a[j - 1] * d2;
+        d1 = d1 / X.K[i - 1] + m_dsxx_dx[c];
+        d2 = d2 / Y.K[j - 1] + m_dsxy_dy[c];
+        vx[c] = vx[c] + (d1 + d2) * DT / rho[c];
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j);
+        R rhh = R(0.25) * (rho[c] + rho[at(i + 1, j)] + rho[at(i + 1, j + 1)] + rho[at(i, j + 1)]);
+        R d1 = D(G(sxy, i + 1, j), G(sxy, i, j), G(sxy, i + 2, j), G(sxy, i - 1, j), dx24);
+        R d2 = D(G(syy, i, j + 1), G(syy, i, j), G(syy, i, j + 2), G(syy, i, j - 1), dy24);
+        m_dsxy_dx[c] = X.bh[i - 1] * m_dsxy_dx[c] + X.ah[i - 1] * d1;
+        m_dsyy_dy[c] = Y.bh[j - 1] * m_dsyy_dy[c] + Y.ah[j - 1] * d2;
+        d1 = d1 / X.Kh[i - 1] + m_dsxy_dx[c];
+        d2 = d2 / Y.Kh[j - 1] + m_dsyy_dy[c];
+        vy[c] = vy[c] + (d1 + d2) * DT / rhh;
+      }
+    {  // source (2D4:672-680)
+      const double st = source_term(p, it);
+      const R fx = R(sa * st), fy = R(ca * st);
+      const int i = p->isource, j = p->jsource;
+      R rhh = R(0.25) * (rho[at(i, j)] + rho[at(i + 1, j)] + rho[at(i + 1, j + 1)] + rho[at(i, j + 1)]);
+      vx[at(i, j)] = vx[at(i, j)] + fx * DT / rho[at(i, j)];
+      vy[at(i, j)] = vy[at(i, j)] + fy * DT / rhh;
+    }
+    for (int j = 1; j <= NY; ++j) {   // rigid edges (2D4:683-693)
+      vx[at(1, j)] = 0; vx[at(NX, j)] = 0; vy[at(1, j)] = 0; vy[at(NX, j)] = 0;
+    }
+    for (int i = 1; i <= NX; ++i) {
+      vx[at(i, 1)] = 0; vx[at(i, NY)] = 0; vy[at(i, 1)] = 0; vy[at(i, NY)] = 0;
+    }
+    for (int r = 0; r < o.nrec; ++r) {
+      o.sisvx[size_t(r) * o.nsteps + it - 1] = double(vx[at(o.ix[r], o.iy[r])]);
+      o.sisvy[size_t(r) * o.nsteps + it - 1] = double(vy[at(o.ix[r], o.iy[r])]);
+    }
+    if (o.ek || o.ep) {   // one cell wider than the second-order program's interior
+      double ek = 0.0, ep = 0.0;
+      for (int j = npml; j <= NY - npml + 1; ++j)
+        for (int i = npml; i <= NX - npml + 1; ++i) {
+          const size_t c = at(i, j);
+          const double vxx = vx[c], vyy = vy[c];
+          ek = ek + double(rho[c]) * (vxx * vxx + vyy * vyy);
+          const double l = lam[c], m = mu[c];
+          const double s1 = sxx[c], s2 = syy[c], s3 = sxy[c];
+          const double exx = ((l + 2.0 * m) * s1 - l * s2) / (4.0 * m * (l + m));
+          const double eyy = ((l + 2.0 * m) * s2 - l * s1) / (4.0 * m * (l + m));
+          const double exy = s3 / (2.0 * m);
+          ep = ep + 0.5 * (exx * s1 + eyy * s2 + 2.0 * exy * s3);
+        }
+      if (o.ek) o.ek[it - 1] = 0.5 * ek;
+      if (o.ep) o.ep[it - 1] = ep;
+    }
+    if (o.vmax) {
+      double vm = 0.0;
+      for (size_t c = 0; c < N; ++c)
+        vm = std::max(vm, std::sqrt(double(vx[c]) * vx[c] + double(vy[c]) * vy[c]));
+      o.vmax[it - 1] = vm;
+    }
+  }
+
+// ---------------------------------------------------------------------------
+// classical split-field PML program (Collino and Tsogka), PML:180-533
+// ---------------------------------------------------------------------------
+// Damping profile divided by two at grid and half points of one axis
+// (PML:204-226 for x, 228-250 for y): d0 = 3 cp ln(1/Rcoef) / (2 delta),
+// quadratic, with the reference's 0.9999 factor on the high-side test.
+void split_profile(const cpml_params* p, int n, double h, std::vector<double>& full,
+                   std::vector<double>& half) {
+  const double delta = p->npoints_pml * h;
+  const double d0 = 3.0 * p->cp * std::log(1.0 / p->rcoef) / (2.0 * delta);
+  const double ol = delta, orr = (n - 1) * h - delta;
+  full.assign(n, 0.0);
+  half.assign(n, 0.0);
+  for (int i = 1; i <= n; ++i) {
+    const double xval = h * double(i - 1);
+    double f = 0.0, g = 0.0;
+    if (xval < ol) {
+      f = d0 * std::pow((ol - xval) / delta, 2);
+      g = d0 * std::pow((ol - xval - h / 2.0) / delta, 2);
+    } else if (xval >= 0.9999 * orr) {
+      f = d0 * std::pow((xval - orr) / delta, 2);
+      g = d0 * std::pow((xval + h / 2.0 - orr) / delta, 2);
+    }
+    full[i - 1] = f / 2.0;
+    half[i - 1] = g / 2.0;
+  }
+}
+
+template <typename R>
+struct StateSplit {
+  const cpml_params* p;
+  int NX, NY;
+  size_t N;
+  R h, odt, rho, lam, mu, l2m;
+  std::vector<R> dx2, dxh2, dy2, dyh2;
+  std::vector<R> vx1, vx2, vy1, vy2, sxx1, sxx2, syy1, syy2, sxy1, sxy2;
+  int npml;
+  double sa, ca;
+  explicit StateSplit(const cpml_params* p_)
+      : p(p_), NX(p_->nx), NY(p_->ny), N(size_t(p_->nx) * p_->ny) {
+    h = R(p->deltax);
+    odt = R(1.0 / p->deltat);                             // ONE_OVER_DELTAT (PML:118)
+    rho = R(p->rho);
+    mu = R(p->rho * p->cs * p->cs);                       // PML:108-110
+    lam = R(p->rho * (p->cp * p->cp - 2.0 * p->cs * p->cs));
+    l2m = R(p->rho * p->cp * p->cp);
+    std::vector<double> f, g;
+    auto cv = [](const std::vector<double>& v) { return std::vector<R>(v.begin(), v.end()); };
+    split_profile(p, NX, p->deltax, f, g); dx2 = cv(f); dxh2 = cv(g);
+    split_profile(p, NY, p->deltay, f, g); dy2 = cv(f); dyh2 = cv(g);
+    for (auto* v : {&vx1, &vx2, &vy1, &vy2, &sxx1, &sxx2, &syy1, &syy2, &sxy1, &sxy2}) v->assign(N, R(0));
+    npml = p->npoints_pml;
+    const double ang = p->angle_force * (PI / 180.0);
+    sa = std::sin(ang); ca = std::cos(ang);
+  }
+  size_t at(int i, int j) const { return size_t(j - 1) * NX + (i - 1); }
+  void advance(int it, const Out& o);
+  void fields(double* out) const {   // total fields vx vy sxx syy sxy
+    const std::vector<R>* A[5] = {&vx1, &vy1, &sxx1, &syy1, &sxy1};
+    const std::vector<R>* B[5] = {&vx2, &vy2, &sxx2, &syy2, &sxy2};
+    for (int f = 0; f < 5; ++f)
+      for (size_t c = 0; c < N; ++c) out[f * N + c] = double((*A[f])[c]) + double((*B[f])[c]);
+  }
+};
+
+// one pass of PML:337-533
+template <typename R>
+void StateSplit<R>::advance(int it, const Out& o) {
+    auto upd = [&](R old, R d, R rhs) { return (old * (odt - d) + rhs) / (odt + d); };
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)            // PML:344-364
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j), e = at(i + 1, j), s_ = at(i, j - 1);
+        const R vdx = (vx1[e] - vx1[c]) / h + (vx2[e] - vx2[c]) / h;
+        const R vdy = (vy1[c] - vy1[s_]) / h + (vy2[c] - vy2[s_]) / h;
+        R d = dxh2[i - 1];
+        sxx1[c] = upd(sxx1[c], d, l2m * vdx);
+        syy1[c] = upd(syy1[c], d, lam * vdx);
+        d = dy2[j - 1];
+        sxx2[c] = upd(sxx2[c], d, lam * vdy);
+        syy2[c] = upd(syy2[c], d, l2m * vdy);
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)        // PML:366-383
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j), w = at(i - 1, j), n_ = at(i, j + 1);
+        const R vdx = (vy1[c] - vy1[w]) / h + (vy2[c] - vy2[w]) / h;
+        const R vdy = (vx1[n_] - vx1[c]) / h + (vx2[n_] - vx2[c]) / h;
+        sxy1[c] = upd(sxy1[c], dx2[i - 1], mu * vdx);
+        sxy2[c] = upd(sxy2[c], dyh2[j - 1], mu * vdy);
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 2; j <= NY; ++j)            // PML:389-406
+      for (int i = 2; i <= NX; ++i) {
+        const size_t c = at(i, j), w = at(i - 1, j), s_ = at(i, j - 1);
+        const R sdx = (sxx1[c] - sxx1[w]) / h + (sxx2[c] - sxx2[w]) / h;
+        const R sdy = (sxy1[c] - sxy1[s_]) / h + (sxy2[c] - sxy2[s_]) / h;
+        vx1[c] = upd(vx1[c], dx2[i - 1], sdx / rho);
+        vx2[c] = upd(vx2[c], dy2[j - 1], sdy / rho);
+      }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= NY - 1; ++j)        // PML:408-425
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = at(i, j), e = at(i + 1, j), n_ = at(i, j + 1);
+        const R sdx = (sxy1[e] - sxy1[c]) / h + (sxy2[e] - sxy2[c]) / h;
+        const R sdy = (syy1[n_] - syy1[c]) / h + (syy2[n_] - syy2[c]) / h;
+        vy1[c] = upd(vy1[c], dxh2[i - 1], sdx / rho);
+        vy2[c] = upd(vy2[c], dyh2[j - 1], sdy / rho);
+      }
+    {  // source on the first split component (PML:428-451)
+      const double st = source_term(p, it);
+      const size_t c = at(p->isource, p->jsource);
+      vx1[c] = vx1[c] + R(sa * st) * R(p->deltat) / rho;
+      vy1[c] = vy1[c] + R(ca * st) * R(p->deltat) / rho;
+    }
+    for (int j = 1; j <= NY; ++j)            // rigid edges, both components (PML:453-478)
+      for (auto* v : {&vx1, &vy1, &vx2, &vy2}) { (*v)[at(1, j)] = 0; (*v)[at(NX, j)] = 0; }
+    for (int i = 1; i <= NX; ++i)
+      for (auto* v : {&vx1, &vy1, &vx2, &vy2}) { (*v)[at(i, 1)] = 0; (*v)[at(i, NY)] = 0; }
+    for (int r = 0; r < o.nrec; ++r) {       // PML:481-484
+      const size_t c = at(o.ix[r], o.iy[r]);
+      o.sisvx[size_t(r) * o.nsteps + it - 1] = double(vx1[c]) + double(vx2[c]);
+      o.sisvy[size_t(r) * o.nsteps + it - 1] = double(vy1[c]) + double(vy2[c]);
+    }
+    if (o.ek || o.ep) {                      // PML:486-515
+      const double l = double(lam), m = double(mu), r = double(rho);
+      double ek = 0.0, ep = 0.0;
+      for (int j = npml + 1; j <= NY - npml; ++j)
+        for (int i = npml + 1; i <= NX - npml; ++i) {
+          const size_t c = at(i, j);
+          const double vxt = double(vx1[c]) + double(vx2[c]), vyt = double(vy1[c]) + double(vy2[c]);
+          ek = ek + r * (vxt * vxt + vyt * vyt);
+          const double s1 = double(sxx1[c]) + double(sxx2[c]);
+          const double s2 = double(syy1[c]) + double(syy2[c]);
+          const double s3 = double(sxy1[c]) + double(sxy2[c]);
+          const double exx = ((l + 2.0 * m) * s1 - l * s2) / (4.0 * m * (l + m));
+          const double eyy = ((l + 2.0 * m) * s2 - l * s1) / (4.0 * m * (l + m));
+          const double exy = s3 / (2.0 * m);
+          ep = ep + 0.5 * (exx * s1 + eyy * s2 + 2.0 * exy * s3);
+        }
+      if (o.ek) o.ek[it - 1] = 0.5 * ek;
+      if (o.ep) o.ep[it - 1] = ep;
+    }
+    if (o.vmax) {
+      double vm = 0.0;
+      for (size_t c = 0; c < N; ++c) {
+        const double a = double(vx1[c]) + double(vx2[c]), b = double(vy1[c]) + double(vy2[c]);
+        vm = std::max(vm, std::sqrt(a * a + b * b));
+      }
+      o.vmax[it - 1] = vm;
+    }
+  }
+
+template <typename R>
+int run_split(const cpml_params* p, const Out& o, double* fields_out) {
+  StateSplit<R> S(p);
+  for (int it = 1; it <= o.nsteps; ++it) S.advance(it, o);
+  if (fields_out) S.fields(fields_out);
+  return CPML_OK;
+}
+
 template <typename R>
 int run2d(const cpml_params* p, const double* lam_in, const double* mu_in,
           const double* rho_in, const Out& o, double* fields_out) {
   State2D<R> S(p, lam_in, mu_in, rho_in);
-  for (int it = 1; it <= o.nsteps; ++it) S.step(it, o);
+  for (int it = 1; it <= o.nsteps; ++it) S.advance(it, o);
   if (fields_out) S.fields(fields_out);
   return CPML_OK;
 }
@@ -598,6 +876,10 @@ int oracle_run(const cpml_params* p, int nsteps, int use_double, const double* l
   if (nrec > 0 && !sisvx) { sx.resize(size_t(nrec) * nsteps); sisvx = sx.data(); }
   if (nrec > 0 && !sisvy) { sy.resize(size_t(nrec) * nsteps); sisvy = sy.data(); }
   Out o{nsteps, nrec, ix, iy, iz, sisvx, sisvy, sisvz, ek, ep, vmax};
+  if (p->ndim == 2 && p->scheme == CPML_SCHEME_SPLIT) {
+    if (lam || mu || rho) return CPML_ERR_INVALID;   // the split-PML program is homogeneous
+    return use_double ? run_split<double>(p, o, fields_out) : run_split<float>(p, o, fields_out);
+  }
   if (p->ndim == 2)
     return use_double ? run2d<double>(p, lam, mu, rho, o, fields_out)
                       : run2d<float>(p, lam, mu, rho, o, fields_out);
@@ -640,7 +922,7 @@ int oracle_session_run(void* h, int nsteps) {
         S->ek.data(), S->ep.data(), nullptr};
   for (int q = 0; q < nsteps; ++q) {
     ++S->it;
-    if (S->s2) S->s2->step(S->it, o);
+    if (S->s2) S->s2->advance(S->it, o);
     else S->s3->step(S->it, o);
   }
   return S->it;

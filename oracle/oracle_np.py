@@ -44,8 +44,11 @@ FLAG_ENERGY, FLAG_EP_PHYSICAL = 0x1, 0x2
 # C-PML profiles: 2D:283-465 (x and y), 3D:560-667 (z). FP64 host loops.
 # ---------------------------------------------------------------------------
 def pml_profile(n, delta, npml, use_min, use_max, cp, f0, deltat,
-                npower=2.0, k_max=1.0, alpha_max=None, rcoef=0.001):
-    """Return dict of d, K, alpha, a, b and their *_half twins (length n)."""
+                npower=2.0, k_max=1.0, alpha_max=None, rcoef=0.001, high_origin_cells=None):
+    """Return dict of d, K, alpha, a, b and their *_half twins (length n).
+    high_origin_cells: the high-side origin sits at that many cells minus the
+    thickness (default n - 1; the fourth-order program's y axis uses n,
+    2D4:401)."""
     if alpha_max is None or alpha_max < 0:
         alpha_max = 2.0 * PI * (f0 / 2.0)                       # 2D:218
     thickness = npml * delta                                   # 2D:285
@@ -56,7 +59,7 @@ def pml_profile(n, delta, npml, use_min, use_max, cp, f0, deltat,
     a = np.zeros(n); ah = np.zeros(n)
     b = np.zeros(n); bh = np.zeros(n)
     origin_left = thickness
-    origin_right = (n - 1) * delta - thickness
+    origin_right = ((n - 1) if high_origin_cells is None else high_origin_cells) * delta - thickness
     for i in range(1, n + 1):
         val = delta * float(i - 1)
         ii = i - 1
@@ -269,6 +272,227 @@ def run2d(p, nsteps=None, lam=None, mu=None, rho=None, rec=None,
     res = Result(sisvx, sisvy, None, ek, ep, vmax=vmax)
     if keep_fields:
         res.fields = dict(vx=vx, vy=vy, sxx=sxx, syy=syy, sxy=sxy)
+    return res
+
+
+# ---------------------------------------------------------------------------
+# 2D fourth-order program: seismic_CPML_2D_isotropic_fourth_order.f90 (2D4)
+# ---------------------------------------------------------------------------
+def run2d4(p, nsteps=None, lam=None, mu=None, rho=None, rec=None, dtype=np.float64,
+           keep_fields=False):
+    """The fourth-order program's time loop (2D4:553-745). Every array is
+    held with the reference's ghost layer, shape (NY+2, NX+2) for Fortran
+    0:NX+1 x 0:NY+1 (2D4:205, 223): Fortran (i, j) is element [j, i]; the
+    ghost layer is never written and stays zero."""
+    T = np.dtype(dtype).type
+    NX, NY = p.nx, p.ny
+    nsteps = p.nstep if nsteps is None else nsteps
+    g = lambda: np.zeros((NY + 2, NX + 2), dtype)
+
+    def padded(a, default):
+        out = g()
+        out[:, :] = default   # the reference fills the whole 0:NX+1 array (2D4:468-474)
+        if a is not None:
+            out[1:NY + 1, 1:NX + 1] = np.asarray(a, dtype)
+        return out
+    rho = padded(rho, p.rho)
+    mu = padded(mu, p.rho * p.cs * p.cs)
+    lam = padded(lam, p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs))
+    px = {k: np.concatenate([[0.0], v, [0.0]]).astype(dtype) for k, v in _prof(p, 0, NX, p.deltax, np.float64).items()}
+    pr = pml_profile(NY, p.deltay, p.npoints_pml, bool(p.use_pml[2]), bool(p.use_pml[3]), p.cp, p.f0,
+                     p.deltat, p.npower, p.k_max_pml, p.alpha_max_pml, p.rcoef, high_origin_cells=NY)
+    py = {k: np.concatenate([[0.0], v, [0.0]]).astype(dtype) for k, v in pr.items()}
+    DX, DY, DT = T(p.deltax), T(p.deltay), T(p.deltat)
+    c27, c24 = T(27.0), T(24.0)
+    half, two, quarter = T(0.5), T(2.0), T(0.25)
+    vx, vy, sxx, syy, sxy = g(), g(), g(), g(), g()
+    m_dvx_dx, m_dvx_dy, m_dvy_dx, m_dvy_dy = g(), g(), g(), g()
+    m_dsxx_dx, m_dsyy_dy, m_dsxy_dx, m_dsxy_dy = g(), g(), g(), g()
+    rec = rec or []
+    sisvx = np.zeros((len(rec), nsteps)); sisvy = np.zeros((len(rec), nsteps))
+    ek = np.zeros(nsteps); ep = np.zeros(nsteps)
+    vmax = []
+    col = lambda d, k: d[k][None, :]
+    row = lambda d, k: d[k][:, None]
+    npml = p.npoints_pml
+    ang = p.angle_force * (PI / 180.0)
+
+    def S(i0, i1, j0, j1, di=0, dj=0):
+        """Fortran i = i0..i1, j = j0..j1 shifted by (di, dj), as a padded-array slice."""
+        return (slice(j0 + dj, j1 + dj + 1), slice(i0 + di, i1 + di + 1))
+
+    def D(f, r, axis_h, p1, p0, p2, m1):
+        # (27 f(p1) - 27 f(p0) - f(p2) + f(m1)) / (24 h); p* are (di, dj) offsets
+        a = lambda o: f[S(*r, *o)]
+        return (c27 * a(p1) - c27 * a(p0) - a(p2) + a(m1)) / (c24 * axis_h)
+
+    for it in range(1, nsteps + 1):
+        r = (1, NX - 1, 2, NY)                                     # 2D4:557-580
+        R = S(*r)
+        lhx = half * (lam[S(*r, 1, 0)] + lam[R]); mhx = half * (mu[S(*r, 1, 0)] + mu[R])
+        l2m = lhx + two * mhx
+        dvx_dx = D(vx, r, DX, (1, 0), (0, 0), (2, 0), (-1, 0))
+        dvy_dy = D(vy, r, DY, (0, 0), (0, -1), (0, 1), (0, -2))
+        m_dvx_dx[R] = col(px, "b_half")[:, 1:NX] * m_dvx_dx[R] + col(px, "a_half")[:, 1:NX] * dvx_dx
+        m_dvy_dy[R] = row(py, "b")[2:NY + 1] * m_dvy_dy[R] + row(py, "a")[2:NY + 1] * dvy_dy
+        dvx_dx = dvx_dx / col(px, "K_half")[:, 1:NX] + m_dvx_dx[R]
+        dvy_dy = dvy_dy / row(py, "K")[2:NY + 1] + m_dvy_dy[R]
+        sxx[R] = sxx[R] + (l2m * dvx_dx + lhx * dvy_dy) * DT
+        syy[R] = syy[R] + (lhx * dvx_dx + l2m * dvy_dy) * DT
+
+        r = (2, NX, 1, NY - 1)                                     # 2D4:582-600
+        R = S(*r)
+        mhy = half * (mu[S(*r, 0, 1)] + mu[R])
+        dvy_dx = D(vy, r, DX, (0, 0), (-1, 0), (1, 0), (-2, 0))
+        dvx_dy = D(vx, r, DY, (0, 1), (0, 0), (0, 2), (0, -1))
+        m_dvy_dx[R] = col(px, "b")[:, 2:NX + 1] * m_dvy_dx[R] + col(px, "a")[:, 2:NX + 1] * dvy_dx
+        m_dvx_dy[R] = row(py, "b_half")[1:NY] * m_dvx_dy[R] + row(py, "a_half")[1:NY] * dvx_dy
+        dvy_dx = dvy_dx / col(px, "K")[:, 2:NX + 1] + m_dvy_dx[R]
+        dvx_dy = dvx_dy / row(py, "K")[1:NY] + m_dvx_dy[R]        # K_y (2D4:596)
+        sxy[R] = sxy[R] + mhy * (dvy_dx + dvx_dy) * DT
+
+        r = (2, NX, 2, NY)                                         # 2D4:606-621
+        R = S(*r)
+        d1 = D(sxx, r, DX, (0, 0), (-1, 0), (1, 0), (-2, 0))
+        d2 = D(sxy, r, DY, (0, 0), (0, -1), (0, 1), (0, -2))
+        m_dsxx_dx[R] = col(px, "b")[:, 2:NX + 1] * m_dsxx_dx[R] + col(px, "a")[:, 2:NX + 1] * d1
+        m_dsxy_dy[R] = row(py, "b")[2:NY + 1] * m_dsxy_dy[R] + row(py, "a")[2:NY + 1] * d2
+        d1 = d1 / col(px, "K")[:, 2:NX + 1] + m_dsxx_dx[R]
+        d2 = d2 / row(py, "K")[2:NY + 1] + m_dsxy_dy[R]
+        vx[R] = vx[R] + (d1 + d2) * DT / rho[R]
+
+        r = (1, NX - 1, 1, NY - 1)                                 # 2D4:623-641
+        R = S(*r)
+        rhh = quarter * (rho[R] + rho[S(*r, 1, 0)] + rho[S(*r, 1, 1)] + rho[S(*r, 0, 1)])
+        d1 = D(sxy, r, DX, (1, 0), (0, 0), (2, 0), (-1, 0))
+        d2 = D(syy, r, DY, (0, 1), (0, 0), (0, 2), (0, -1))
+        m_dsxy_dx[R] = col(px, "b_half")[:, 1:NX] * m_dsxy_dx[R] + col(px, "a_half")[:, 1:NX] * d1
+        m_dsyy_dy[R] = row(py, "b_half")[1:NY] * m_dsyy_dy[R] + row(py, "a_half")[1:NY] * d2
+        d1 = d1 / col(px, "K_half")[:, 1:NX] + m_dsxy_dx[R]
+        d2 = d2 / row(py, "K_half")[1:NY] + m_dsyy_dy[R]
+        vy[R] = vy[R] + (d1 + d2) * DT / rhh
+
+        st = source_term(p, it)                                    # 2D4:644-680
+        fx, fy = T(math.sin(ang) * st), T(math.cos(ang) * st)
+        i, j = p.isource, p.jsource
+        rs = quarter * (rho[j, i] + rho[j, i + 1] + rho[j + 1, i + 1] + rho[j + 1, i])
+        vx[j, i] = vx[j, i] + fx * DT / rho[j, i]
+        vy[j, i] = vy[j, i] + fy * DT / rs
+        for f in (vx, vy):                                         # 2D4:683-693, whole 0:N+1 lines
+            f[:, 1] = 0; f[:, NX] = 0; f[1, :] = 0; f[NY, :] = 0
+        for q, (ix, iy) in enumerate(rec):
+            sisvx[q, it - 1] = vx[iy, ix]
+            sisvy[q, it - 1] = vy[iy, ix]
+        I = S(npml, NX - npml + 1, npml, NY - npml + 1)            # 2D4:696-712
+        ek[it - 1] = 0.5 * np.sum(rho[I].astype(np.float64) * (
+            vx[I].astype(np.float64) ** 2 + vy[I].astype(np.float64) ** 2))
+        l, m_ = lam[I].astype(np.float64), mu[I].astype(np.float64)
+        s1, s2, s3 = sxx[I].astype(np.float64), syy[I].astype(np.float64), sxy[I].astype(np.float64)
+        exx = ((l + 2.0 * m_) * s1 - l * s2) / (4.0 * m_ * (l + m_))
+        eyy = ((l + 2.0 * m_) * s2 - l * s1) / (4.0 * m_ * (l + m_))
+        ep[it - 1] = np.sum(0.5 * (exx * s1 + eyy * s2 + 2.0 * (s3 / (2.0 * m_)) * s3))
+        if it % p.it_display == 0 or it == 5:
+            vmax.append((it, float(np.max(np.sqrt(vx.astype(np.float64) ** 2 + vy.astype(np.float64) ** 2)))))
+    res = Result(sisvx, sisvy, None, ek, ep, vmax=vmax)
+    if keep_fields:
+        inner = (slice(1, NY + 1), slice(1, NX + 1))
+        res.fields = dict(vx=vx[inner], vy=vy[inner], sxx=sxx[inner], syy=syy[inner], sxy=sxy[inner])
+    return res
+
+
+# ---------------------------------------------------------------------------
+# classical split-field PML: seismic_PML_Collino_2D_isotropic.f90 (PML)
+# ---------------------------------------------------------------------------
+def split_profile(n, h, npml, cp, rcoef):
+    """Damping d/2 at grid and half points (PML:180-250)."""
+    delta = npml * h
+    d0 = 3.0 * cp * math.log(1.0 / rcoef) / (2.0 * delta)
+    ol, orr = delta, (n - 1) * h - delta
+    f = np.zeros(n); g = np.zeros(n)
+    for i in range(1, n + 1):
+        x = h * float(i - 1)
+        if x < ol:
+            f[i - 1] = d0 * ((ol - x) / delta) ** 2
+            g[i - 1] = d0 * ((ol - x - h / 2.0) / delta) ** 2
+        elif x >= 0.9999 * orr:
+            f[i - 1] = d0 * ((x - orr) / delta) ** 2
+            g[i - 1] = d0 * ((x + h / 2.0 - orr) / delta) ** 2
+    return f / 2.0, g / 2.0
+
+
+def run_split(p, nsteps=None, rec=None, dtype=np.float64, keep_fields=False):
+    """The split-field PML program's time loop (PML:337-533): every field is
+    the sum of an x and a y part, each damped by its own axis's profile."""
+    T = np.dtype(dtype).type
+    NX, NY = p.nx, p.ny
+    nsteps = p.nstep if nsteps is None else nsteps
+    h, odt = T(p.deltax), T(1.0 / p.deltat)
+    rho = T(p.rho)
+    mu = T(p.rho * p.cs * p.cs)
+    lam = T(p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs))
+    l2m = T(p.rho * p.cp * p.cp)
+    dx2, dxh2 = (a.astype(dtype)[None, :] for a in split_profile(NX, p.deltax, p.npoints_pml, p.cp, p.rcoef))
+    dy2, dyh2 = (a.astype(dtype)[:, None] for a in split_profile(NY, p.deltay, p.npoints_pml, p.cp, p.rcoef))
+    z = lambda: np.zeros((NY, NX), dtype)
+    vx1, vx2, vy1, vy2 = z(), z(), z(), z()
+    sxx1, sxx2, syy1, syy2, sxy1, sxy2 = z(), z(), z(), z(), z(), z()
+    rec = rec or []
+    sisvx = np.zeros((len(rec), nsteps)); sisvy = np.zeros((len(rec), nsteps))
+    ek = np.zeros(nsteps); ep = np.zeros(nsteps)
+    vmax = []
+    ang = p.angle_force * (PI / 180.0)
+    npml = p.npoints_pml
+    upd = lambda old, d, rhs: (old * (odt - d) + rhs) / (odt + d)
+    for it in range(1, nsteps + 1):
+        R = (slice(1, NY), slice(0, NX - 1))                        # PML:344-364
+        vdx = (vx1[1:, 1:] - vx1[1:, :-1]) / h + (vx2[1:, 1:] - vx2[1:, :-1]) / h
+        vdy = (vy1[1:, :-1] - vy1[:-1, :-1]) / h + (vy2[1:, :-1] - vy2[:-1, :-1]) / h
+        d = dxh2[:, :-1]
+        sxx1[R] = upd(sxx1[R], d, l2m * vdx)
+        syy1[R] = upd(syy1[R], d, lam * vdx)
+        d = dy2[1:]
+        sxx2[R] = upd(sxx2[R], d, lam * vdy)
+        syy2[R] = upd(syy2[R], d, l2m * vdy)
+        R = (slice(0, NY - 1), slice(1, NX))                        # PML:366-383
+        vdx = (vy1[:-1, 1:] - vy1[:-1, :-1]) / h + (vy2[:-1, 1:] - vy2[:-1, :-1]) / h
+        vdy = (vx1[1:, 1:] - vx1[:-1, 1:]) / h + (vx2[1:, 1:] - vx2[:-1, 1:]) / h
+        sxy1[R] = upd(sxy1[R], dx2[:, 1:], mu * vdx)
+        sxy2[R] = upd(sxy2[R], dyh2[:-1], mu * vdy)
+        R = (slice(1, NY), slice(1, NX))                            # PML:389-406
+        sdx = (sxx1[1:, 1:] - sxx1[1:, :-1]) / h + (sxx2[1:, 1:] - sxx2[1:, :-1]) / h
+        sdy = (sxy1[1:, 1:] - sxy1[:-1, 1:]) / h + (sxy2[1:, 1:] - sxy2[:-1, 1:]) / h
+        vx1[R] = upd(vx1[R], dx2[:, 1:], sdx / rho)
+        vx2[R] = upd(vx2[R], dy2[1:], sdy / rho)
+        R = (slice(0, NY - 1), slice(0, NX - 1))                    # PML:408-425
+        sdx = (sxy1[:-1, 1:] - sxy1[:-1, :-1]) / h + (sxy2[:-1, 1:] - sxy2[:-1, :-1]) / h
+        sdy = (syy1[1:, :-1] - syy1[:-1, :-1]) / h + (syy2[1:, :-1] - syy2[:-1, :-1]) / h
+        vy1[R] = upd(vy1[R], dxh2[:, :-1], sdx / rho)
+        vy2[R] = upd(vy2[R], dyh2[:-1], sdy / rho)
+        st = source_term(p, it)                                     # PML:428-451
+        i, j = p.isource - 1, p.jsource - 1
+        vx1[j, i] = vx1[j, i] + T(math.sin(ang) * st) * T(p.deltat) / rho
+        vy1[j, i] = vy1[j, i] + T(math.cos(ang) * st) * T(p.deltat) / rho
+        for f in (vx1, vy1, vx2, vy2):                              # PML:453-478
+            f[:, 0] = 0; f[:, NX - 1] = 0; f[0, :] = 0; f[NY - 1, :] = 0
+        vxt = vx1.astype(np.float64) + vx2.astype(np.float64)
+        vyt = vy1.astype(np.float64) + vy2.astype(np.float64)
+        for q, (ix, iy) in enumerate(rec):                          # PML:481-484
+            sisvx[q, it - 1] = vxt[iy - 1, ix - 1]
+            sisvy[q, it - 1] = vyt[iy - 1, ix - 1]
+        I = (slice(npml, NY - npml), slice(npml, NX - npml))        # PML:486-515
+        ek[it - 1] = 0.5 * np.sum(float(rho) * (vxt[I] ** 2 + vyt[I] ** 2))
+        l, m_ = float(lam), float(mu)
+        s1 = (sxx1.astype(np.float64) + sxx2)[I]
+        s2 = (syy1.astype(np.float64) + syy2)[I]
+        s3 = (sxy1.astype(np.float64) + sxy2)[I]
+        exx = ((l + 2.0 * m_) * s1 - l * s2) / (4.0 * m_ * (l + m_))
+        eyy = ((l + 2.0 * m_) * s2 - l * s1) / (4.0 * m_ * (l + m_))
+        ep[it - 1] = np.sum(0.5 * (exx * s1 + eyy * s2 + 2.0 * (s3 / (2.0 * m_)) * s3))
+        if it % p.it_display == 0 or it == 5:
+            vmax.append((it, float(np.max(np.sqrt(vxt ** 2 + vyt ** 2)))))
+    res = Result(sisvx, sisvy, None, ek, ep, vmax=vmax)
+    if keep_fields:
+        res.fields = dict(vx=vx1 + vx2, vy=vy1 + vy2, sxx=sxx1 + sxx2, syy=syy1 + syy2, sxy=sxy1 + sxy2)
     return res
 
 

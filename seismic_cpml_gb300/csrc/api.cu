@@ -23,15 +23,13 @@
 #include "cpml_internal.cuh"
 
 namespace cpml {
-struct ProfileArgs {
-  int n, npml, use_min, use_max;
-  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
-};
 void launch_build_profile(const ProfileArgs& P, double* out64, float* out32, cudaStream_t st);
 void launch_reduce_chunk(const StepArgs& s, int C, double* ek, double* ep, double* vmax, int* bad,
                          cudaStream_t st);
 void launch_step3d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
 void launch_step2d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t st);
+void launch_step2d_order4(const StepArgs& s, int ls, bool het, cudaStream_t st);
+void launch_step2d_split(const StepArgs& s, int ls, cudaStream_t st);
 int persist2d_grid(const StepArgs& s, bool het);
 cudaError_t launch_chunk2d_persistent(const StepArgs& s, int C, bool het, unsigned* bar, int grid,
                                       cudaStream_t st);
@@ -57,6 +55,15 @@ namespace {
 const double kPi = 3.141592653589793238462643;
 const double kStability = 1.0e25;  // STABILITY_THRESHOLD (2D:201)
 const int kMaxChunk = 128;
+
+// FNV-1a, 64-bit: fingerprints of the parameter block, model and receivers
+// that a state snapshot must match before it is loaded
+const uint64_t kFnvBasis = 1469598103934665603ULL;
+uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ULL; }
+  return h;
+}
 
 double source_term(const cpml_params* p, int it) {  // 2D:644-654
   const double a = kPi * kPi * p->f0 * p->f0;
@@ -93,6 +100,7 @@ struct cpml_handle {
   Axis axes[3] = {};
   float* model[3] = {};  // lam, mu, rho (per-cell, optional)
   bool het = false;
+  uint64_t model_hash = 0; // FNV-1a of the per-cell model's host arrays (0: homogeneous)
   double cp_max = 0;
   double rho_src[2] = {0, 0};  // rho used for the x / y source increments
   float* src_fx = nullptr;
@@ -119,6 +127,11 @@ struct cpml_handle {
 };
 
 namespace {
+
+bool is_split(const cpml_handle* h) { return h->ndim == 2 && h->p.scheme == CPML_SCHEME_SPLIT; }
+bool is_order4(const cpml_handle* h) { return h->ndim == 2 && h->p.order == 4; }
+// the second-order 2D C-PML program: the only 2D form with a persistent kernel
+bool is_standard2d(const cpml_handle* h) { return h->ndim == 2 && !is_split(h) && !is_order4(h); }
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return CPML_OK;
@@ -189,6 +202,11 @@ int validate(const cpml_params* p) {
     return CPML_ERR_INVALID;
   if (p->ndim == 3 && (p->ksource < 1 || p->ksource > nz)) return CPML_ERR_INVALID;
   if (p->it_display < 1) return CPML_ERR_INVALID;
+  if (p->order != 0 && p->order != 2 && p->order != 4) return CPML_ERR_INVALID;
+  if (p->scheme != CPML_SCHEME_CPML && p->scheme != CPML_SCHEME_SPLIT) return CPML_ERR_INVALID;
+  if (p->order == 4 && (p->ndim != 2 || p->scheme != CPML_SCHEME_CPML)) return CPML_ERR_INVALID;
+  // the split-field program has one grid spacing h (PML:100)
+  if (p->scheme == CPML_SCHEME_SPLIT && (p->ndim != 2 || p->deltax != p->deltay)) return CPML_ERR_INVALID;
   const double cells = double(p->nx) * p->ny * nz;
   if (cells > 4.0e9) return CPML_ERR_RANGE;
   return CPML_OK;
@@ -251,6 +269,17 @@ StepArgs make_args(cpml_handle* h, int q = 0) {
   s.partials = h->partials;
   s.nblocks = h->nblocks;
   s.ep_physical = (p.flags & CPML_FLAG_EP_PHYSICAL) ? 1 : 0;
+  s.o24dx = float(1.0 / (24.0 * p.deltax));
+  s.o24dy = float(1.0 / (24.0 * p.deltay));
+  if (is_split(h)) {  // x parts in set 0, y parts in set 1 (PML:163-165)
+    s.split = 1;
+    s.g.vx = h->fld1[0]; s.g.vy = h->fld1[1];
+    s.g.sxx = h->fld1[3]; s.g.syy = h->fld1[4]; s.g.sxy = h->fld1[6];
+    s.lam_split = float(lam);
+    s.mu_split = float(mu);
+    s.l2m_split = float(p.rho * p.cp * p.cp);   // lambda_plus_two_mu = rho cp^2 (PML:111)
+    s.orho_split = float(1.0 / p.rho);
+  }
   return s;
 }
 
@@ -270,10 +299,54 @@ int upload_source(cpml_handle* h) {
   return cudaStreamSynchronize(h->stream) == cudaSuccess ? CPML_OK : CPML_ERR_CUDA;
 }
 
+// Split-field PML tables of one axis (PML:180-250), built on the host in
+// FP64: the damping profile divided by two at grid and half points, d and dh,
+// and the relaxation factors a = 1/dt - d, b = 1/dt + d (ah, bh at half
+// points) the kernels read. No memory variables: slab width 0.
+int build_axis_split(cpml_handle* h, int axis, int n, double h_) {
+  const cpml_params& p = h->p;
+  const double delta = p.npoints_pml * h_;
+  const double d0 = 3.0 * p.cp * std::log(1.0 / p.rcoef) / (2.0 * delta);
+  const double ol = delta, orr = (n - 1) * h_ - delta, odt = 1.0 / p.deltat;
+  std::vector<double> hp(size_t(10) * n, 0.0);
+  std::vector<float> f32(size_t(6) * n, 0.0f);
+  for (int i = 0; i < n; ++i) {
+    const double x = h_ * double(i);
+    double f = 0.0, g = 0.0;
+    if (x < ol) {
+      f = d0 * std::pow((ol - x) / delta, 2);
+      g = d0 * std::pow((ol - x - h_ / 2.0) / delta, 2);
+    } else if (x >= 0.9999 * orr) {   // the reference's edge fix (PML:213)
+      f = d0 * std::pow((x - orr) / delta, 2);
+      g = d0 * std::pow((x + h_ / 2.0 - orr) / delta, 2);
+    }
+    f /= 2.0;
+    g /= 2.0;
+    hp[0 * size_t(n) + i] = f; hp[1 * size_t(n) + i] = 1.0; hp[4 * size_t(n) + i] = 1.0;
+    hp[5 * size_t(n) + i] = g; hp[6 * size_t(n) + i] = 1.0; hp[9 * size_t(n) + i] = 1.0;
+    f32[0 * size_t(n) + i] = float(odt - f); f32[1 * size_t(n) + i] = float(odt + f);
+    f32[2 * size_t(n) + i] = 1.0f;
+    f32[3 * size_t(n) + i] = float(odt - g); f32[4 * size_t(n) + i] = float(odt + g);
+    f32[5 * size_t(n) + i] = 1.0f;
+  }
+  int st;
+  if ((st = dalloc(h, &h->prof64[axis], size_t(10) * n))) return st;
+  if ((st = dalloc(h, &h->prof32[axis], size_t(6) * n))) return st;
+  CK(cudaMemcpy(h->prof64[axis], hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->prof32[axis], f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+  Axis& A = h->axes[axis];
+  const float* t = h->prof32[axis];
+  A.a = t; A.b = t + n; A.ik = t + 2 * n; A.ah = t + 3 * n; A.bh = t + 4 * n; A.ikh = t + 5 * n;
+  A.n = n; A.lo = 0; A.hi = 0;
+  return CPML_OK;
+}
+
 int build_axis(cpml_handle* h, int axis, int n, double delta) {
+  if (is_split(h)) return build_axis_split(h, axis, n, delta);
   const cpml_params& p = h->p;
   ProfileArgs P{};
   P.n = n; P.npml = p.npoints_pml;
+  P.high_cells = (is_order4(h) && axis == 1) ? n : n - 1;
   P.use_min = p.use_pml[2 * axis]; P.use_max = p.use_pml[2 * axis + 1];
   P.delta = delta; P.cp = p.cp; P.f0 = p.f0; P.dt = p.deltat; P.npower = p.npower;
   P.kmax = p.k_max_pml; P.amax = p.alpha_max_pml < 0 ? 2.0 * kPi * (p.f0 / 2.0) : p.alpha_max_pml;
@@ -365,6 +438,10 @@ void launch_step(cpml_handle* h, int q, int ls) {
   if (h->ndim == 3) {
     if (h->pingpong) fused3d_launch(h->plan.data(), s, ls, q, h->stream);
     else launch_step3d_two_sweep(s, ls, h->het, h->stream);
+  } else if (is_split(h)) {
+    launch_step2d_split(s, ls, h->stream);
+  } else if (is_order4(h)) {
+    launch_step2d_order4(s, ls, h->het, h->stream);
   } else {
     launch_step2d_two_sweep(s, ls, h->het, h->stream);
   }
@@ -463,7 +540,7 @@ int configure_path_impl(cpml_handle* h) {
     h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
   }
   h->persist = false;
-  if (h->ndim == 2 && h->kernel != CPML_KERNEL_TWO_SWEEP) {
+  if (is_standard2d(h) && h->kernel != CPML_KERNEL_TWO_SWEEP) {
     const StepArgs s = make_args(h);
     h->persist_grid = persist2d_grid(s, h->het);
     // automatic choice: persistent only when the grid has more tiles than
@@ -529,6 +606,9 @@ int cpml_create(const cpml_params* pin, cpml_handle** out) {
   const int used2[9] = {1, 1, 0, 1, 1, 0, 1, 0, 0};
   for (int f = 0; f < 9; ++f)
     if ((h->ndim == 3 ? used3 : used2)[f] && (st = dalloc(h, &h->fld[f], h->ncellp))) return fail(st);
+  if (is_split(h))   // the y parts of the split fields (vx_2 ... sigmaxy_2, PML:163-165)
+    for (int f = 0; f < 9; ++f)
+      if (used2[f] && (st = dalloc(h, &h->fld1[f], h->ncellp))) return fail(st);
   if ((st = build_axis(h, 0, h->nx, pin->deltax))) return fail(st);
   if ((st = build_axis(h, 1, h->ny, pin->deltay))) return fail(st);
   if (h->ndim == 3) {
@@ -560,6 +640,7 @@ int cpml_create(const cpml_params* pin, cpml_handle** out) {
 int cpml_set_model(cpml_handle* h, const float* lam, const float* mu, const float* rho) {
   if (!h) return CPML_ERR_INVALID;
   if (!lam && !mu && !rho) return CPML_OK;
+  if (is_split(h)) return CPML_ERR_INVALID;   // the split-field program is homogeneous
   const cpml_params& p = h->p;
   const size_t n = size_t(h->nx) * h->ny * h->nz;
   const float def[3] = {float(p.rho * (p.cp * p.cp - 2.0 * p.cs * p.cs)), float(p.rho * p.cs * p.cs),
@@ -573,6 +654,11 @@ int cpml_set_model(cpml_handle* h, const float* lam, const float* mu, const floa
     cpm = std::max(cpm, std::sqrt((l + 2.0 * m) / r));
   }
   if (cpml_courant(&p, cpm) > 1.0) return CPML_ERR_CFL;
+  uint64_t hash = kFnvBasis;
+  for (int q = 0; q < 3; ++q) {
+    if (src[q]) hash = fnv1a(hash, src[q], sizeof(float) * n);
+    else hash = fnv1a(hash, &def[q], sizeof(float));
+  }
   int st;
   std::vector<float> tmp;
   for (int q = 0; q < 3; ++q) {
@@ -586,6 +672,7 @@ int cpml_set_model(cpml_handle* h, const float* lam, const float* mu, const floa
     CK(cudaStreamSynchronize(h->stream));
   }
   h->het = true;
+  h->model_hash = hash;
   h->cp_max = cpm;
   if ((st = configure_path(h))) return st;
   // rho at the source (2D:661-667 uses rho(i,j) and the 4-point average for
@@ -734,22 +821,212 @@ static float* field_ptr(cpml_handle* h, int field) {
   return cur_fields(h)[field];
 }
 
+}  // extern "C"
+namespace {
+// The split-field program's total field is the sum of its x and y parts
+// (PML:153-159); this adds the y part, copied the same way, into out.
+template <typename Copy>
+int add_split_part(cpml_handle* h, int field, size_t n, float* out, Copy copy) {
+  if (!is_split(h)) return CPML_OK;
+  std::vector<float> part(n);
+  CK(copy(part.data(), h->fld1[field]));
+  CK(cudaStreamSynchronize(h->stream));
+  for (size_t c = 0; c < n; ++c) out[c] = out[c] + part[c];
+  return CPML_OK;
+}
+}  // namespace
+extern "C" {
+
 int cpml_get_field(cpml_handle* h, int field, float* out) {
   if (!h || !out) return CPML_ERR_INVALID;
   float* f = field_ptr(h, field);
   if (!f) return CPML_ERR_INVALID;
-  CK(cudaMemcpy2DAsync(out, sizeof(float) * h->nx, f, sizeof(float) * h->px, sizeof(float) * h->nx,
-                       size_t(h->ny) * h->nz, cudaMemcpyDeviceToHost, h->stream));
+  auto copy = [&](float* dst, const float* src) {
+    return cudaMemcpy2DAsync(dst, sizeof(float) * h->nx, src, sizeof(float) * h->px, sizeof(float) * h->nx,
+                             size_t(h->ny) * h->nz, cudaMemcpyDeviceToHost, h->stream);
+  };
+  CK(copy(out, f));
   CK(cudaStreamSynchronize(h->stream));
-  return CPML_OK;
+  return add_split_part(h, field, size_t(h->nx) * h->ny * h->nz, out, copy);
 }
 
+// Split-field handles: the total goes to the x part, the y part is zeroed.
 int cpml_set_field(cpml_handle* h, int field, const float* in) {
   if (!h || !in) return CPML_ERR_INVALID;
   float* f = field_ptr(h, field);
   if (!f) return CPML_ERR_INVALID;
   CK(cudaMemcpy2DAsync(f, sizeof(float) * h->px, in, sizeof(float) * h->nx, sizeof(float) * h->nx,
                        size_t(h->ny) * h->nz, cudaMemcpyHostToDevice, h->stream));
+  if (is_split(h)) CK(cudaMemsetAsync(h->fld1[field], 0, sizeof(float) * h->ncellp, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+// ---- checkpoint / restart ---------------------------------------------------
+// Snapshot layout (host memory, native byte order): StateHeader, then the
+// current time level's wavefields ([k][j][i] FP32, 9 in 3D, vx vy sxx syy sxy
+// in 2D), every C-PML memory variable in its slab layout (axis by axis,
+// variable by variable, the stress-side ones at the current time level),
+// the seismogram samples so far ([3][nrec][it] FP32), then ek, ep, max|v|
+// (FP64) and the non-finite flags (int32) of steps 1..it.
+}  // extern "C"
+namespace {
+struct StateHeader {
+  char magic[8];
+  int32_t version, ndim, nx, ny, nz, npml, nstep, nrec, it, het, nfield, nvar;
+  int32_t slab_w[3];
+  int32_t unused;
+  uint64_t param_hash, model_hash, rec_hash;
+  double last_vmax;
+  uint64_t bytes;
+};
+const char kStateMagic[8] = {'C', 'P', 'M', 'L', 'S', 'T', 'A', 'T'};
+const int32_t kStateVersion = 1;
+
+uint64_t param_hash(const cpml_handle* h) {
+  cpml_params q = h->p;
+  std::memset(q.reserved_i, 0, sizeof(q.reserved_i));
+  std::memset(q.reserved_d, 0, sizeof(q.reserved_d));
+  return fnv1a(kFnvBasis, &q, sizeof(q));
+}
+uint64_t rec_hash(const cpml_handle* h) {
+  return fnv1a(kFnvBasis, h->rec_ijk.data(), sizeof(int) * h->rec_ijk.size());
+}
+// Device arrays of the time level held in buffer set `set` (set 1 only
+// exists on the fused 3D path); a split-field handle adds its y parts.
+int state_fields(const cpml_handle* h, int set, float** out) {
+  static const int f2[5] = {0, 1, 3, 4, 6};
+  const int n = h->ndim == 3 ? 9 : 5;
+  float* const* F = set == 0 ? h->fld : h->fld1;
+  for (int q = 0; q < n; ++q) out[q] = F[h->ndim == 3 ? q : f2[q]];
+  if (!is_split(h)) return n;
+  for (int q = 0; q < 5; ++q) out[5 + q] = h->fld1[f2[q]];
+  return 10;
+}
+int state_nfield(const cpml_handle* h) { return h->ndim == 3 ? 9 : (is_split(h) ? 10 : 5); }
+size_t state_bytes(const cpml_handle* h, int it) {
+  const size_t ncell = size_t(h->nx) * h->ny * h->nz;
+  const int nf = state_nfield(h), nvar = h->ndim == 3 ? 6 : 4;
+  size_t b = sizeof(StateHeader) + size_t(nf) * ncell * sizeof(float);
+  for (int a = 0; a < h->ndim; ++a) b += size_t(nvar) * slab_floats(h, a) * sizeof(float);
+  b += size_t(3) * h->nrec * it * sizeof(float);
+  b += size_t(it) * (3 * sizeof(double) + sizeof(int));
+  return b;
+}
+float* slab_ptr(const Slabs& S, int axis, int v) { return axis == 0 ? S.x[v] : (axis == 1 ? S.y[v] : S.z[v]); }
+}  // namespace
+extern "C" {
+
+int cpml_state_size(cpml_handle* h, size_t* bytes) {
+  if (!h || !bytes) return CPML_ERR_INVALID;
+  *bytes = state_bytes(h, h->it);
+  return CPML_OK;
+}
+
+int cpml_save_state(cpml_handle* h, void* buf, size_t bytes) {
+  if (!h || !buf) return CPML_ERR_INVALID;
+  const size_t need = state_bytes(h, h->it);
+  if (bytes < need) return CPML_ERR_RANGE;
+  StateHeader H{};
+  std::memcpy(H.magic, kStateMagic, 8);
+  H.version = kStateVersion;
+  H.ndim = h->ndim; H.nx = h->nx; H.ny = h->ny; H.nz = h->nz; H.npml = h->p.npoints_pml;
+  H.nstep = h->p.nstep; H.nrec = h->nrec; H.it = h->it; H.het = h->het ? 1 : 0;
+  float* F[10];
+  H.nfield = state_fields(h, (h->pingpong && (h->it & 1)) ? 1 : 0, F);
+  H.nvar = h->ndim == 3 ? 6 : 4;
+  for (int a = 0; a < 3; ++a) H.slab_w[a] = a < h->ndim ? h->axes[a].width() : 0;
+  H.param_hash = param_hash(h); H.model_hash = h->model_hash; H.rec_hash = rec_hash(h);
+  H.last_vmax = h->last_vmax;
+  H.bytes = need;
+  char* out = static_cast<char*>(buf);
+  std::memcpy(out, &H, sizeof(H));
+  out += sizeof(H);
+  const size_t fs = sizeof(float), ncell = size_t(h->nx) * h->ny * h->nz;
+  for (int q = 0; q < H.nfield; ++q) {
+    CK(cudaMemcpy2DAsync(out, fs * h->nx, F[q], fs * h->px, fs * h->nx, size_t(h->ny) * h->nz,
+                         cudaMemcpyDeviceToHost, h->stream));
+    out += ncell * fs;
+  }
+  // stress-side memory variables (0..2) alternate with the fields on the fused path
+  const bool odd = h->pingpong && (h->it & 1);
+  for (int a = 0; a < h->ndim; ++a)
+    for (int v = 0; v < H.nvar; ++v) {
+      const size_t n = slab_floats(h, a);
+      const float* src = slab_ptr((v < 3 && odd) ? h->slabs1 : h->slabs, a, v);
+      if (n) CK(cudaMemcpyAsync(out, src, n * fs, cudaMemcpyDeviceToHost, h->stream));
+      out += n * fs;
+    }
+  const size_t it = h->it, ns = h->p.nstep;
+  if (h->nrec > 0 && it > 0)
+    CK(cudaMemcpy2DAsync(out, fs * it, h->seis, fs * ns, fs * it, size_t(3) * h->nrec, cudaMemcpyDeviceToHost,
+                         h->stream));
+  out += size_t(3) * h->nrec * it * fs;
+  if (it > 0) {
+    for (double* src : {h->ek, h->ep, h->vmax}) {
+      CK(cudaMemcpyAsync(out, src, it * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      out += it * sizeof(double);
+    }
+    CK(cudaMemcpyAsync(out, h->bad, it * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return CPML_OK;
+}
+
+int cpml_load_state(cpml_handle* h, const void* buf, size_t bytes) {
+  if (!h || !buf || bytes < sizeof(StateHeader)) return CPML_ERR_INVALID;
+  StateHeader H;
+  std::memcpy(&H, buf, sizeof(H));
+  const int nf = state_nfield(h);
+  bool ok = std::memcmp(H.magic, kStateMagic, 8) == 0 && H.version == kStateVersion && H.ndim == h->ndim &&
+            H.nx == h->nx && H.ny == h->ny && H.nz == h->nz && H.npml == h->p.npoints_pml &&
+            H.nstep == h->p.nstep && H.nrec == h->nrec && H.het == (h->het ? 1 : 0) && H.nfield == nf &&
+            H.nvar == (h->ndim == 3 ? 6 : 4) && H.it >= 0 && H.it <= h->p.nstep &&
+            H.param_hash == param_hash(h) && H.model_hash == h->model_hash && H.rec_hash == rec_hash(h);
+  for (int a = 0; a < 3 && ok; ++a) ok = H.slab_w[a] == (a < h->ndim ? h->axes[a].width() : 0);
+  if (!ok) return CPML_ERR_INVALID;
+  if (H.bytes != state_bytes(h, H.it) || bytes < H.bytes) return CPML_ERR_INVALID;
+  int st;
+  if ((st = zero_state(h))) return st;   // clears records beyond it, the step counter and the error word
+  h->it = H.it;
+  h->last_vmax = H.last_vmax;
+  const char* in = static_cast<const char*>(buf) + sizeof(H);
+  const size_t fs = sizeof(float), ncell = size_t(h->nx) * h->ny * h->nz;
+  // both buffer sets of the fused path get the snapshot (the write set is
+  // overwritten by the next step anyway)
+  float* F[2][10];
+  state_fields(h, 0, F[0]);
+  const bool two = h->pingpong;
+  if (two) state_fields(h, 1, F[1]);
+  for (int q = 0; q < nf; ++q) {
+    for (int set = 0; set < (two ? 2 : 1); ++set)
+      CK(cudaMemcpy2DAsync(F[set][q], fs * h->px, in, fs * h->nx, fs * h->nx, size_t(h->ny) * h->nz,
+                           cudaMemcpyHostToDevice, h->stream));
+    in += ncell * fs;
+  }
+  for (int a = 0; a < h->ndim; ++a)
+    for (int v = 0; v < H.nvar; ++v) {
+      const size_t n = slab_floats(h, a);
+      for (const Slabs* S : {&h->slabs, &h->slabs1}) {
+        float* dst = slab_ptr(*S, a, v);
+        if (n && dst) CK(cudaMemcpyAsync(dst, in, n * fs, cudaMemcpyHostToDevice, h->stream));
+      }
+      in += n * fs;
+    }
+  const size_t it = H.it, ns = h->p.nstep;
+  if (h->nrec > 0 && it > 0)
+    CK(cudaMemcpy2DAsync(h->seis, fs * ns, in, fs * it, fs * it, size_t(3) * h->nrec, cudaMemcpyHostToDevice,
+                         h->stream));
+  in += size_t(3) * h->nrec * it * fs;
+  if (it > 0) {
+    for (double* dst : {h->ek, h->ep, h->vmax}) {
+      CK(cudaMemcpyAsync(dst, in, it * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      in += it * sizeof(double);
+    }
+    CK(cudaMemcpyAsync(h->bad, in, it * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  }
+  const int itv = H.it;
+  CK(cudaMemcpyAsync(h->it_base, &itv, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return CPML_OK;
 }
@@ -761,23 +1038,26 @@ int cpml_get_plane(cpml_handle* h, int field, int axis, int index, float* out) {
   const int n[3] = {h->nx, h->ny, h->nz};
   if (index < 1 || index > n[axis]) return CPML_ERR_INVALID;
   const size_t fs = sizeof(float);
-  if (axis == 2) {         // [j][i]
-    CK(cudaMemcpy2DAsync(out, fs * h->nx, f + size_t(index - 1) * h->plane, fs * h->px, fs * h->nx,
-                         h->ny, cudaMemcpyDeviceToHost, h->stream));
-  } else if (axis == 1) {  // [k][i]
-    CK(cudaMemcpy2DAsync(out, fs * h->nx, f + size_t(index - 1) * h->px, fs * h->plane, fs * h->nx,
-                         h->nz, cudaMemcpyDeviceToHost, h->stream));
-  } else {                 // [k][j]
-    CK(cudaMemcpy2DAsync(out, fs, f + (index - 1), fs * h->px, fs, size_t(h->ny) * h->nz,
-                         cudaMemcpyDeviceToHost, h->stream));
-  }
+  auto copy = [&](float* dst, const float* src) {
+    if (axis == 2)         // [j][i]
+      return cudaMemcpy2DAsync(dst, fs * h->nx, src + size_t(index - 1) * h->plane, fs * h->px, fs * h->nx,
+                               h->ny, cudaMemcpyDeviceToHost, h->stream);
+    if (axis == 1)         // [k][i]
+      return cudaMemcpy2DAsync(dst, fs * h->nx, src + size_t(index - 1) * h->px, fs * h->plane, fs * h->nx,
+                               h->nz, cudaMemcpyDeviceToHost, h->stream);
+    return cudaMemcpy2DAsync(dst, fs, src + (index - 1), fs * h->px, fs, size_t(h->ny) * h->nz,  // [k][j]
+                             cudaMemcpyDeviceToHost, h->stream);
+  };
+  CK(copy(out, f));
   CK(cudaStreamSynchronize(h->stream));
-  return CPML_OK;
+  const size_t np = axis == 2 ? size_t(h->nx) * h->ny : (axis == 1 ? size_t(h->nx) * h->nz : size_t(h->ny) * h->nz);
+  return add_split_part(h, field, np, out, copy);
 }
 
 double cpml_algorithmic_bytes_per_step(cpml_handle* h) {
   if (!h) return 0.0;
   const double ncell = double(h->nx) * h->ny * h->nz;
+  if (is_split(h)) return 8.0 * 10 * ncell;   // ten split fields read and written once
   const int nfield = h->ndim == 3 ? 9 : 5;
   double bytes = 8.0 * nfield * ncell + (h->het ? 12.0 * ncell : 0.0);
   const int nax = h->ndim;
@@ -809,7 +1089,7 @@ int cpml_last_run_ms(cpml_handle* h, double* ms) {
 
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth) {
   if (!h || kernel < 0 || kernel > 3) return CPML_ERR_INVALID;
-  if ((kernel == CPML_KERNEL_FUSED && h->ndim != 3) || (kernel == CPML_KERNEL_PERSISTENT && h->ndim != 2))
+  if ((kernel == CPML_KERNEL_FUSED && h->ndim != 3) || (kernel == CPML_KERNEL_PERSISTENT && !is_standard2d(h)))
     return CPML_ERR_INVALID;
   if (zchunk < 2 || !fused3d_shape_ok(tile_y, depth)) return CPML_ERR_INVALID;
   if (h->it != 0) return CPML_ERR_INVALID;  // only on a fresh or reset handle
@@ -900,7 +1180,7 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
       for (int ty : {8, 16})
         for (int lz : {16, 24, 32, 48, 64}) cand.push_back(TuneVal{CPML_KERNEL_FUSED, ty, lz, 2, 0.0});
     cand.push_back(TuneVal{CPML_KERNEL_TWO_SWEEP, 8, 32, 2, 0.0});
-    if (h->ndim == 2) {
+    if (is_standard2d(h)) {
       if (persist2d_grid(make_args(h), h->het) > 0) cand.push_back(TuneVal{CPML_KERNEL_PERSISTENT, 8, 32, 2, 0.0});
     }
     const int flags = h->p.flags;

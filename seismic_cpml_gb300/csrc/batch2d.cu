@@ -28,10 +28,6 @@
 
 namespace cpml {
 
-struct ProfileArgs {
-  int n, npml, use_min, use_max;
-  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
-};
 void launch_build_profile(const ProfileArgs& P, double* out64, float* out32, cudaStream_t st);
 
 constexpr int BTX = 32, BTY = 8, BNT = BTX * BTY;
@@ -228,6 +224,7 @@ int brealloc(cpml_batch* b, T** slot, size_t n) {
 int shot_axis(cpml_batch* b, const cpml_params& p, int axis, int n, double delta, Axis* A) {
   ProfileArgs P{};
   P.n = n; P.npml = p.npoints_pml; P.use_min = p.use_pml[2 * axis]; P.use_max = p.use_pml[2 * axis + 1];
+  P.high_cells = n - 1;
   P.delta = delta; P.cp = p.cp; P.f0 = p.f0; P.dt = p.deltat; P.npower = p.npower; P.kmax = p.k_max_pml;
   P.amax = p.alpha_max_pml < 0 ? 2.0 * kPi * (p.f0 / 2.0) : p.alpha_max_pml;
   P.rcoef = p.rcoef;

@@ -93,6 +93,17 @@ struct StepArgs {
   int nblocks;             // blocks of the velocity kernel
   int ep_physical;         // 3D: textbook Ep instead of the reference's
   int* err;                // device error word (bounded waits that gave up)
+  float o24dx, o24dy;      // 2D fourth order: 1 / (24 DELTA) (2D4:565-566)
+  int split;               // 2D split-field PML: f holds the x parts, g the y parts
+  float lam_split, mu_split, l2m_split, orho_split;  // its homogeneous model (PML:106-111)
+};
+
+// Inputs of the FP64 C-PML profile builder of one axis (support.cu).
+struct ProfileArgs {
+  int n, npml, use_min, use_max;
+  int high_cells;  // high-side origin = high_cells * delta - thickness (n - 1; n on the
+                   // y axis of the fourth-order program, 2D4:401)
+  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
 };
 
 // Linear index helpers

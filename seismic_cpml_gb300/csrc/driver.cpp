@@ -136,6 +136,20 @@ void write_gnuplot(const std::string& dir, bool three_d, int nrec) {
     std::fprintf(f, " pause -1 \"Hit any key...\"\n\n");
     std::fclose(f);
   }
+  if (!three_d) {
+    // energy of this run against the classical split-field PML run of the
+    // Collino program in ../collino (2D:764-777)
+    f = std::fopen((dir + "/plot_comparison").c_str(), "w");
+    if (f) {
+      std::fprintf(f, " # set term x11\n set term postscript landscape monochrome dashed \"Helvetica\" 22\n\n"
+                      " set xlabel \"Time (s)\"\n set ylabel \"Total energy\"\n\n"
+                      " set output \"compare_total_energy_semilog.eps\"\n set logscale y\n"
+                      " plot \"energy.dat\" us 1:4 t 'Total energy CPML' w l lc 1, "
+                      "\"../collino/energy.dat\" us 1:4 t 'Total energy Collino' w l lc 2\n"
+                      " pause -1 \"Hit any key...\"\n\n");
+      std::fclose(f);
+    }
+  }
   f = std::fopen((dir + "/plotgnu").c_str(), "w");
   if (f) {
     std::fprintf(f, " set term x11\n # set term postscript landscape monochrome dashed \"Helvetica\" 22\n\n"

@@ -4,6 +4,7 @@
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -96,6 +97,23 @@ int cpml_params_default_3d(cpml_params* p) {
   return CPML_OK;
 }
 
+int cpml_params_default_2d_fourth(cpml_params* p) {
+  if (!p) return CPML_ERR_INVALID;
+  cpml_params_default_2d(p);
+  p->order = 4;
+  p->nstep = 2000 * 2;                                   // 2D4:156
+  p->deltat = 2.0e-3 / 2;                                // 2D4:162
+  p->it_display = 100 * 2;                               // 2D4:187
+  return CPML_OK;
+}
+
+int cpml_params_default_2d_split(cpml_params* p) {
+  if (!p) return CPML_ERR_INVALID;
+  cpml_params_default_2d(p);                             // PML:96-141 share the 2D block
+  p->scheme = CPML_SCHEME_SPLIT;
+  return CPML_OK;
+}
+
 double cpml_courant(const cpml_params* p, double cp_max) {
   if (!p) return NAN;
   double s = 1.0 / (p->deltax * p->deltax) + 1.0 / (p->deltay * p->deltay);
@@ -124,11 +142,41 @@ int cpml_pml_profile(const cpml_params* p, int axis, int n, double* d, double* K
                      double* bh) {
   if (!p || axis < 0 || axis > 2 || n < 1 || p->npoints_pml < 1) return CPML_ERR_INVALID;
   const double delta = axis == 0 ? p->deltax : (axis == 1 ? p->deltay : p->deltaz);
+  if (p->scheme == CPML_SCHEME_SPLIT) {
+    // split-field damping divided by two (PML:180-250); K = 1, alpha = a = 0, b = 1
+    const double th = p->npoints_pml * delta;
+    const double d0 = 3.0 * p->cp * std::log(1.0 / p->rcoef) / (2.0 * th);
+    const double ol = th, orr = (n - 1) * delta - th;
+    for (int i = 0; i < n; ++i) {
+      const double x = delta * double(i);
+      double f = 0.0, g = 0.0;
+      if (x < ol) {
+        f = d0 * std::pow((ol - x) / th, 2);
+        g = d0 * std::pow((ol - x - delta / 2.0) / th, 2);
+      } else if (x >= 0.9999 * orr) {
+        f = d0 * std::pow((x - orr) / th, 2);
+        g = d0 * std::pow((x + delta / 2.0 - orr) / th, 2);
+      }
+      if (d) d[i] = f / 2.0;
+      if (dh) dh[i] = g / 2.0;
+      if (K) K[i] = 1.0;
+      if (Kh) Kh[i] = 1.0;
+      if (alpha) alpha[i] = 0.0;
+      if (alphah) alphah[i] = 0.0;
+      if (a) a[i] = 0.0;
+      if (ah) ah[i] = 0.0;
+      if (b) b[i] = 1.0;
+      if (bh) bh[i] = 1.0;
+    }
+    return CPML_OK;
+  }
   const bool umin = p->use_pml[2 * axis] != 0, umax = p->use_pml[2 * axis + 1] != 0;
   const double amax = p->alpha_max_pml < 0 ? 2.0 * kPi * (p->f0 / 2.0) : p->alpha_max_pml;
   const double th = p->npoints_pml * delta;
   const double d0 = -(p->npower + 1) * p->cp * std::log(p->rcoef) / (2.0 * th);
-  const double ol = th, orr = (n - 1) * delta - th;
+  // the fourth-order program's y origin is one cell further out (2D4:401)
+  const int high = (p->ndim == 2 && p->order == 4 && axis == 1) ? n : n - 1;
+  const double ol = th, orr = high * delta - th;
   for (int i = 0; i < n; ++i) {
     double vd = 0, vK = 1, va = 0, vdh = 0, vKh = 1, vah = 0;
     const double val = delta * double(i);
@@ -198,6 +246,35 @@ int cpml_write_seismograms(const char* dir, const double* vx, const double* vy, 
       }
       if (std::fclose(f) != 0) return CPML_ERR_IO;
     }
+  }
+  return CPML_OK;
+}
+
+int cpml_write_seismograms_su(const char* dir, const double* vx, const double* vy, const double* vz,
+                              int nt, int nrec, double deltat) {
+  if (nt < 1 || nrec < 0 || !vx || !vy || !(deltat > 0)) return CPML_ERR_INVALID;
+  // the header's sample count and interval are 16-bit integers
+  // (integer(2) head(1:120), head(58) = nstep, head(59) = deltat*1e6)
+  const double dt_us = std::trunc(deltat * 1.0e6);
+  if (nt > 32767 || dt_us > 32767.0 || dt_us < 1.0) return CPML_ERR_RANGE;
+  int16_t head[120];
+  std::memset(head, 0, sizeof head);
+  head[57] = (int16_t)nt;
+  head[58] = (int16_t)dt_us;
+  const double* comp[3] = {vx, vy, vz};
+  const char* name[3] = {"seisVx.su", "seisVy.su", "seisVz.su"};
+  std::vector<float> trace(nt);
+  for (int c = 0; c < 3; ++c) {
+    if (!comp[c]) continue;
+    FILE* f = std::fopen(join(dir, name[c]).c_str(), "wb");
+    if (!f) return CPML_ERR_IO;
+    bool ok = true;
+    for (int r = 0; r < nrec && ok; ++r) {   // one header + nt REAL(4) samples per receiver
+      for (int it = 0; it < nt; ++it) trace[it] = (float)comp[c][size_t(r) * nt + it];
+      ok = std::fwrite(head, sizeof head, 1, f) == 1 &&
+           std::fwrite(trace.data(), sizeof(float), size_t(nt), f) == size_t(nt);
+    }
+    if (std::fclose(f) != 0 || !ok) return CPML_ERR_IO;
   }
   return CPML_OK;
 }

@@ -15,10 +15,6 @@
 
 namespace cpml {
 
-struct ProfileArgs {
-  int n, npml, use_min, use_max;
-  double delta, cp, f0, dt, npower, kmax, amax, rcoef;
-};
 
 // One thread per grid index: full point and half point.
 __global__ void build_profile_kernel(ProfileArgs P, double* __restrict__ out64,
@@ -27,7 +23,7 @@ __global__ void build_profile_kernel(ProfileArgs P, double* __restrict__ out64,
   if (i >= P.n) return;
   const double th = P.npml * P.delta;
   const double d0 = -(P.npower + 1) * P.cp * log(P.rcoef) / (2.0 * th);
-  const double ol = th, orr = (P.n - 1) * P.delta - th;
+  const double ol = th, orr = P.high_cells * P.delta - th;
   const double val = P.delta * double(i);
   double d = 0, K = 1, al = 0, dh = 0, Kh = 1, alh = 0;
   if (P.use_min) {
@@ -75,8 +71,8 @@ reduce_chunk_kernel(StepArgs s, int C, double* __restrict__ ek_out, double* __re
     for (int r = threadIdx.x; r < s.nrec; r += blockDim.x) {
       const long long c = s.rec_cell[r];
       const size_t o = (size_t)r * s.nstep + (size_t)(it - 1);
-      s.seis[o] = s.f.vx[c];
-      s.seis[slab + o] = s.f.vy[c];
+      s.seis[o] = s.split ? __fadd_rn(s.f.vx[c], s.g.vx[c]) : s.f.vx[c];
+      s.seis[slab + o] = s.split ? __fadd_rn(s.f.vy[c], s.g.vy[c]) : s.f.vy[c];
       if (s.f.vz) s.seis[2 * slab + o] = s.f.vz[c];
     }
     return;

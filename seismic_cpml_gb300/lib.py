@@ -25,6 +25,8 @@ _h = ctypes.c_void_p
 SIGNATURES = [
     ("cpml_params_default_2d", ctypes.c_int, [_P(CpmlParams)]),
     ("cpml_params_default_3d", ctypes.c_int, [_P(CpmlParams)]),
+    ("cpml_params_default_2d_fourth", ctypes.c_int, [_P(CpmlParams)]),
+    ("cpml_params_default_2d_split", ctypes.c_int, [_P(CpmlParams)]),
     ("cpml_courant", ctypes.c_double, [_P(CpmlParams), ctypes.c_double]),
     ("cpml_nearest_gridpoint", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -41,6 +43,9 @@ SIGNATURES = [
     ("cpml_get_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
     ("cpml_get_plane", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp]),
     ("cpml_set_field", ctypes.c_int, [_h, ctypes.c_int, _fp]),
+    ("cpml_state_size", ctypes.c_int, [_h, _P(ctypes.c_size_t)]),
+    ("cpml_save_state", ctypes.c_int, [_h, _vp, ctypes.c_size_t]),
+    ("cpml_load_state", ctypes.c_int, [_h, _vp, ctypes.c_size_t]),
     ("cpml_algorithmic_bytes_per_step", ctypes.c_double, [_h]),
     ("cpml_last_run_ms", ctypes.c_int, [_h, _dp]),
     ("cpml_get_stream", ctypes.c_int, [_h, _P(ctypes.c_void_p)]),
@@ -85,6 +90,8 @@ SIGNATURES = [
      + [ctypes.c_int, ctypes.c_float, _vp]),
     ("cpml_write_seismograms", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_double]),
+    ("cpml_write_seismograms_su", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, _dp, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_double]),
     ("cpml_write_energy", ctypes.c_int, [ctypes.c_char_p, _dp, _dp, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_int]),
     ("cpml_write_pnm", ctypes.c_int, [ctypes.c_char_p, _fp, ctypes.c_int, ctypes.c_int,

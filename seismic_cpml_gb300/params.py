@@ -13,6 +13,7 @@ import ctypes
 import math
 
 STF_DGAUSSIAN, STF_GAUSSIAN, STF_RICKER = 0, 1, 2
+SCHEME_CPML, SCHEME_SPLIT = 0, 1
 FLAG_ENERGY, FLAG_EP_PHYSICAL, FLAG_NO_STABILITY = 0x1, 0x2, 0x4
 
 FIELDS = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "syy": 4, "szz": 5,
@@ -31,7 +32,9 @@ class CpmlParams(ctypes.Structure):
         ("stf", ctypes.c_int32),
         ("it_display", ctypes.c_int32),
         ("flags", ctypes.c_int32),
-        ("reserved_i", ctypes.c_int32 * 4),
+        ("order", ctypes.c_int32),
+        ("scheme", ctypes.c_int32),
+        ("reserved_i", ctypes.c_int32 * 2),
         ("deltax", ctypes.c_double), ("deltay", ctypes.c_double), ("deltaz", ctypes.c_double),
         ("deltat", ctypes.c_double),
         ("cp", ctypes.c_double), ("cs", ctypes.c_double), ("rho", ctypes.c_double),
@@ -99,6 +102,27 @@ def default_2d() -> CpmlParams:
     p.k_max_pml = 1.0
     p.alpha_max_pml = -1.0            # => 2*pi*(f0/2) (2D:218)
     p.rcoef = 0.001
+    return p
+
+
+def default_2d_fourth() -> CpmlParams:
+    """seismic_CPML_2D_isotropic_fourth_order.f90:132-190: the second-order
+    program's block with the 27/24 fourth-order operator, DELTAT halved and
+    NSTEP, IT_DISPLAY doubled."""
+    p = default_2d()
+    p.order = 4
+    p.nstep = 2000 * 2
+    p.deltat = 2.0e-3 / 2
+    p.it_display = 100 * 2
+    return p
+
+
+def default_2d_split() -> CpmlParams:
+    """seismic_PML_Collino_2D_isotropic.f90:96-141: classical split-field PML,
+    homogeneous, h = 10 m, 2000 steps of 2 ms, first derivative of a
+    Gaussian at (80, 428), 135 degrees."""
+    p = default_2d()
+    p.scheme = SCHEME_SPLIT
     return p
 
 

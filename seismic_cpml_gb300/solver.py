@@ -142,6 +142,23 @@ class Solver:
         a = _f32(arr).reshape(self.shape)
         _L.check(self.L.cpml_set_field(self.h, FIELDS[name], a.ctypes.data_as(_fp)), "set_field")
 
+    # -- checkpoint / restart ---------------------------------------------
+    def save_state(self) -> np.ndarray:
+        """Snapshot of the time loop's state (cpml_save_state) as a uint8 array."""
+        n = ctypes.c_size_t()
+        _L.check(self.L.cpml_state_size(self.h, ctypes.byref(n)), "cpml_state_size")
+        buf = np.zeros(n.value, np.uint8)
+        _L.check(self.L.cpml_save_state(self.h, buf.ctypes.data_as(ctypes.c_void_p), n.value),
+                 "cpml_save_state")
+        return buf
+
+    def load_state(self, buf) -> None:
+        """Restore a snapshot made by save_state on a handle of the same
+        parameters, model and receivers (cpml_load_state)."""
+        b = np.ascontiguousarray(buf, dtype=np.uint8)
+        _L.check(self.L.cpml_load_state(self.h, b.ctypes.data_as(ctypes.c_void_p), b.size),
+                 "cpml_load_state")
+
     def plane(self, name: str, axis: int, index: int) -> np.ndarray:
         dims = list(self.shape) if self.p.ndim == 3 else [1] + list(self.shape)
         nz, ny, nx = dims

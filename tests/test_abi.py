@@ -43,7 +43,9 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_default_parameter_blocks_match_the_mirror(lib):
     for fn, mirror in ((lib.cpml_params_default_2d, P.default_2d),
-                       (lib.cpml_params_default_3d, P.default_3d)):
+                       (lib.cpml_params_default_3d, P.default_3d),
+                       (lib.cpml_params_default_2d_fourth, P.default_2d_fourth),
+                       (lib.cpml_params_default_2d_split, P.default_2d_split)):
         c = P.CpmlParams()
         assert fn(ctypes.byref(c)) == 0
         m = mirror()
@@ -76,6 +78,39 @@ def test_pml_profile_matches_oracle(lib):
         keys = ["d", "K", "alpha", "a", "b", "d_half", "K_half", "alpha_half", "a_half", "b_half"]
         for q, k in enumerate(keys):
             assert np.array_equal(arrs[q], ref[k]), (axis, k)
+
+
+@pytest.mark.parametrize("program", ["fourth_order", "split_pml"])
+def test_pml_profile_of_the_other_2d_programs(lib, program):
+    """The host profile entry point follows each program's own profile: the
+    fourth-order y origin (2D4:401) and the split-field damping divided by two
+    (PML:180-250), against both oracle restatements."""
+    p = P.default_2d_fourth() if program == "fourth_order" else P.default_2d_split()
+    for axis, n in enumerate((p.nx, p.ny)):
+        arrs = [np.zeros(n) for _ in range(10)]
+        assert lib.cpml_pml_profile(ctypes.byref(p), axis, n, *[a.ctypes.data_as(_dp) for a in arrs]) == 0
+        if program == "fourth_order":
+            ref = oracle_c.profile(p, axis)
+            keys = ["d", "K", "alpha", "a", "b", "d_half", "K_half", "alpha_half", "a_half", "b_half"]
+            for q, k in enumerate(keys):
+                assert np.array_equal(arrs[q], ref[k]), (axis, k)
+            pn = oracle_np.pml_profile(n, 10.0, p.npoints_pml, True, True, p.cp, p.f0, p.deltat,
+                                       high_origin_cells=n if axis == 1 else None)
+            assert np.allclose(arrs[0], pn["d"], rtol=1e-14, atol=0)
+        else:
+            f, g = oracle_np.split_profile(n, 10.0, p.npoints_pml, p.cp, p.rcoef)
+            assert np.allclose(arrs[0], f, rtol=1e-14, atol=0) and np.allclose(arrs[5], g, rtol=1e-14, atol=0)
+            assert np.all(arrs[1] == 1.0) and np.all(arrs[3] == 0.0) and f[0] > 0 and f[50] == 0
+
+
+def test_create_validates_the_other_2d_programs(lib):
+    h = ctypes.c_void_p()
+    for mk, field, value in ((P.default_2d_fourth, "order", 3), (P.default_2d_split, "scheme", 2),
+                             (P.default_2d_split, "deltay", 12.0), (P.default_2d_split, "order", 4),
+                             (P.default_3d, "order", 4), (P.default_3d, "scheme", 1)):
+        q = mk()
+        setattr(q, field, value)
+        assert lib.cpml_create(ctypes.byref(q), ctypes.byref(h)) == -1, (mk.__name__, field)
 
 
 def test_strerror_covers_all_codes(lib):
@@ -112,6 +147,44 @@ def test_noalloc_rejects_oversize_before_any_device_call(lib):
                                      1, None) == -9
     assert lib.cpml_energy3d_noalloc(None, 8, 8, 8, 8, 2, 1e9, 1e9, 2e3, None, None, None, 0,
                                      1, None) == -1
+
+
+@pytest.mark.parametrize("dims", [(1, 8, 30), (8, 4, 30), (8, 8, 4), (20, 20, 20)])
+def test_noalloc_rejects_an_empty_energy_interior(lib, dims):
+    """2*npml >= nx, ny or nz leaves no interior cell: CPML_ERR_INVALID before
+    any device call (the fake pointers are never dereferenced)."""
+    nx, ny, nz = dims
+    ptrs = (ctypes.c_void_p * 9)(*([1] * 9))
+    assert lib.cpml_energy3d_noalloc(ptrs, nx, ny, nz, nx, 10 if nx == 20 else 2, 1e9, 1e9, 2e3,
+                                     None, None, None, 0, 1, None) == -1
+
+
+def test_noalloc_rejects_a_partial_model_triple(lib):
+    ptrs = (ctypes.c_void_p * 9)(*([1] * 9))
+    for cells in ((1, None, None), (None, 1, None), (1, 1, None), (None, None, 1)):
+        assert lib.cpml_energy3d_noalloc(ptrs, 8, 8, 8, 8, 2, 1e9, 1e9, 2e3, *cells, 0, 1, None) == -1
+
+
+def test_su_seismogram_writer(lib, tmp_path):
+    """seisVx.su / seisVy.su / seisVz.su: per receiver 120 int16 header words
+    (word 58 = samples, word 59 = interval in microseconds) and the samples as
+    REAL(4), the layout of the reference's SU output."""
+    nt, nrec, dt = 11, 3, 4.0e-4
+    vx = np.arange(nt * nrec, dtype=np.float64).reshape(nrec, nt) * 1e-3 - 0.01
+    vy, vz = -vx, 2.0 * vx
+    d = str(tmp_path).encode()
+    assert lib.cpml_write_seismograms_su(d, vx.ctypes.data_as(_dp), vy.ctypes.data_as(_dp),
+                                         vz.ctypes.data_as(_dp), nt, nrec, dt) == 0
+    rec_t = np.dtype([("head", "<i2" if np.little_endian else ">i2", (120,)), ("data", "=f4", (nt,))])
+    for name, ref in (("seisVx.su", vx), ("seisVy.su", vy), ("seisVz.su", vz)):
+        raw = (tmp_path / name).read_bytes()
+        assert len(raw) == nrec * (240 + 4 * nt)
+        recs = np.frombuffer(raw, dtype=rec_t)
+        assert np.all(recs["head"][:, 57] == nt) and np.all(recs["head"][:, 58] == 400)
+        assert np.count_nonzero(recs["head"]) == 2 * nrec
+        assert np.array_equal(recs["data"], ref.astype(np.float32))
+    assert lib.cpml_write_seismograms_su(d, vx.ctypes.data_as(_dp), vy.ctypes.data_as(_dp), None,
+                                         40000, 1, dt) == -9
 
 
 def test_seismogram_and_energy_writers(lib, tmp_path):

@@ -37,6 +37,52 @@ def test_two_restatements_agree(ndim, het):
     assert np.allclose(a.ek, b.ek, rtol=1e-12, atol=0) and np.allclose(a.ep, b.ep, rtol=1e-12, atol=0)
 
 
+@pytest.mark.parametrize("program", ["fourth_order", "fourth_order_het", "split_pml"])
+def test_two_restatements_agree_on_the_other_2d_programs(program):
+    """seismic_CPML_2D_isotropic_fourth_order.f90 and
+    seismic_PML_Collino_2D_isotropic.f90: the C++ restatement (ghost reads
+    through a bounds test; split parts as separate arrays) and the numpy one
+    (arrays held with the reference's ghost layer; sliced updates) agree."""
+    p, rec = P.small_2d(nstep=150)
+    kw = {}
+    if program.startswith("fourth"):
+        p.order = 4
+        p.deltat = 1.0e-3
+        if program.endswith("het"):
+            m = layered_2d(p, seed=4)
+            kw = dict(lam=m[0], mu=m[1], rho=m[2])
+        b = oracle_np.run2d4(p, rec=rec, keep_fields=True, **kw)
+    else:
+        p.scheme = P.SCHEME_SPLIT
+        b = oracle_np.run_split(p, rec=rec, keep_fields=True)
+    a = oracle_c.run(p, rec=rec, keep_fields=True, **kw)
+    for name, f in b.fields.items():
+        assert np.array_equal(a.fields[name], f), name
+    assert np.array_equal(a.sisvx, b.sisvx) and np.array_equal(a.sisvy, b.sisvy)
+    assert np.abs(a.sisvx).max() > 0
+    assert np.allclose(a.ek, b.ek, rtol=1e-12, atol=0) and np.allclose(a.ep, b.ep, rtol=1e-12, atol=0)
+
+
+def test_fourth_order_program_details():
+    """The fourth-order program's y profile starts its high-side C-PML one
+    cell further out (2D4:401) and its x profile does not; a split-field
+    handle refuses a per-cell model."""
+    p = P.default_2d_fourth()
+    q = P.default_2d()
+    y4, y2 = oracle_c.profile(p, 1), oracle_c.profile(q, 1)
+    x4, x2 = oracle_c.profile(p, 0), oracle_c.profile(q, 0)
+    assert np.array_equal(x4["d"], x2["d"])
+    assert np.array_equal(y4["d"][:100], y2["d"][:100])
+    assert not np.array_equal(y4["d"][-12:], y2["d"][-12:])
+    n = p.ny
+    assert y4["d"][n - 1] < y2["d"][n - 1] and y4["d"][n - 10] == 0.0 < y2["d"][n - 10]
+    s = P.default_2d_split()
+    s.nx, s.ny, s.nstep = 30, 30, 2
+    s.isource, s.jsource = 15, 15
+    with pytest.raises(RuntimeError):
+        oracle_c.run(s, lam=np.ones((30, 30)))
+
+
 def test_restatements_agree_on_reference_flags():
     """3D energy quirk (3D:1170-1171) and its physical variant, both oracles."""
     p, rec = P.small_3d(nstep=40)

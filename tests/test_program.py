@@ -66,3 +66,5 @@ def test_program_2d_default_outputs(program, tmp_path, golden):
         assert (tmp_path / f"image{it:06d}_Vx.pnm").exists()
         assert (tmp_path / f"image{it:06d}_Vy.pnm").exists()
     assert (tmp_path / "plotgnu").exists() and (tmp_path / "plot_energy").exists()
+    cmp_script = (tmp_path / "plot_comparison").read_text()   # 2D:764-777
+    assert '"../collino/energy.dat" us 1:4' in cmp_script and "compare_total_energy_semilog.eps" in cmp_script
