@@ -42,8 +42,9 @@ def _case(name):
 def _results(s, names):
     vx, vy, vz = s.seismograms()
     ek, ep = s.energy()
-    return dict(vx=vx, vy=vy, vz=vz, ek=ek, ep=ep, status=s.status(),
-                **{n: s.field(n) for n in names})
+    out = dict(vx=vx, vy=vy, vz=vz, ek=ek, ep=ep, status=s.status())
+    out.update({"field_" + n: s.field(n) for n in names})
+    return out
 
 
 CASES = ["2d", "2d_het", "2d_persistent", "2d_order4_het", "2d_split", "3d_fused", "3d_fused_het",
