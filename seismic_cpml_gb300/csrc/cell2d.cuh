@@ -44,72 +44,116 @@ struct Shot2D {
   const float* src_fy;
 };
 
+// Where a cell update finds the fields, the per-cell model and the memory
+// variables it touches. GlobalView is a shot's own arrays in HBM; a kernel
+// that stages a region in shared memory supplies its own view. The update
+// functions below are the same source for every view, so the arithmetic
+// (and every rounding) is identical wherever the state lives.
+struct GlobalView {
+  const Shot2D& s;
+  __device__ __forceinline__ float* vx() const { return s.vx; }
+  __device__ __forceinline__ float* vy() const { return s.vy; }
+  __device__ __forceinline__ float* sxx() const { return s.sxx; }
+  __device__ __forceinline__ float* syy() const { return s.syy; }
+  __device__ __forceinline__ float* sxy() const { return s.sxy; }
+  __device__ __forceinline__ const float* lam() const { return s.lam; }
+  __device__ __forceinline__ const float* mu() const { return s.mu; }
+  __device__ __forceinline__ const float* rho() const { return s.rho; }
+  __device__ __forceinline__ float* mx(int q) const { return s.mx[q]; }
+  __device__ __forceinline__ float* my(int q) const { return s.my[q]; }
+  __device__ __forceinline__ long long pitch() const { return s.px; }
+  __device__ __forceinline__ long long at(int i, int j) const { return (long long)j * s.px + i; }
+  __device__ __forceinline__ long long mxi(int i, int j, int sx) const {
+    (void)i;
+    return (long long)j * s.ax.width() + sx;
+  }
+  __device__ __forceinline__ long long myi(int i, int j, int sy) const {
+    (void)j;
+    return (long long)sy * s.px + i;
+  }
+};
+
 // Stress update of cell (i, j), 0-based.
-template <bool HET>
-__device__ __forceinline__ void stress2d_cell(const Shot2D& s, int i, int j) {
+template <bool HET, class V>
+__device__ __forceinline__ void stress2d_cell(const Shot2D& s, const V& v, int i, int j) {
   const int sx = s.ax.slab(i), sy = s.ay.slab(j);
-  const long long px = s.px;
-  const long long c = (long long)j * px + i;
-  const long long mx = (long long)j * s.ax.width() + sx;
-  const long long my = (long long)sy * px + i;
-  const float vxc = s.vx[c], vyc = s.vy[c];
+  const long long px = v.pitch();
+  const long long c = v.at(i, j);
+  const long long mx = v.mxi(i, j, sx);
+  const long long my = v.myi(i, j, sy);
+  float* const VX = v.vx();
+  float* const VY = v.vy();
+  const float vxc = VX[c], vyc = VY[c];
   // sigma_xx, sigma_yy: j = 2..NY, i = 1..NX-1
   if (j >= 1 && i <= s.nx - 2) {
-    float d1 = __fmul_rn(__fsub_rn(s.vx[c + 1], vxc), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(vyc, s.vy[c - px]), s.ody);
-    d1 = pml2(d1, sx, s.mx[0], mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-    d2 = pml2(d2, sy, s.my[1], my, s.ay.a, s.ay.b, s.ay.ik, j);
+    float d1 = __fmul_rn(__fsub_rn(VX[c + 1], vxc), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(vyc, VY[c - px]), s.ody);
+    d1 = pml2(d1, sx, v.mx(0), mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
+    d2 = pml2(d2, sy, v.my(1), my, s.ay.a, s.ay.b, s.ay.ik, j);
     float dl = s.dt_lam, dl2m = s.dt_l2m;
     if (HET) {
-      const float lh = __fmul_rn(0.5f, __fadd_rn(s.lam[c + 1], s.lam[c]));
-      const float mh = __fmul_rn(0.5f, __fadd_rn(s.mu[c + 1], s.mu[c]));
+      const float lh = __fmul_rn(0.5f, __fadd_rn(v.lam()[c + 1], v.lam()[c]));
+      const float mh = __fmul_rn(0.5f, __fadd_rn(v.mu()[c + 1], v.mu()[c]));
       dl = __fmul_rn(s.dt, lh);
       dl2m = __fmul_rn(s.dt, fmaf(2.0f, mh, lh));
     }
-    s.sxx[c] = __fadd_rn(s.sxx[c], fmaf(dl2m, d1, __fmul_rn(dl, d2)));
-    s.syy[c] = __fadd_rn(s.syy[c], fmaf(dl, d1, __fmul_rn(dl2m, d2)));
+    float* const SXX = v.sxx();
+    float* const SYY = v.syy();
+    SXX[c] = __fadd_rn(SXX[c], fmaf(dl2m, d1, __fmul_rn(dl, d2)));
+    SYY[c] = __fadd_rn(SYY[c], fmaf(dl, d1, __fmul_rn(dl2m, d2)));
   }
   // sigma_xy: j = 1..NY-1, i = 2..NX
   if (j <= s.ny - 2 && i >= 1) {
-    float d1 = __fmul_rn(__fsub_rn(vyc, s.vy[c - 1]), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(s.vx[c + px], vxc), s.ody);
-    d1 = pml2(d1, sx, s.mx[1], mx, s.ax.a, s.ax.b, s.ax.ik, i);
-    d2 = pml2(d2, sy, s.my[0], my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
-    const float dm = HET ? __fmul_rn(s.dt, __fmul_rn(0.5f, __fadd_rn(s.mu[c + px], s.mu[c]))) : s.dt_mu;
-    s.sxy[c] = fmaf(dm, __fadd_rn(d1, d2), s.sxy[c]);
+    float d1 = __fmul_rn(__fsub_rn(vyc, VY[c - 1]), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(VX[c + px], vxc), s.ody);
+    d1 = pml2(d1, sx, v.mx(1), mx, s.ax.a, s.ax.b, s.ax.ik, i);
+    d2 = pml2(d2, sy, v.my(0), my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
+    const float dm = HET ? __fmul_rn(s.dt, __fmul_rn(0.5f, __fadd_rn(v.mu()[c + px], v.mu()[c]))) : s.dt_mu;
+    float* const SXY = v.sxy();
+    SXY[c] = fmaf(dm, __fadd_rn(d1, d2), SXY[c]);
   }
+}
+
+template <bool HET>
+__device__ __forceinline__ void stress2d_cell(const Shot2D& s, int i, int j) {
+  stress2d_cell<HET>(s, GlobalView{s}, i, j);
 }
 
 // Velocity update of cell (i, j) at 1-based step it, with source, rigid
 // edges, and the cell's energy and |v|^2 contributions.
-template <bool HET>
-__device__ __forceinline__ void velocity2d_cell(const Shot2D& s, int i, int j, int it, float& ek,
+template <bool HET, class V>
+__device__ __forceinline__ void velocity2d_cell(const Shot2D& s, const V& v, int i, int j, int it, float& ek,
                                                 float& ep, float& vm2, int& bad) {
   const int sx = s.ax.slab(i), sy = s.ay.slab(j);
-  const long long px = s.px;
-  const long long c = (long long)j * px + i;
-  const long long mx = (long long)j * s.ax.width() + sx;
-  const long long my = (long long)sy * px + i;
-  float vx = s.vx[c], vy = s.vy[c];
-  const float sxx = s.sxx[c], syy = s.syy[c], sxy = s.sxy[c];
+  const long long px = v.pitch();
+  const long long c = v.at(i, j);
+  const long long mx = v.mxi(i, j, sx);
+  const long long my = v.myi(i, j, sy);
+  float* const VX = v.vx();
+  float* const VY = v.vy();
+  const float* const SXX = v.sxx();
+  const float* const SYY = v.syy();
+  const float* const SXY = v.sxy();
+  float vx = VX[c], vy = VY[c];
+  const float sxx = SXX[c], syy = SYY[c], sxy = SXY[c];
   // v_x: j = 2..NY, i = 2..NX
   if (j >= 1 && i >= 1) {
-    float d1 = __fmul_rn(__fsub_rn(sxx, s.sxx[c - 1]), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(sxy, s.sxy[c - px]), s.ody);
-    d1 = pml2(d1, sx, s.mx[2], mx, s.ax.a, s.ax.b, s.ax.ik, i);
-    d2 = pml2(d2, sy, s.my[2], my, s.ay.a, s.ay.b, s.ay.ik, j);
-    const float f = HET ? __fdiv_rn(s.dt, s.rho[c]) : s.dt_over_rho;
+    float d1 = __fmul_rn(__fsub_rn(sxx, SXX[c - 1]), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(sxy, SXY[c - px]), s.ody);
+    d1 = pml2(d1, sx, v.mx(2), mx, s.ax.a, s.ax.b, s.ax.ik, i);
+    d2 = pml2(d2, sy, v.my(2), my, s.ay.a, s.ay.b, s.ay.ik, j);
+    const float f = HET ? __fdiv_rn(s.dt, v.rho()[c]) : s.dt_over_rho;
     vx = fmaf(__fadd_rn(d1, d2), f, vx);
   }
   // v_y: j = 1..NY-1, i = 1..NX-1
   if (j <= s.ny - 2 && i <= s.nx - 2) {
-    float d1 = __fmul_rn(__fsub_rn(s.sxy[c + 1], sxy), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(s.syy[c + px], syy), s.ody);
-    d1 = pml2(d1, sx, s.mx[3], mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-    d2 = pml2(d2, sy, s.my[3], my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
+    float d1 = __fmul_rn(__fsub_rn(SXY[c + 1], sxy), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(SYY[c + px], syy), s.ody);
+    d1 = pml2(d1, sx, v.mx(3), mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
+    d2 = pml2(d2, sy, v.my(3), my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
     float f = s.dt_over_rho;
     if (HET) {
-      const float* r = s.rho;
+      const float* r = v.rho();
       const float r4 = __fadd_rn(__fadd_rn(__fadd_rn(r[c], r[c + 1]), r[c + 1 + px]), r[c + px]);
       f = __fdiv_rn(s.dt, __fmul_rn(0.25f, r4));
     }
@@ -120,8 +164,8 @@ __device__ __forceinline__ void velocity2d_cell(const Shot2D& s, int i, int j, i
     vy = __fadd_rn(vy, s.src_fy[it - 1]);
   }
   if (i == 0 || i == s.nx - 1 || j == 0 || j == s.ny - 1) { vx = 0.f; vy = 0.f; }  // 2D:670-680
-  s.vx[c] = vx;
-  s.vy[c] = vy;
+  VX[c] = vx;
+  VY[c] = vy;
   const float v2 = vx * vx + vy * vy;
   vm2 = fmaxf(vm2, v2);
   bad |= not_finite(v2);
@@ -129,9 +173,9 @@ __device__ __forceinline__ void velocity2d_cell(const Shot2D& s, int i, int j, i
   if (i >= n0 && i < s.nx - n0 && j >= n0 && j < s.ny - n0) {
     float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
     if (HET) {
-      const float l = s.lam[c], m = s.mu[c];
+      const float l = v.lam()[c], m = v.mu()[c];
       const float den = 1.0f / (4.0f * m * (l + m));
-      hr = 0.5f * s.rho[c];
+      hr = 0.5f * v.rho()[c];
       c1 = (l + 2.0f * m) * den;
       c2 = l * den;
       i2m = 1.0f / (2.0f * m);
@@ -141,6 +185,12 @@ __device__ __forceinline__ void velocity2d_cell(const Shot2D& s, int i, int j, i
     const float eyy = c1 * syy - c2 * sxx;
     ep += 0.5f * (exx * sxx + eyy * syy) + i2m * (sxy * sxy);
   }
+}
+
+template <bool HET>
+__device__ __forceinline__ void velocity2d_cell(const Shot2D& s, int i, int j, int it, float& ek, float& ep,
+                                                float& vm2, int& bad) {
+  velocity2d_cell<HET>(s, GlobalView{s}, i, j, it, ek, ep, vm2, bad);
 }
 
 // View of a single-shot handle's state as a Shot2D.
