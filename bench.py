@@ -481,6 +481,12 @@ def run_batch2d(args, world, rank, local, pg):
     shots = batch2d_shots()
     cells = sum(sh[0].nx * sh[0].ny * sh[0].nstep for sh in shots)
     b = Batch([sh[0] for sh in shots], models=[sh[1] for sh in shots], receivers=[sh[2] for sh in shots])
+    if args.tuning:
+        b.set_tuning(*(int(x) for x in args.tuning.split(",")[:2]))
+        tune = None
+    else:
+        tune = b.autotune(trial_steps=200)       # outside the timed region
+    depth, tile_y = b.tuning()
     for _ in range(args.warmup):
         b.run()
     torch.cuda.synchronize()
@@ -505,6 +511,7 @@ def run_batch2d(args, world, rank, local, pg):
     for _ in range(args.steps):
         with Batch([sh[0] for sh in shots], models=[sh[1] for sh in shots],
                    receivers=[sh[2] for sh in shots]) as e:
+            e.set_tuning(depth, tile_y)
             e.run()
             for q in range(len(shots)):
                 e.seismograms(q)
@@ -532,7 +539,9 @@ def run_batch2d(args, world, rank, local, pg):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch2d_256_shots", "shots": len(shots), "cell_updates": cells,
-                   "l2": "inputs larger than L2 (about 4.5 GB of shot state)"},
+                   "l2": "inputs larger than L2 (about 4.5 GB of shot state)",
+                   "kernel": {"depth": depth, "tile_y": tile_y, "autotuned": tune is not None,
+                              "autotune_ms_per_step": tune["ms_per_step"] if tune else None}},
         "sequential_single_shot": {"value": round(seq, 3), "unit": "Mcell-updates/s",
                                    "speedup_of_batch": round(value / seq, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

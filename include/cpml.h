@@ -291,6 +291,18 @@ int cpml_batch_last_run_ms(cpml_batch* b, double* ms);
    cpml_batch_run return CPML_ERR_TIMEOUT with every CTA of the launch
    returned; the next run starts clean. For tests of that path. */
 int cpml_batch_set_wait_limit(cpml_batch* b, long long cycles);
+/* Temporal blocking of the batched engine: depth = time steps a tile
+   advances in shared memory per HBM round trip and per grid barrier, tile_y
+   = rows of its 32-wide tiles. Supported (depth, tile_y): (1, 8) the
+   two-barrier-per-step engine, (2, 8), (2, 16), (3, 16). Results are
+   bit-identical for every choice. Depth > 1 allocates a second buffer set
+   per shot (fields and memory variables). No reference counterpart. */
+int cpml_batch_set_tuning(cpml_batch* b, int depth, int tile_y);
+int cpml_batch_get_tuning(cpml_batch* b, int* depth, int* tile_y);
+/* Time the first trial_steps steps of the batch under every supported
+   (depth, tile_y) (CUDA events around the launch) and keep the fastest;
+   the batch is left ready for cpml_batch_run. No reference counterpart. */
+int cpml_batch_autotune(cpml_batch* b, int trial_steps, int* depth, int* tile_y, double* ms_per_step);
 void cpml_batch_destroy(cpml_batch* b);
 
 /* Kinetic and potential energy (the 3D program's formulas, 3D:1131-1180) of

@@ -51,6 +51,24 @@ class Batch:
         """Bound of one grid-barrier wait in SM cycles (0 = default)."""
         _L.check(self.L.cpml_batch_set_wait_limit(self.h, int(cycles)), "cpml_batch_set_wait_limit")
 
+    def set_tuning(self, depth: int = 1, tile_y: int = 8) -> None:
+        """Time steps per shared-memory pass (temporal blocking) and tile rows
+        (cpml_batch_set_tuning): (1, 8), (2, 8), (2, 16) or (3, 16)."""
+        _L.check(self.L.cpml_batch_set_tuning(self.h, int(depth), int(tile_y)), "cpml_batch_set_tuning")
+
+    def tuning(self):
+        d, t = ctypes.c_int(), ctypes.c_int()
+        _L.check(self.L.cpml_batch_get_tuning(self.h, ctypes.byref(d), ctypes.byref(t)))
+        return d.value, t.value
+
+    def autotune(self, trial_steps: int = 100):
+        """Time every (depth, tile_y) on the first trial_steps steps and keep
+        the fastest (cpml_batch_autotune)."""
+        d, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _L.check(self.L.cpml_batch_autotune(self.h, int(trial_steps), ctypes.byref(d), ctypes.byref(t),
+                                            ctypes.byref(ms)), "cpml_batch_autotune")
+        return {"depth": d.value, "tile_y": t.value, "ms_per_step": ms.value}
+
     def last_run_ms(self) -> float:
         v = ctypes.c_double()
         _L.check(self.L.cpml_batch_last_run_ms(self.h, ctypes.byref(v)))
@@ -99,10 +117,15 @@ def _main(argv=None):
     ap.add_argument("--interior", type=int, nargs=2, default=(400, 600), help="interior cells per side, range")
     ap.add_argument("--record-s", type=float, default=0.1, help="simulated seconds per shot")
     ap.add_argument("--runs", type=int, default=2)
+    ap.add_argument("--tuning", type=str, default=None, help="depth,tile_y (default: autotune)")
     a = ap.parse_args(argv)
     shots = batch2d_shots(nshots=a.shots, interior=tuple(a.interior), record_s=a.record_s)
     cells = sum(p.nx * p.ny * p.nstep for p, _, _ in shots)
     with Batch([p for p, _, _ in shots], models=[m for _, m, _ in shots], receivers=[r for _, _, r in shots]) as b:
+        if a.tuning:
+            b.set_tuning(*(int(x) for x in a.tuning.split(",")))
+        else:
+            print("autotune:", b.autotune())
         for r in range(a.runs):
             b.run()
             ms = b.last_run_ms()

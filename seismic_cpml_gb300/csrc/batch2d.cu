@@ -13,6 +13,18 @@
 // 32 x 8 tiles handed out round-robin over the resident CTAs, so uneven grid
 // sizes balance without a queue. Grid barriers spin with a bound (~2 s) and
 // report CPML_ERR_TIMEOUT instead of hanging.
+//
+// Temporal blocking (depth D = 2 or 3, batch2d_tb_kernel): each item, a
+// 32 x TH tile, is staged in shared memory with a halo of 2D cells (fields,
+// per-cell model and, on C-PML tiles, memory variables) and advanced D time
+// steps there: stress on the tile grown by 2(D-u)-1 cells, then velocity on
+// it grown by 2(D-u)-2, for u = 0..D-1, so each update only reads cells the
+// previous one produced. Only the tile's own cells go back to HBM, into the
+// other of two buffer sets (neighbouring items still read the old set), and
+// one grid barrier ends the phase: D time steps per HBM round trip and per
+// barrier instead of one step and two barriers. The cell updates are the
+// same functions (cell2d.cuh) on a shared-memory view, so the results are
+// bit-identical to depth 1.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -35,6 +47,9 @@ constexpr long long kBarrierCycles = 4000000000LL;
 
 struct BatchArgs {
   const Shot2D* shots;      // by shot id
+  const Shot2D* shots_alt;  // the same shots on their second buffer set (temporal blocking)
+  const int* item_rb;       // temporal blocking: receivers of item q are [item_rb[q], item_rb[q+1])
+  const int* shot_nstep;    // NSTEP by shot id
   const int4* items;        // (shot, i0, j0, -) in schedule order
   const int* items_at;      // [max_nstep] items of the shots running at step t
   const int* recs_at;       // [max_nstep] receivers of the shots running at step t
@@ -122,6 +137,163 @@ __global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
   if (a.max_nstep > 0) record_batch(a, a.max_nstep - 1);
 }
 
+// The staged region of one item: 16 arrays of RW x RH cells in shared
+// memory (vx vy sxx syy sxy | lambda mu rho | four x-slab and four y-slab
+// memory variables, all indexed like the fields); grid cell (i, j) is
+// element (j - oy) * RW + (i - ox).
+template <int RW, int RC>
+struct RegionView {
+  float* f;
+  int ox, oy;
+  __device__ __forceinline__ float* vx() const { return f; }
+  __device__ __forceinline__ float* vy() const { return f + RC; }
+  __device__ __forceinline__ float* sxx() const { return f + 2 * RC; }
+  __device__ __forceinline__ float* syy() const { return f + 3 * RC; }
+  __device__ __forceinline__ float* sxy() const { return f + 4 * RC; }
+  __device__ __forceinline__ const float* lam() const { return f + 5 * RC; }
+  __device__ __forceinline__ const float* mu() const { return f + 6 * RC; }
+  __device__ __forceinline__ const float* rho() const { return f + 7 * RC; }
+  __device__ __forceinline__ float* mx(int q) const { return f + (8 + q) * RC; }
+  __device__ __forceinline__ float* my(int q) const { return f + (12 + q) * RC; }
+  __device__ __forceinline__ long long pitch() const { return RW; }
+  __device__ __forceinline__ long long at(int i, int j) const { return (long long)(j - oy) * RW + (i - ox); }
+  __device__ __forceinline__ long long mxi(int i, int j, int sx) const { (void)sx; return at(i, j); }
+  __device__ __forceinline__ long long myi(int i, int j, int sy) const { (void)sy; return at(i, j); }
+};
+
+template <int TH, int D>
+struct TbGeo {
+  static constexpr int R = 2 * D;              // halo: 2 cells per time step
+  static constexpr int RW = BTX + 2 * R, RH = TH + 2 * R, RC = RW * RH;
+  static constexpr size_t SMEM = size_t(16) * RC * sizeof(float);
+};
+
+// Temporal blocking: D time steps of every running shot per grid-barrier
+// phase (see the file comment). Items are (shot, i0, j0, -) tiles of 32 x TH.
+template <int TH, int D>
+__global__ void __launch_bounds__(BNT, TH == 8 ? 4 : (D == 2 ? 3 : 2)) batch2d_tb_kernel(BatchArgs a) {
+  using G = TbGeo<TH, D>;
+  constexpr int R = G::R, RW = G::RW, RC = G::RC;
+  extern __shared__ __align__(16) float reg[];
+  __shared__ Shot2D shd;
+  static_assert(sizeof(Shot2D) % 8 == 0, "descriptor copied in 8-byte words");
+  const int tid = threadIdx.x;
+  unsigned nbar = 0;
+  int phase = 0;
+  for (int t = 0; t < a.max_nstep; t += D, ++phase) {
+    const int n = a.items_at[t];
+    const Shot2D* SA = (phase & 1) ? a.shots_alt : a.shots;   // holds time step t
+    const Shot2D* SB = (phase & 1) ? a.shots : a.shots_alt;   // receives step t + k
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+      const int4 itm = a.items[q];
+      __syncthreads();   // the previous item is done with shd and the region
+      {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(SA + itm.x);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(&shd);
+        for (int w = tid; w < (int)(sizeof(Shot2D) / 8); w += BNT) dst[w] = src[w];
+      }
+      __syncthreads();
+      const Shot2D& S = shd;
+      const int k = min(D, a.shot_nstep[itm.x] - t);  // steps of this shot in this phase
+      const int i0 = itm.y, j0 = itm.z, ox = i0 - R, oy = j0 - R;
+      const RegionView<RW, RC> V{reg, ox, oy};
+      const int wx = S.ax.width(), wy = S.ay.width();
+      const bool xs = wx > 0 && (ox < S.ax.lo || ox + RW > S.nx - S.ax.hi);
+      const bool ys = wy > 0 && (oy < S.ay.lo || oy + G::RH > S.ny - S.ay.hi);
+      // stage the region (zero outside the grid; the updates never read there)
+      for (int c = tid; c < RC; c += BNT) {
+        const int gi = ox + c % RW, gj = oy + c / RW;
+        const bool in = gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny;
+        const long long g = (long long)gj * S.px + gi;
+        reg[c] = in ? S.vx[g] : 0.f;
+        reg[RC + c] = in ? S.vy[g] : 0.f;
+        reg[2 * RC + c] = in ? S.sxx[g] : 0.f;
+        reg[3 * RC + c] = in ? S.syy[g] : 0.f;
+        reg[4 * RC + c] = in ? S.sxy[g] : 0.f;
+        if (S.het) {
+          reg[5 * RC + c] = in ? S.lam[g] : 0.f;
+          reg[6 * RC + c] = in ? S.mu[g] : 0.f;
+          reg[7 * RC + c] = in ? S.rho[g] : 0.f;
+        }
+        if (xs) {
+          const int sx = in ? S.ax.slab(gi) : -1;
+          const long long m = (long long)gj * wx + sx;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) reg[(8 + v) * RC + c] = sx >= 0 ? S.mx[v][m] : 0.f;
+        }
+        if (ys) {
+          const int sy = in ? S.ay.slab(gj) : -1;
+          const long long m = (long long)sy * S.px + gi;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) reg[(12 + v) * RC + c] = sy >= 0 ? S.my[v][m] : 0.f;
+        }
+      }
+      __syncthreads();
+      // the tile grown by e cells, inside the grid (e is a compile-time
+      // constant on full phases, so the cell index splits without a division)
+      auto sweep = [&](int e, auto&& fn) {
+        const int w = BTX + 2 * e, h = TH + 2 * e;
+        for (int c = tid; c < w * h; c += BNT) {
+          const int gi = i0 - e + c % w, gj = j0 - e + c / w;
+          if (gi >= 0 && gi < S.nx && gj >= 0 && gj < S.ny) fn(gi, gj);
+        }
+      };
+      auto substep = [&](int u, int es) {
+        sweep(es, [&](int gi, int gj) {
+          if (S.het) stress2d_cell<true>(S, V, gi, gj);
+          else stress2d_cell<false>(S, V, gi, gj);
+        });
+        __syncthreads();
+        sweep(es - 1, [&](int gi, int gj) {
+          float ek = 0.f, ep = 0.f, vm2 = 0.f;
+          int bad = 0;
+          if (S.het) velocity2d_cell<true>(S, V, gi, gj, t + u + 1, ek, ep, vm2, bad);
+          else velocity2d_cell<false>(S, V, gi, gj, t + u + 1, ek, ep, vm2, bad);
+          if (bad && gi >= i0 && gi < i0 + BTX && gj >= j0 && gj < j0 + TH) atomicOr(a.err, 4);
+        });
+        __syncthreads();
+        // receivers in this tile, sample of step t + u + 1
+        for (int r = a.item_rb[q] + tid; r < a.item_rb[q + 1]; r += BNT) {
+          const int cell = a.rec[r].y;
+          const long long rc = V.at(cell % S.px, cell / S.px);
+          a.seis[a.rec_off[r] + t + u] = reg[rc];
+          a.seis[a.rec_offy[r] + t + u] = reg[RC + rc];
+        }
+      };
+      if (k == D) {
+#pragma unroll
+        for (int u = 0; u < D; ++u) substep(u, 2 * (D - u) - 1);
+      } else {   // the last phase of a shot whose NSTEP is not a multiple of D
+        for (int u = 0; u < k; ++u) substep(u, 2 * (k - u) - 1);
+      }
+      // own cells to the other buffer set
+      const Shot2D& W = SB[itm.x];
+      float* const wf[5] = {W.vx, W.vy, W.sxx, W.syy, W.sxy};
+      for (int c = tid; c < BTX * TH; c += BNT) {
+        const int gi = i0 + c % BTX, gj = j0 + c / BTX;
+        if (gi >= S.nx || gj >= S.ny) continue;
+        const long long g = (long long)gj * S.px + gi;
+        const long long rc = V.at(gi, gj);
+#pragma unroll
+        for (int f = 0; f < 5; ++f) wf[f][g] = reg[f * RC + rc];
+        if (xs) {
+          const int sx = S.ax.slab(gi);
+          if (sx >= 0)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) W.mx[v][(long long)gj * wx + sx] = reg[(8 + v) * RC + rc];
+        }
+        if (ys) {
+          const int sy = S.ay.slab(gj);
+          if (sy >= 0)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) W.my[v][(long long)sy * S.px + gi] = reg[(12 + v) * RC + rc];
+        }
+      }
+    }
+    if (!grid_sync(a, nbar)) return;
+  }
+}
+
 }  // namespace cpml
 
 using namespace cpml;
@@ -142,6 +314,7 @@ struct HostShot {
   cpml_params p;
   int px = 0;
   Shot2D s{};
+  Shot2D alt{};            // s on the second buffer set (temporal blocking)
   std::vector<int> rec;    // padded cells
   std::vector<int> recij;  // 1-based pairs
   double rho_src[2];
@@ -155,6 +328,12 @@ struct cpml_batch {
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   Shot2D* d_shots = nullptr;
+  Shot2D* d_shots_alt = nullptr;
+  int* d_item_rb = nullptr;
+  int* d_shot_nstep = nullptr;
+  int depth = 1, tile_y = 8;   // time steps per phase, tile rows (1: the two-barrier kernel)
+  bool alt_ready = false;      // second buffer sets allocated
+  int trial_steps = 0;         // >0: runs stop after this many steps (autotuning trials)
   int4* d_items = nullptr;
   int* d_items_at = nullptr;
   int* d_recs_at = nullptr;
@@ -266,6 +445,39 @@ int upload_source(cpml_batch* b, HostShot& H, float** fx, float** fy) {
   return CPML_OK;
 }
 
+// The kernel of a (depth, tile rows) choice and its dynamic shared memory;
+// *fn = nullptr for an unsupported pair.
+void kernel_for(int depth, int tile_y, const void** fn, size_t* smem) {
+  *fn = nullptr;
+  *smem = 0;
+  if (depth == 1 && tile_y == 8) { *fn = (const void*)batch2d_kernel; return; }
+  if (depth == 2 && tile_y == 8) { *fn = (const void*)batch2d_tb_kernel<8, 2>; *smem = TbGeo<8, 2>::SMEM; }
+  if (depth == 2 && tile_y == 16) { *fn = (const void*)batch2d_tb_kernel<16, 2>; *smem = TbGeo<16, 2>::SMEM; }
+  if (depth == 3 && tile_y == 16) { *fn = (const void*)batch2d_tb_kernel<16, 3>; *smem = TbGeo<16, 3>::SMEM; }
+}
+
+// The second buffer set of every shot (fields and memory variables) that
+// temporal blocking alternates with the first.
+int alloc_alt(cpml_batch* b) {
+  if (b->alt_ready) return CPML_OK;
+  for (HostShot& H : b->shots) {
+    const size_t n = size_t(H.px) * H.p.ny;
+    Shot2D A = H.s;
+    float* f = nullptr;
+    int st;
+    if ((st = balloc(b, &f, 5 * n))) return st;
+    A.vx = f; A.vy = f + n; A.sxx = f + 2 * n; A.syy = f + 3 * n; A.sxy = f + 4 * n;
+    const size_t wx = H.s.ax.width(), wy = H.s.ay.width();
+    for (int v = 0; v < 4; ++v) {
+      if ((st = balloc(b, &A.mx[v], wx * H.p.ny))) return st;
+      if ((st = balloc(b, &A.my[v], wy * size_t(H.px)))) return st;
+    }
+    H.alt = A;
+  }
+  b->alt_ready = true;
+  return CPML_OK;
+}
+
 int build_schedule(cpml_batch* b) {
   const int ns = (int)b->shots.size();
   std::vector<int> order(ns);
@@ -284,18 +496,36 @@ int build_schedule(cpml_batch* b) {
     seis_base[s] = seis_total;
     seis_total += size_t(2) * H.rec.size() * H.p.nstep;
   }
+  // depth 1: 32 x 8 tiles, receivers grouped by shot (recorded from HBM after
+  // each step); temporal blocking: 32 x tile_y tiles, receivers grouped by the
+  // tile that holds them (recorded from the staged region)
+  const bool tb = b->depth > 1;
+  const int th = tb ? b->tile_y : BTY;
+  std::vector<int> item_rb(1, 0);
   for (int k = 0; k < ns; ++k) {
     const int s = order[k];
     const HostShot& H = b->shots[s];
-    for (int j0 = 0; j0 < H.p.ny; j0 += BTY)
-      for (int i0 = 0; i0 < H.p.nx; i0 += BTX) items.push_back(make_int4(s, i0, j0, 0));
-    items_end[k] = (int)items.size();
     const size_t nr = H.rec.size();
-    for (size_t r = 0; r < nr; ++r) {
-      rec.push_back(make_int2(s, H.rec[r]));
-      off.push_back((long long)(seis_base[s] + r * H.p.nstep));
-      offy.push_back((long long)(seis_base[s] + (nr + r) * H.p.nstep));
-    }
+    for (int j0 = 0; j0 < H.p.ny; j0 += th)
+      for (int i0 = 0; i0 < H.p.nx; i0 += BTX) {
+        items.push_back(make_int4(s, i0, j0, 0));
+        if (!tb) continue;
+        for (size_t r = 0; r < nr; ++r) {
+          const int i = H.rec[r] % H.px, j = H.rec[r] / H.px;
+          if (i < i0 || i >= i0 + BTX || j < j0 || j >= j0 + th) continue;
+          rec.push_back(make_int2(s, H.rec[r]));
+          off.push_back((long long)(seis_base[s] + r * H.p.nstep));
+          offy.push_back((long long)(seis_base[s] + (nr + r) * H.p.nstep));
+        }
+        item_rb.push_back((int)rec.size());
+      }
+    items_end[k] = (int)items.size();
+    if (!tb)
+      for (size_t r = 0; r < nr; ++r) {
+        rec.push_back(make_int2(s, H.rec[r]));
+        off.push_back((long long)(seis_base[s] + r * H.p.nstep));
+        offy.push_back((long long)(seis_base[s] + (nr + r) * H.p.nstep));
+      }
     recs_end[k] = (int)rec.size();
   }
   std::vector<int> items_at(b->max_nstep), recs_at(b->max_nstep);
@@ -313,6 +543,12 @@ int build_schedule(cpml_batch* b) {
   if ((st = brealloc(b, &b->d_rec_off, std::max<size_t>(off.size(), 1)))) return st;
   if ((st = brealloc(b, &b->d_rec_offy, std::max<size_t>(offy.size(), 1)))) return st;
   if ((st = brealloc(b, &b->d_seis, std::max<size_t>(seis_total, 1)))) return st;
+  if ((st = brealloc(b, &b->d_item_rb, item_rb.size()))) return st;
+  BCK(cudaMemcpy(b->d_item_rb, item_rb.data(), sizeof(int) * item_rb.size(), cudaMemcpyHostToDevice));
+  std::vector<int> nsteps(ns);
+  for (int s = 0; s < ns; ++s) nsteps[s] = b->shots[s].p.nstep;
+  if ((st = brealloc(b, &b->d_shot_nstep, std::max(ns, 1)))) return st;
+  BCK(cudaMemcpy(b->d_shot_nstep, nsteps.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
   b->seis_floats = seis_total;
   if (!items.empty()) BCK(cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
   if (b->max_nstep) {
@@ -325,22 +561,32 @@ int build_schedule(cpml_batch* b) {
     BCK(cudaMemcpy(b->d_rec_offy, offy.data(), sizeof(long long) * offy.size(), cudaMemcpyHostToDevice));
   }
   for (int s = 0; s < ns; ++s) b->shots[s].seis = b->d_seis + seis_base[s];
-  // shot descriptors
-  std::vector<Shot2D> ds(ns);
-  for (int s = 0; s < ns; ++s) ds[s] = b->shots[s].s;
+  // shot descriptors, on both buffer sets
+  std::vector<Shot2D> ds(ns), da(ns);
+  for (int s = 0; s < ns; ++s) { ds[s] = b->shots[s].s; da[s] = b->alt_ready ? b->shots[s].alt : b->shots[s].s; }
   if (!b->d_shots && (st = balloc(b, &b->d_shots, std::max(ns, 1)))) return st;
+  if (!b->d_shots_alt && (st = balloc(b, &b->d_shots_alt, std::max(ns, 1)))) return st;
   BCK(cudaMemcpy(b->d_shots, ds.data(), sizeof(Shot2D) * ns, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_shots_alt, da.data(), sizeof(Shot2D) * ns, cudaMemcpyHostToDevice));
   // resident grid: every CTA must be co-resident for the grid barrier
   int dev = 0, nsm = 0, per_sm = 0;
   BCK(cudaGetDevice(&dev));
   BCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch2d_kernel, BNT, 0));
+  const void* fn = nullptr;
+  size_t smem = 0;
+  kernel_for(b->depth, b->tile_y, &fn, &smem);
+  if (!fn) return CPML_ERR_INVALID;
+  if (smem > 48 * 1024) BCK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BNT, smem));
   const int first = b->max_nstep ? items_at[0] : 1;
   b->grid = std::max(1, std::min(nsm * std::max(per_sm, 1), first));
   BatchArgs& A = b->args;
-  A.shots = b->d_shots; A.items = b->d_items; A.items_at = b->d_items_at; A.recs_at = b->d_recs_at;
+  A.shots = b->d_shots; A.shots_alt = b->d_shots_alt; A.item_rb = b->d_item_rb;
+  A.shot_nstep = b->d_shot_nstep;
+  A.items = b->d_items; A.items_at = b->d_items_at; A.recs_at = b->d_recs_at;
   A.rec = b->d_rec; A.rec_off = b->d_rec_off; A.rec_offy = b->d_rec_offy; A.seis = b->d_seis;
-  A.max_nstep = b->max_nstep; A.bar = b->d_bar; A.err = b->d_err;
+  A.max_nstep = b->trial_steps > 0 ? std::min(b->max_nstep, b->trial_steps) : b->max_nstep;
+  A.bar = b->d_bar; A.err = b->d_err;
   A.wait_cycles = b->wait_cycles > 0 ? b->wait_cycles : kBarrierCycles;
   b->dirty = false;
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -349,26 +595,35 @@ int build_schedule(cpml_batch* b) {
 }
 
 cudaError_t launch_batch(cpml_batch* b) {
+  const void* fn = nullptr;
+  size_t smem = 0;
+  kernel_for(b->depth, b->tile_y, &fn, &smem);
+  if (!fn) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(b->grid);
   cfg.blockDim = dim3(BNT);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = b->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, batch2d_kernel, b->args);
+  void* args[] = {&b->args};
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 int zero_batch(cpml_batch* b) {
   for (HostShot& H : b->shots) {
     const size_t n = size_t(H.px) * H.p.ny;
-    for (float* f : {H.s.vx, H.s.vy, H.s.sxx, H.s.syy, H.s.sxy}) BCK(cudaMemsetAsync(f, 0, 4 * n, b->stream));
-    const size_t wx = H.s.ax.width(), wy = H.s.ay.width();
-    for (int v = 0; v < 4; ++v) {
-      if (H.s.mx[v]) BCK(cudaMemsetAsync(H.s.mx[v], 0, 4 * wx * H.p.ny, b->stream));
-      if (H.s.my[v]) BCK(cudaMemsetAsync(H.s.my[v], 0, 4 * wy * size_t(H.px), b->stream));
+    for (const Shot2D* S : {&H.s, &H.alt}) {
+      if (S == &H.alt && !b->alt_ready) continue;
+      for (float* f : {S->vx, S->vy, S->sxx, S->syy, S->sxy}) BCK(cudaMemsetAsync(f, 0, 4 * n, b->stream));
+      const size_t wx = S->ax.width(), wy = S->ay.width();
+      for (int v = 0; v < 4; ++v) {
+        if (S->mx[v]) BCK(cudaMemsetAsync(S->mx[v], 0, 4 * wx * H.p.ny, b->stream));
+        if (S->my[v]) BCK(cudaMemsetAsync(S->my[v], 0, 4 * wy * size_t(H.px), b->stream));
+      }
     }
   }
   if (b->d_seis) BCK(cudaMemsetAsync(b->d_seis, 0, 4 * std::max<size_t>(b->seis_floats, 1), b->stream));
@@ -462,6 +717,7 @@ int cpml_batch_set_model(cpml_batch* b, int shot, const float* lam, const float*
                           cudaMemcpyHostToDevice, b->stream));
   }
   H.s.lam = H.model; H.s.mu = H.model + np; H.s.rho = H.model + 2 * np; H.s.het = 1;
+  if (b->alt_ready) { H.alt.lam = H.s.lam; H.alt.mu = H.s.mu; H.alt.rho = H.s.rho; H.alt.het = 1; }
   const int i = p.isource, j = p.jsource;
   auto R = [&](int i1, int j1) { return double(rho[size_t(j1 - 1) * p.nx + (i1 - 1)]); };
   H.rho_src[0] = R(i, j);
@@ -541,13 +797,17 @@ int cpml_batch_get_seismograms(cpml_batch* b, int shot, double* vx, double* vy) 
 int cpml_batch_get_field(cpml_batch* b, int shot, int field, float* out) {
   if (!b || shot < 0 || shot >= (int)b->shots.size() || !out) return CPML_ERR_INVALID;
   HostShot& H = b->shots[shot];
+  // temporal blocking alternates the buffer sets once per phase of `depth`
+  // steps: a shot that ran an odd number of phases ends on its second set
+  const int phases = (H.p.nstep + b->depth - 1) / b->depth;
+  const Shot2D& S = (b->depth > 1 && (phases & 1)) ? H.alt : H.s;
   const float* f = nullptr;
   switch (field) {
-    case CPML_FIELD_VX: f = H.s.vx; break;
-    case CPML_FIELD_VY: f = H.s.vy; break;
-    case CPML_FIELD_SXX: f = H.s.sxx; break;
-    case CPML_FIELD_SYY: f = H.s.syy; break;
-    case CPML_FIELD_SXY: f = H.s.sxy; break;
+    case CPML_FIELD_VX: f = S.vx; break;
+    case CPML_FIELD_VY: f = S.vy; break;
+    case CPML_FIELD_SXX: f = S.sxx; break;
+    case CPML_FIELD_SYY: f = S.syy; break;
+    case CPML_FIELD_SXY: f = S.sxy; break;
     default: return CPML_ERR_INVALID;
   }
   BCK(cudaMemcpy2D(out, 4 * size_t(H.p.nx), f, 4 * size_t(H.px), 4 * size_t(H.p.nx), H.p.ny,
@@ -559,6 +819,52 @@ int cpml_batch_set_wait_limit(cpml_batch* b, long long cycles) {
   if (!b || cycles < 0) return CPML_ERR_INVALID;
   b->wait_cycles = cycles;
   b->dirty = true;   // the bound travels in the captured launch arguments
+  return CPML_OK;
+}
+
+int cpml_batch_set_tuning(cpml_batch* b, int depth, int tile_y) {
+  if (!b) return CPML_ERR_INVALID;
+  const void* fn = nullptr;
+  size_t smem = 0;
+  kernel_for(depth, tile_y, &fn, &smem);
+  if (!fn) return CPML_ERR_INVALID;
+  int st;
+  if (depth > 1 && (st = alloc_alt(b))) return st;
+  b->depth = depth;
+  b->tile_y = tile_y;
+  b->dirty = true;
+  return CPML_OK;
+}
+
+int cpml_batch_get_tuning(cpml_batch* b, int* depth, int* tile_y) {
+  if (!b) return CPML_ERR_INVALID;
+  if (depth) *depth = b->depth;
+  if (tile_y) *tile_y = b->tile_y;
+  return CPML_OK;
+}
+
+int cpml_batch_autotune(cpml_batch* b, int trial_steps, int* depth, int* tile_y, double* ms_per_step) {
+  if (!b || trial_steps < 1) return CPML_ERR_INVALID;
+  const int cand[4][2] = {{1, 8}, {2, 8}, {2, 16}, {3, 16}};
+  int bd = 1, bt = 8, st;
+  double best = 1e300;
+  for (const auto& c : cand) {
+    if ((st = cpml_batch_set_tuning(b, c[0], c[1]))) { b->trial_steps = 0; return st; }
+    b->trial_steps = trial_steps;
+    if ((st = cpml_batch_run(b)) || (st = cpml_batch_run(b))) {   // the first run builds the graph
+      b->trial_steps = 0;
+      b->dirty = true;
+      return st;
+    }
+    const int steps = std::min(trial_steps, b->max_nstep);
+    const double ms = b->last_ms / std::max(steps, 1);
+    if (ms < best) { best = ms; bd = c[0]; bt = c[1]; }
+  }
+  b->trial_steps = 0;
+  if ((st = cpml_batch_set_tuning(b, bd, bt))) return st;
+  if (depth) *depth = bd;
+  if (tile_y) *tile_y = bt;
+  if (ms_per_step) *ms_per_step = best;
   return CPML_OK;
 }
 

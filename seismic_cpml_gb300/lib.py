@@ -62,6 +62,9 @@ SIGNATURES = [
     ("cpml_batch_get_field", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, _fp]),
     ("cpml_batch_last_run_ms", ctypes.c_int, [_h, _dp]),
     ("cpml_batch_set_wait_limit", ctypes.c_int, [_h, ctypes.c_longlong]),
+    ("cpml_batch_set_tuning", ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int]),
+    ("cpml_batch_get_tuning", ctypes.c_int, [_h, _ip, _ip]),
+    ("cpml_batch_autotune", ctypes.c_int, [_h, ctypes.c_int, _ip, _ip, _dp]),
     ("cpml_batch_destroy", None, [_h]),
     ("cpml_energy3d_noalloc", ctypes.c_int, [_P(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int,

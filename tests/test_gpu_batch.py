@@ -16,11 +16,22 @@ def small_shots():
     return batch2d_shots(nshots=6, seed=11, interior=(24, 70), npml=8, record_s=0.25, nrec=7)
 
 
-def test_batch_equals_single_shots_bitwise():
+TUNINGS = [(1, 8), (2, 8), (2, 16), (3, 16)]
+
+
+@pytest.mark.parametrize("tuning", TUNINGS, ids=["d1", "d2t8", "d2t16", "d3t16"])
+def test_batch_equals_single_shots_bitwise(tuning):
+    """Every temporal-blocking depth and tile height: shots of odd and even
+    NSTEP (a last phase of fewer steps than the depth), homogeneous and
+    per-cell models, receivers in the C-PML and the interior, bit-identical
+    seismograms and final fields to single-shot handles."""
     shots = small_shots()
     assert len({p.nstep for p, _, _ in shots}) > 1          # uneven lengths
+    assert {p.nstep % 2 for p, _, _ in shots} == {0, 1} and {p.nstep % 3 for p, _, _ in shots} >= {1, 2}
     models = [m if s % 2 == 0 else None for s, (_, m, _) in enumerate(shots)]
     with Batch([p for p, _, _ in shots], models=models, receivers=[r for _, _, r in shots]) as b:
+        b.set_tuning(*tuning)
+        assert b.tuning() == tuning
         b.run()
         for s, (p, m, rec) in enumerate(shots):
             with Solver(p, rec, model=models[s]) as one:
@@ -31,6 +42,22 @@ def test_batch_equals_single_shots_bitwise():
             assert np.array_equal(vx, vx1) and np.array_equal(vy, vy1), s
             for n, f in f1.items():
                 assert np.array_equal(b.field(s, n), f), (s, n)
+
+
+def test_batch_autotune_keeps_results_exact():
+    shots = small_shots()[:4]
+    args = ([p for p, _, _ in shots], [m for _, m, _ in shots], [r for _, _, r in shots])
+    with Batch(*args) as ref:
+        ref.run()
+        want = [ref.seismograms(s) for s in range(4)]
+    with Batch(*args) as b:
+        best = b.autotune(trial_steps=40)
+        assert (best["depth"], best["tile_y"]) in TUNINGS and best["ms_per_step"] > 0
+        assert b.tuning() == (best["depth"], best["tile_y"])
+        b.run()
+        for s in range(4):
+            vx, vy = b.seismograms(s)
+            assert np.array_equal(vx, want[s][0]) and np.array_equal(vy, want[s][1])
 
 
 def test_batch_matches_oracle():
