@@ -62,14 +62,22 @@ extern "C" {
                                     homogeneous model, DELTAX = DELTAY, second order */
 
 /* ---- step kernels (cpml_set_tuning) ----------------------------------- */
-#define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: persistent when the
-                                     grid has more 32 x 8 tiles than the GPU holds
-                                     resident CTAs, else two-sweep                      */
+#define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: the on-chip cluster
+                                     kernel when the grid fits, else persistent when it
+                                     has more 32 x 8 tiles than the GPU holds resident
+                                     CTAs, else two-sweep                               */
 #define CPML_KERNEL_TWO_SWEEP  1  /* stress kernel + velocity kernel, in place          */
 #define CPML_KERNEL_FUSED      2  /* 3D only: one kernel per step, two buffer sets, TMA  */
 #define CPML_KERNEL_PERSISTENT 3  /* 2D only: the two sweeps of a whole chunk of steps in
                                      one cooperative launch, grid barriers between them;
                                      results bit-identical to CPML_KERNEL_TWO_SWEEP      */
+#define CPML_KERNEL_CLUSTER    4  /* 2D second order only: the whole grid (fields, model,
+                                     memory variables) in the shared memory of one
+                                     thread-block cluster for a chunk of steps, halo rows
+                                     exchanged through distributed shared memory; fields
+                                     and seismograms bit-identical to TWO_SWEEP, energy
+                                     summed per CTA (equal to rounding). CPML_ERR_INVALID
+                                     when the grid does not fit on chip                 */
 
 /* ---- fields (for cpml_get_field / cpml_get_plane) ---------------------- */
 #define CPML_FIELD_VX  0

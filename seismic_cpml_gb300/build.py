@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libcpml.so")
 PROGRAM = os.path.join(OUT, "cpml_program")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels2d.cu", "kernels2d_ext.cu", "kernels3d.cu", "fused3d.cu", "support.cu",
-           "noalloc.cu", "batch2d.cu", "surrogate.cu", "host.cpp"]
+           "noalloc.cu", "batch2d.cu", "cluster2d.cu", "surrogate.cu", "host.cpp"]
 
 
 def nvcc() -> str:

@@ -31,6 +31,8 @@ void launch_step2d_two_sweep(const StepArgs& s, int ls, bool het, cudaStream_t s
 void launch_step2d_order4(const StepArgs& s, int ls, bool het, cudaStream_t st);
 void launch_step2d_split(const StepArgs& s, int ls, cudaStream_t st);
 int persist2d_grid(const StepArgs& s, bool het);
+ClusterLayout cluster2d_layout(const StepArgs& s, bool het);
+cudaError_t launch_chunk2d_cluster(const StepArgs& s, int C, bool het, const ClusterLayout& L, cudaStream_t st);
 cudaError_t launch_chunk2d_persistent(const StepArgs& s, int C, bool het, unsigned* bar, int grid,
                                       cudaStream_t st);
 int blocks3d(const StepArgs& s);
@@ -86,6 +88,8 @@ struct cpml_handle {
   float* fld1[9] = {};     // buffer set 1 (fused 3D path: time n+1 while set 0 holds n)
   bool pingpong = false;   // fields alternate between the sets every step
   bool plan_ok = false;    // the last re-plan (configure_path) completed; cpml_run needs it
+  bool cluster = false;    // 2D: the whole grid on chip in one cluster launch per chunk
+  ClusterLayout clay{};    // its layout
   bool persist = false;    // 2D: one cooperative launch per chunk of steps
   int persist_grid = 0;    // its CTAs
   unsigned* bar = nullptr; // its grid-barrier words
@@ -455,8 +459,10 @@ int get_graph(cpml_handle* h, int C, cudaGraphExec_t* out) {
   if (it != h->graphs.end()) { *out = it->second; return CPML_OK; }
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  if (h->persist) {
-    const cudaError_t le = launch_chunk2d_persistent(make_args(h), C, h->het, h->bar, h->persist_grid, h->stream);
+  if (h->cluster || h->persist) {
+    const cudaError_t le = h->cluster ? launch_chunk2d_cluster(make_args(h), C, h->het, h->clay, h->stream)
+                                      : launch_chunk2d_persistent(make_args(h), C, h->het, h->bar, h->persist_grid,
+                                                                  h->stream);
     if (le != cudaSuccess) {
       cudaStreamEndCapture(h->stream, &g);
       if (g) cudaGraphDestroy(g);
@@ -540,7 +546,18 @@ int configure_path_impl(cpml_handle* h) {
     h->nblocks = h->ndim == 3 ? blocks3d(s) : blocks2d(s);
   }
   h->persist = false;
-  if (is_standard2d(h) && h->kernel != CPML_KERNEL_TWO_SWEEP) {
+  h->cluster = false;
+  if (is_standard2d(h) && (h->kernel == CPML_KERNEL_CLUSTER || h->kernel == CPML_KERNEL_AUTO)) {
+    // a grid small enough to live in one cluster's shared memory runs on chip
+    h->clay = cluster2d_layout(make_args(h), h->het);
+    if (h->clay.ncl > 0) {
+      h->cluster = true;
+      h->nblocks = h->clay.ncl;
+    } else if (h->kernel == CPML_KERNEL_CLUSTER) {
+      return CPML_ERR_INVALID;
+    }
+  }
+  if (!h->cluster && is_standard2d(h) && h->kernel != CPML_KERNEL_TWO_SWEEP) {
     const StepArgs s = make_args(h);
     h->persist_grid = persist2d_grid(s, h->het);
     // automatic choice: persistent only when the grid has more tiles than
@@ -1088,8 +1105,9 @@ int cpml_last_run_ms(cpml_handle* h, double* ms) {
 }
 
 int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth) {
-  if (!h || kernel < 0 || kernel > 3) return CPML_ERR_INVALID;
-  if ((kernel == CPML_KERNEL_FUSED && h->ndim != 3) || (kernel == CPML_KERNEL_PERSISTENT && !is_standard2d(h)))
+  if (!h || kernel < 0 || kernel > 4) return CPML_ERR_INVALID;
+  if ((kernel == CPML_KERNEL_FUSED && h->ndim != 3) ||
+      ((kernel == CPML_KERNEL_PERSISTENT || kernel == CPML_KERNEL_CLUSTER) && !is_standard2d(h)))
     return CPML_ERR_INVALID;
   if (zchunk < 2 || !fused3d_shape_ok(tile_y, depth)) return CPML_ERR_INVALID;
   if (h->it != 0) return CPML_ERR_INVALID;  // only on a fresh or reset handle
@@ -1103,7 +1121,9 @@ int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int dept
 int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth) {
   if (!h) return CPML_ERR_INVALID;
   if (kernel)
-    *kernel = h->pingpong ? CPML_KERNEL_FUSED : (h->persist ? CPML_KERNEL_PERSISTENT : CPML_KERNEL_TWO_SWEEP);
+    *kernel = h->pingpong ? CPML_KERNEL_FUSED
+                          : (h->cluster ? CPML_KERNEL_CLUSTER
+                                        : (h->persist ? CPML_KERNEL_PERSISTENT : CPML_KERNEL_TWO_SWEEP));
   if (tile_y) *tile_y = h->tile_y;
   if (zchunk) *zchunk = h->zchunk;
   if (depth) *depth = h->depth;
@@ -1112,9 +1132,10 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
 
 int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels) {
   if (!h) return CPML_ERR_INVALID;
-  if (step_kernels) *step_kernels = h->pingpong ? fused3d_kernels_per_step(h->plan.data()) : (h->persist ? 0 : 2);
-  // chunk reduction + step counter (+ the persistent 2D launch, which runs the chunk's steps)
-  if (chunk_kernels) *chunk_kernels = h->persist ? 3 : 2;
+  const bool chunked = h->persist || h->cluster;   // one launch runs the chunk's steps
+  if (step_kernels) *step_kernels = h->pingpong ? fused3d_kernels_per_step(h->plan.data()) : (chunked ? 0 : 2);
+  // chunk reduction + step counter (+ the chunk's persistent or cluster launch)
+  if (chunk_kernels) *chunk_kernels = chunked ? 3 : 2;
   return CPML_OK;
 }
 
@@ -1182,6 +1203,7 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
     cand.push_back(TuneVal{CPML_KERNEL_TWO_SWEEP, 8, 32, 2, 0.0});
     if (is_standard2d(h)) {
       if (persist2d_grid(make_args(h), h->het) > 0) cand.push_back(TuneVal{CPML_KERNEL_PERSISTENT, 8, 32, 2, 0.0});
+      if (cluster2d_layout(make_args(h), h->het).ncl > 0) cand.push_back(TuneVal{CPML_KERNEL_CLUSTER, 8, 32, 2, 0.0});
     }
     const int flags = h->p.flags;
     h->p.flags |= CPML_FLAG_NO_STABILITY;  // time the kernels, not the host checks

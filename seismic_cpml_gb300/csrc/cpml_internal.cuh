@@ -106,6 +106,17 @@ struct ProfileArgs {
   double delta, cp, f0, dt, npower, kmax, amax, rcoef;
 };
 
+// On-chip layout of a small 2D grid held by one thread-block cluster
+// (cluster2d.cu); ncl = 0 when the grid does not fit.
+struct ClusterLayout {
+  int ncl;        // CTAs in the cluster (rows split into ncl bands)
+  int rows;       // own rows per CTA (the last one may have fewer)
+  int pitch;      // shared-memory row pitch (floats)
+  int ysl;        // y-slab rows a CTA can own
+  int het;
+  size_t smem;    // dynamic shared memory per CTA
+};
+
 // Linear index helpers
 __host__ __device__ inline long long cell3(const StepArgs& s, int i, int j, int k) {
   return (long long)k * s.plane + (long long)j * s.px + i;

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpml.so")
 
 OK = 0
-KERNEL_AUTO, KERNEL_TWO_SWEEP, KERNEL_FUSED, KERNEL_PERSISTENT = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_TWO_SWEEP, KERNEL_FUSED, KERNEL_PERSISTENT, KERNEL_CLUSTER = 0, 1, 2, 3, 4
 ERR = {-1: "INVALID", -2: "CFL", -3: "OOM", -4: "UNSTABLE", -5: "TIMEOUT", -6: "CUDA",
        -7: "NOT_READY", -8: "IO", -9: "RANGE"}
 

@@ -62,6 +62,35 @@ def check(g, ref, fields=None, floor=None, trace_tol=TRACE_TOL, energy_tol=ENERG
     return et, ee
 
 
+CLUSTER_CASES = {"small": lambda: P.small_2d(), "small_tall": lambda: P.small_2d(nx=40, ny=300, nstep=200),
+                 "reference_2d": lambda: (P.default_2d(), P.reference_receivers_2d(P.default_2d())),
+                 "config_2d_plain": P.config_2d_plain}
+
+
+@pytest.mark.parametrize("het", [False, True])
+@pytest.mark.parametrize("case", list(CLUSTER_CASES))
+def test_2d_cluster_kernel_is_bitwise_two_sweep(case, het):
+    """The on-chip cluster kernel (the whole grid in the shared memory of one
+    cluster, halo rows through distributed shared memory) gives bit-identical
+    seismograms and fields to the two-sweep kernels, on grids whose bands
+    hold the source, receivers, both y slabs and a short last band; its
+    energy is summed per CTA (compensated FP32 sums over a few cells per
+    thread) instead of one cell per thread and tile, equal to ~1e-8."""
+    p, rec = CLUSTER_CASES[case]()
+    if case in ("reference_2d", "config_2d_plain"):
+        p.nstep = 600
+    model = layered_2d(p, seed=8) if het else None
+    a = run_gpu(p, rec, model, tuning=(4, 8, 32, 2))
+    b = run_gpu(p, rec, model, tuning=(1, 8, 32, 2))
+    for k in ("vx", "vy"):
+        assert np.array_equal(a[k], b[k]), k
+    for n in a["fields"]:
+        assert np.array_equal(a["fields"][n], b["fields"][n]), n
+    e_a, e_b = a["ek"] + a["ep"], b["ek"] + b["ep"]
+    assert np.abs(e_a - e_b).max() <= 1e-7 * np.abs(e_b).max()
+    assert a["it"] == b["it"] == p.nstep and np.abs(a["vx"]).max() > 0
+
+
 @pytest.mark.parametrize("het", [False, True])
 def test_2d_small(het):
     p, rec = P.small_2d()
@@ -94,8 +123,10 @@ def test_2d_persistent_is_bitwise_two_sweep(het, shape):
 
 
 def test_2d_kernel_choice_and_launch_accounting():
-    p, rec = P.small_2d()                            # 16 tiles: one resident wave
-    with Solver(p, rec) as s:                        # automatic: two-sweep
+    p, rec = P.small_2d()                            # fits in one cluster's shared memory
+    with Solver(p, rec) as s:                        # automatic: the on-chip cluster kernel
+        assert s.tuning()[0] == 4 and s.launches_per_step() == (0, 3)
+    with Solver(p, rec, tuning=(1, 8, 32, 2)) as s:
         assert s.tuning()[0] == 1 and s.launches_per_step() == (2, 2)
     with Solver(p, rec, tuning=(3, 8, 32, 2)) as s:
         assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
@@ -109,6 +140,8 @@ def test_2d_kernel_choice_and_launch_accounting():
     with Solver(p3, rec3) as s:
         with pytest.raises(RuntimeError):
             s.set_tuning(3, 8, 32, 2)                # the persistent kernel is 2D only
+        with pytest.raises(RuntimeError):
+            s.set_tuning(4, 8, 32, 2)                # so is the cluster kernel
 
 
 TUNINGS_3D = [(1, 8, 32, 2), (2, 16, 32, 2), (2, 8, 7, 2), (2, 16, 5, 2), (2, 8, 9, 2), (2, 8, 11, 2)]
@@ -384,7 +417,7 @@ def test_autotune_2d_times_both_kernels_and_keeps_results_exact():
     p, rec = P.small_2d(nx=1200, ny=900, nstep=60)   # 4275 tiles: both 2D kernels are candidates
     with Solver(p, rec) as s:
         best = s.autotune(trial_steps=8)
-        assert best["kernel"] in (1, 3) and best["ms_per_step"] > 0
+        assert best["kernel"] in (1, 3, 4) and best["ms_per_step"] > 0
         assert s.tuning()[0] == best["kernel"] and s.status()[0] == 0
         s.run()
         vx, vy, _ = s.seismograms()

@@ -103,6 +103,8 @@ def test_kernel_choices_of_the_other_programs():
             assert s.tuning()[0] == 1 and s.launches_per_step() == (2, 2)   # two-sweep
             with pytest.raises(CpmlError):
                 s.set_tuning(3, 8, 32, 2)        # the persistent kernel is the second-order program's
+            with pytest.raises(CpmlError):
+                s.set_tuning(4, 8, 32, 2)        # and so is the on-chip cluster kernel
     p = P.default_2d_split()
     p.nstep = 20
     with Solver(p, []) as s:
