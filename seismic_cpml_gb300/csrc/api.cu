@@ -547,15 +547,13 @@ int configure_path_impl(cpml_handle* h) {
   }
   h->persist = false;
   h->cluster = false;
-  if (is_standard2d(h) && (h->kernel == CPML_KERNEL_CLUSTER || h->kernel == CPML_KERNEL_AUTO)) {
-    // a grid small enough to live in one cluster's shared memory runs on chip
+  if (is_standard2d(h) && h->kernel == CPML_KERNEL_CLUSTER) {
+    // the grid on chip in one cluster (only on request: on the 101 x 641
+    // reference grid it measured 13.3 against 9.0 us per step two-sweep)
     h->clay = cluster2d_layout(make_args(h), h->het);
-    if (h->clay.ncl > 0) {
-      h->cluster = true;
-      h->nblocks = h->clay.ncl;
-    } else if (h->kernel == CPML_KERNEL_CLUSTER) {
-      return CPML_ERR_INVALID;
-    }
+    if (h->clay.ncl <= 0) return CPML_ERR_INVALID;
+    h->cluster = true;
+    h->nblocks = h->clay.ncl;
   }
   if (!h->cluster && is_standard2d(h) && h->kernel != CPML_KERNEL_TWO_SWEEP) {
     const StepArgs s = make_args(h);

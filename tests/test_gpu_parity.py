@@ -123,11 +123,11 @@ def test_2d_persistent_is_bitwise_two_sweep(het, shape):
 
 
 def test_2d_kernel_choice_and_launch_accounting():
-    p, rec = P.small_2d()                            # fits in one cluster's shared memory
-    with Solver(p, rec) as s:                        # automatic: the on-chip cluster kernel
-        assert s.tuning()[0] == 4 and s.launches_per_step() == (0, 3)
-    with Solver(p, rec, tuning=(1, 8, 32, 2)) as s:
+    p, rec = P.small_2d()                            # 16 tiles: one resident wave
+    with Solver(p, rec) as s:                        # automatic: two-sweep
         assert s.tuning()[0] == 1 and s.launches_per_step() == (2, 2)
+    with Solver(p, rec, tuning=(4, 8, 32, 2)) as s:  # on request: the on-chip cluster kernel
+        assert s.tuning()[0] == 4 and s.launches_per_step() == (0, 3)
     with Solver(p, rec, tuning=(3, 8, 32, 2)) as s:
         assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
     pb, recb = P.small_2d(nx=4000, ny=400, nstep=20)  # 6250 tiles: more than the resident CTAs
