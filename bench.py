@@ -361,7 +361,7 @@ def run_ours(args, world, rank, local, pg):
                    "receivers": len(rec), "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (%.1f GB of wavefields)" % (18 * 4 * ncell / 1e9),
                    "kernel": {"kind": ["auto", "two_sweep", "fused"][kern[0]], "tile_y": kern[1],
-                              "zchunk": kern[2], "depth": kern[3],
+                              "zchunk": kern[2], "tma_lookahead": kern[3],
                               "autotuned": tune is not None}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,

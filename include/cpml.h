@@ -247,15 +247,18 @@ int cpml_last_run_ms(cpml_handle* h, double* ms);
    counterpart: the reference has no device. */
 int cpml_get_stream(cpml_handle* h, void** stream);
 
-/* Select the step kernel (CPML_KERNEL_*; FUSED is 3D only, PERSISTENT 2D
-   only: CPML_ERR_INVALID otherwise) and its launch shape: tile_y (rows of the
-   32-wide tile), zchunk (planes per CTA in the z sweep) and depth (planes the
-   TMA loads run ahead); the shape only matters to the fused kernel.
-   Supported (tile_y, depth): (8,2) (16,2). Only on a fresh or reset handle. No reference counterpart: the
-   reference's loop nests (3D:825-1052) have no tunables; the autotuner
-   drives this. */
-int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int depth);
-int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* depth);
+/* Select the step kernel (CPML_KERNEL_*; FUSED is 3D only, PERSISTENT and
+   CLUSTER are 2D second order only: CPML_ERR_INVALID otherwise) and its
+   launch shape: tile_y (rows of the 32-wide tile), zchunk (planes per CTA in
+   the z sweep) and lookahead (planes the fused kernel's TMA loads run ahead
+   of the plane being computed: 2, the only supported value). The shape only
+   matters to the fused kernel. Supported (tile_y, lookahead): (8,2) (16,2).
+   Single-shot kernels advance one time step per sweep: temporal blocking
+   is the batched engine's (cpml_batch_set_tuning). Only on a fresh or reset
+   handle. No reference counterpart: the reference's loop nests (3D:825-1052)
+   have no tunables; the autotuner drives this. */
+int cpml_set_tuning(cpml_handle* h, int kernel, int tile_y, int zchunk, int lookahead);
+int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* lookahead);
 /* Kernels one time step launches with the current tuning, and kernels per
    chunk of steps (the FP64 reduction and the step counter); a chunk ends at
    it = 5 and every IT_DISPLAY steps. For launch accounting; no reference

@@ -62,9 +62,10 @@ class Solver:
                                            iz.ctypes.data_as(_ip)), "cpml_set_receivers")
         self.receivers = rec
 
-    def set_tuning(self, kernel: int = 0, tile_y: int = 8, zchunk: int = 24, depth: int = 2) -> None:
-        """Step kernel (0 auto, 1 two-sweep, 2 fused 3D, 3 persistent 2D) and launch shape."""
-        _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk), int(depth)),
+    def set_tuning(self, kernel: int = 0, tile_y: int = 8, zchunk: int = 24, lookahead: int = 2) -> None:
+        """Step kernel (0 auto, 1 two-sweep, 2 fused 3D, 3 persistent 2D, 4 on-chip 2D
+        cluster) and launch shape (lookahead: the fused kernel's TMA look-ahead, 2)."""
+        _L.check(self.L.cpml_set_tuning(self.h, int(kernel), int(tile_y), int(zchunk), int(lookahead)),
                  "set_tuning")
 
     def launches_per_step(self):
