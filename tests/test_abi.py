@@ -41,6 +41,33 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(names) == bound, set(names) ^ bound
 
 
+def test_fortran_binding_module_matches_the_library(lib):
+    """include/cpml_gpu.f90 (not compiled here: no Fortran compiler): every
+    function it binds is exported, and its cpml_params type lists the C
+    struct's fields in order with the same kinds and array lengths."""
+    src = open(os.path.join(ROOT, "include", "cpml_gpu.f90")).read().lower()
+    names = re.findall(r"(?:function|subroutine)\s+(cpml_\w+)\s*\(", src)
+    assert len(names) > 30
+    for n in names:
+        assert hasattr(lib, n), n
+    body = src[src.index("type, bind(c) :: cpml_params"):src.index("end type")]
+    fields = []
+    for line in body.splitlines()[1:]:
+        if "::" not in line:
+            continue
+        kind = "int" if "integer(c_int32_t)" in line else "double"
+        for item in line.split("::")[1].split(","):
+            item = item.strip()
+            m = re.match(r"(\w+)(?:\((\d+)\))?", item)
+            fields.append((m.group(1), kind, int(m.group(2) or 1)))
+    want = []
+    for name, ctype in P.CpmlParams._fields_:
+        n = getattr(ctype, "_length_", 1)
+        base = ctype._type_ if hasattr(ctype, "_length_") else ctype
+        want.append((name, "int" if base is ctypes.c_int32 else "double", n))
+    assert fields == want
+
+
 def test_default_parameter_blocks_match_the_mirror(lib):
     for fn, mirror in ((lib.cpml_params_default_2d, P.default_2d),
                        (lib.cpml_params_default_3d, P.default_3d),
