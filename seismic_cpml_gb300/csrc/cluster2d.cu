@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1)
         a.seis[(size_t)a.nrec * a.nstep + o] = V.vy()[V.at(i, j)];
       }
     }
-    block_partials<CL_THREADS>(ek.value(), ep.value(), vm2, bad, a.partials + ((size_t)ls * a.nblocks + rank) * 4);
+    block_partials<CL_THREADS>(ek.df(), ep.df(), vm2, bad, a.partials + ((size_t)ls * a.nblocks + rank) * 4);
     cluster_sync();
   }
 

@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
     }
     __syncthreads();
   }
-  block_partials<FNT>(ek.value(), ep.value(), vm2, bad, s.partials + ((size_t)ls * s.nblocks + blin) * 4);
+  block_partials<FNT>(ek.df(), ep.df(), vm2, bad, s.partials + ((size_t)ls * s.nblocks + blin) * 4);
 }
 
 // ---------------------------------------------------------------------------

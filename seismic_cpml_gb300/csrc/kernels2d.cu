@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(T2X* T2Y) velocity2d(StepArgs a, int ls) {
     velocity2d_cell<HET>(s, i, j, it, ek, ep, vm2, bad);
   }
   const long long blin = blockIdx.x + (long long)gridDim.x * blockIdx.y;
-  block_partials<T2X * T2Y>((double)ek, (double)ep, vm2, bad,
+  block_partials<T2X * T2Y>(DF{ek, 0.f}, DF{ep, 0.f}, vm2, bad,
                             a.partials + ((size_t)ls * a.nblocks + blin) * 4);
 }
 
@@ -74,8 +74,11 @@ __global__ void __launch_bounds__(T2X* T2Y) velocity2d(StepArgs a, int ls) {
 // pays once per chunk instead of twice per step.
 constexpr long long kGridWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
+// Five CTAs per SM (at most 51 registers, a few bytes of spill): the kernel is
+// latency-bound, and resident warps matter more than the last registers.
+
 template <bool HET>
-__global__ void __launch_bounds__(T2X* T2Y) persist2d(StepArgs a, int C, unsigned* bar) {
+__global__ void __launch_bounds__(T2X* T2Y, 5) persist2d(StepArgs a, int C, unsigned* bar) {
   const int tid = threadIdx.x, tx = tid & (T2X - 1), ty = tid / T2X;
   const int gx = (a.nx + T2X - 1) / T2X;
   const int ntiles = a.nblocks;
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(T2X* T2Y) persist2d(StepArgs a, int C, unsigne
       float ek = 0.f, ep = 0.f, vm2 = 0.f;
       int bad = 0;
       if (i < a.nx && j < a.ny) velocity2d_cell<HET>(s, i, j, base + ls + 1, ek, ep, vm2, bad);
-      block_partials<T2X * T2Y>((double)ek, (double)ep, vm2, bad, a.partials + ((size_t)ls * ntiles + q) * 4);
+      block_partials<T2X * T2Y>(DF{ek, 0.f}, DF{ep, 0.f}, vm2, bad, a.partials + ((size_t)ls * ntiles + q) * 4);
       __syncthreads();   // block_partials' shared scratch is reused by the next tile
     }
     if (ls + 1 < C && !grid_barrier(bar, ++nbar * gridDim.x, a.err, 1, kGridWaitCycles)) return;

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(E2X* E2Y) velocity2d4(StepArgs a, int ls) {
     }
   }
   const long long blin = blockIdx.x + (long long)gridDim.x * blockIdx.y;
-  block_partials<E2X * E2Y>((double)ek, (double)ep, vm2, bad, a.partials + ((size_t)ls * a.nblocks + blin) * 4);
+  block_partials<E2X * E2Y>(DF{ek, 0.f}, DF{ep, 0.f}, vm2, bad, a.partials + ((size_t)ls * a.nblocks + blin) * 4);
 }
 
 // --------------------------------------------------------------------------
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(E2X* E2Y) velocity_split(StepArgs a, int ls) {
     }
   }
   const long long blin = blockIdx.x + (long long)gridDim.x * blockIdx.y;
-  block_partials<E2X * E2Y>((double)ek, (double)ep, vm2, bad, a.partials + ((size_t)ls * a.nblocks + blin) * 4);
+  block_partials<E2X * E2Y>(DF{ek, 0.f}, DF{ep, 0.f}, vm2, bad, a.partials + ((size_t)ls * a.nblocks + blin) * 4);
 }
 
 void launch_step2d_order4(const StepArgs& s, int ls, bool het, cudaStream_t st) {

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(T3X* T3Y) velocity3d(StepArgs s, int ls) {
     }
   }
   const long long blin = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-  block_partials<T3X * T3Y>(ek.value(), ep.value(), vm2, bad,
+  block_partials<T3X * T3Y>(ek.df(), ep.df(), vm2, bad,
                             s.partials + ((size_t)ls * s.nblocks + blin) * 4);
 }
 

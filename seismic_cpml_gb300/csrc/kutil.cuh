@@ -18,6 +18,23 @@ __device__ __forceinline__ float pml(float d, int sidx, float* __restrict__ mem,
   return d * __ldg(ik + idx) + m;
 }
 
+// A double-float value hi + lo (about 48 significant bits) built from FP32
+// arithmetic alone: the energy reductions sum per-thread partials this way,
+// because FP64 adds run at a small fraction of the FP32 rate on this part.
+struct DF {
+  float hi, lo;
+};
+// Knuth's two-sum of the leading parts plus the trailing parts, renormalised.
+// The _rn intrinsics keep the compiler from contracting or re-associating.
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  const float t = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+  const float h = __fadd_rn(s, t);
+  return DF{h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+
 // Compensated (Kahan) FP32 accumulator: per-thread energy partials stay at
 // FP64-like accuracy without FP64 arithmetic per cell (FP64 throughput on
 // this part is a small fraction of FP32).
@@ -30,6 +47,7 @@ struct Kahan {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ DF df() const { return DF{s, -c}; }
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -109,6 +127,51 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, i
   }
   __syncthreads();
   return ok != 0;
+}
+
+// The same reduction with double-float partials: a fixed shuffle tree per
+// warp, then warp 0 over the warps' results, all in FP32 two-sum arithmetic;
+// only the block's two totals are converted to FP64 (out[0..3] as above).
+template <int NT>
+__device__ __forceinline__ void block_partials(DF ek, DF ep, float vm2, int bad, double* __restrict__ out) {
+  constexpr int NW = NT / 32;
+  __shared__ float s_e[4][NW];
+  __shared__ float s_vm[NW];
+  __shared__ int s_bad[NW];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x + threadIdx.z * blockDim.x * blockDim.y;
+  const int lane = tid & 31, w = tid >> 5;
+  auto wsum = [](DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      v = df_add(v, DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+    return v;
+  };
+  ek = wsum(ek);
+  ep = wsum(ep);
+  vm2 = warp_max(vm2);
+  bad = warp_or(bad);
+  if (lane == 0) {
+    s_e[0][w] = ek.hi; s_e[1][w] = ek.lo; s_e[2][w] = ep.hi; s_e[3][w] = ep.lo;
+    s_vm[w] = vm2; s_bad[w] = bad;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const bool in = lane < NW;
+    ek = DF{in ? s_e[0][lane] : 0.f, in ? s_e[1][lane] : 0.f};
+    ep = DF{in ? s_e[2][lane] : 0.f, in ? s_e[3][lane] : 0.f};
+    vm2 = in ? s_vm[lane] : 0.f;
+    bad = in ? s_bad[lane] : 0;
+    ek = wsum(ek);
+    ep = wsum(ep);
+    vm2 = warp_max(vm2);
+    bad = warp_or(bad);
+    if (lane == 0) {
+      out[0] = (double)ek.hi + (double)ek.lo;
+      out[1] = (double)ep.hi + (double)ep.lo;
+      out[2] = (double)vm2;
+      out[3] = (double)bad;
+    }
+  }
 }
 
 // v^2 check that also catches NaN / Inf (the reference's maxval would skip
