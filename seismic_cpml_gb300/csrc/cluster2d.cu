@@ -34,6 +34,9 @@ namespace cpml {
 
 constexpr int CL_THREADS = 1024;
 constexpr int CL_MAX = 16;
+constexpr int CL_CHUNK = 128;     // longest chunk of steps the runtime launches
+constexpr int CL_REC = 64;        // receivers a CTA buffers on chip ...
+constexpr int CL_RECBUF = 4096;   // ... in at most this many samples
 
 // Shared-memory view of a CTA's band: fields and model on rows jb-1 .. je
 // (own rows plus one halo row each side), x-slab memory variables on the own
@@ -127,6 +130,25 @@ __global__ void __launch_bounds__(CL_THREADS, 1)
       V.my(v)[r * L.pitch + i] = a.m.y[v][(long long)s.ay.slab(j) * a.px + i];
     }
   }
+  // The step loop writes nothing to HBM (a cluster barrier with release
+  // semantics would wait for such writes every half step): the energy
+  // partials and, when they fit, this CTA's receiver samples are kept in
+  // shared memory and written out after the last step of the chunk.
+  __shared__ double part_buf[CL_CHUNK][4];
+  __shared__ float rec_buf[CL_RECBUF];
+  __shared__ int rec_id[CL_REC];
+  __shared__ int n_own;
+  if (tid == 0) n_own = 0;
+  __syncthreads();
+  for (int r = tid; r < a.nrec; r += CL_THREADS) {
+    const int j = a.rec_cell[r] / a.px;
+    if (j >= jb && j < je) {
+      const int q = atomicAdd(&n_own, 1);
+      if (q < CL_REC) rec_id[q] = r;
+    }
+  }
+  __syncthreads();
+  const bool rec_on_chip = n_own <= CL_REC && 2 * n_own * C <= CL_RECBUF && C <= CL_CHUNK;
   __syncthreads();
   cluster_sync();
 
@@ -176,17 +198,40 @@ __global__ void __launch_bounds__(CL_THREADS, 1)
       if ((int)rank + 1 < L.ncl) st_peer(V.vy() + i, rank + 1, V.vy()[V.at(i, je - 1)]);
     }
     // receivers on the own rows, sample of step it (2D:683-686)
-    for (int r = tid; r < a.nrec; r += CL_THREADS) {
-      const int cell = a.rec_cell[r], j = cell / a.px, i = cell - j * a.px;
-      if (j >= jb && j < je) {
-        const size_t o = (size_t)r * a.nstep + (size_t)(it - 1);
-        a.seis[o] = V.vx()[V.at(i, j)];
-        a.seis[(size_t)a.nrec * a.nstep + o] = V.vy()[V.at(i, j)];
+    if (rec_on_chip) {
+      for (int q = tid; q < n_own; q += CL_THREADS) {
+        const int cell = a.rec_cell[rec_id[q]], j = cell / a.px, i = cell - j * a.px;
+        rec_buf[2 * (q * C + ls)] = V.vx()[V.at(i, j)];
+        rec_buf[2 * (q * C + ls) + 1] = V.vy()[V.at(i, j)];
+      }
+    } else {
+      for (int r = tid; r < a.nrec; r += CL_THREADS) {
+        const int cell = a.rec_cell[r], j = cell / a.px, i = cell - j * a.px;
+        if (j >= jb && j < je) {
+          const size_t o = (size_t)r * a.nstep + (size_t)(it - 1);
+          a.seis[o] = V.vx()[V.at(i, j)];
+          a.seis[(size_t)a.nrec * a.nstep + o] = V.vy()[V.at(i, j)];
+        }
       }
     }
-    block_partials<CL_THREADS>(ek.df(), ep.df(), vm2, bad, a.partials + ((size_t)ls * a.nblocks + rank) * 4);
+    if (C <= CL_CHUNK)
+      block_partials<CL_THREADS>(ek.df(), ep.df(), vm2, bad, part_buf[ls]);
+    else
+      block_partials<CL_THREADS>(ek.df(), ep.df(), vm2, bad, a.partials + ((size_t)ls * a.nblocks + rank) * 4);
     cluster_sync();
   }
+
+  // ---- the chunk's energy partials and receiver samples ---------------------
+  if (C <= CL_CHUNK)
+    for (int q = tid; q < 4 * C; q += CL_THREADS)
+      a.partials[((size_t)(q >> 2) * a.nblocks + rank) * 4 + (q & 3)] = part_buf[q >> 2][q & 3];
+  if (rec_on_chip)
+    for (int q = tid; q < n_own * C; q += CL_THREADS) {
+      const int k = q / C, ls = q - k * C, r = rec_id[k];
+      const size_t o = (size_t)r * a.nstep + (size_t)(base + ls);
+      a.seis[o] = rec_buf[2 * q];
+      a.seis[(size_t)a.nrec * a.nstep + o] = rec_buf[2 * q + 1];
+    }
 
   // ---- write the band's own rows and memory variables back -----------------
   float* const go[5] = {a.f.vx, a.f.vy, a.f.sxx, a.f.syy, a.f.sxy};
@@ -229,8 +274,10 @@ ClusterLayout cluster2d_layout(const StepArgs& s, bool het) {
     T.het = het ? 1 : 0;
     T.smem = sizeof(float) * ((size_t)8 * (T.rows + 2) * T.pitch + (size_t)4 * T.rows * wx +
                               (size_t)4 * T.ysl * T.pitch);
-    if (T.smem > (size_t)optin) continue;
     const void* fn = het ? (const void*)cluster2d_kernel<true> : (const void*)cluster2d_kernel<false>;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) { cudaGetLastError(); return L; }
+    if (T.smem + fa.sharedSizeBytes > (size_t)optin) continue;   // static buffers count too
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T.smem) != cudaSuccess ||
         (ncl > 8 && cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
       cudaGetLastError();
