@@ -110,7 +110,10 @@ struct Geo {
   // m-1 still reads (they may overlap in time: one CTA barrier per plane).
   static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 2 + 4 + 4 : 0);
   static constexpr int RING = 24 * REG;
-  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + 16 + 64;
+  // the tile's C-PML coefficients: a, b, 1/K at grid and half points, for
+  // x = i0-4 .. i0+FTX+3 and y = j0-1 .. j0+TY
+  static constexpr int NCOF = 6 * (BX + RY);
+  static constexpr size_t SMEM = (size_t)NBOX * SLOT * 4 + (size_t)RING * 4 + (size_t)NCOF * 4 + 16 + 64;
   static constexpr int NH = 2 * FTX + 2 * TY;        // halo stress cells
 };
 
@@ -148,7 +151,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
   float* r_szz = r_sxy + 4 * REG;
   float* r_sxz = r_szz + 4 * REG;
   float* r_syz = r_sxz + 4 * REG;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(r_syz + 4 * REG);
+  float* cfx = r_syz + 4 * REG;          // [6][BX]: a b ik ah bh ikh along x
+  float* cfy = cfx + 6 * BX;             // [6][RY] along y
+  uint64_t* bar = reinterpret_cast<uint64_t*>(cfy + 6 * G::RY);
 
   const int tid = threadIdx.x;
   const int tx = tid & 31, ty = tid >> 5;
@@ -201,6 +206,25 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // The coefficients depend on one coordinate only: staged once per item,
+  // they cost the plane loop shared-memory reads instead of an L2 round
+  // trip per sweep. Points off the axis get the neutral a = b = 0, 1/K = 1.
+  if (UX) {
+    for (int t = tid; t < 6 * BX; t += FNT) {
+      const int c = t / BX, i = i0 - 4 + (t - c * BX);
+      const float* arr = c == 0 ? s.ax.a : c == 1 ? s.ax.b : c == 2 ? s.ax.ik
+                       : c == 3 ? s.ax.ah : c == 4 ? s.ax.bh : s.ax.ikh;
+      cfx[t] = (i >= 0 && i < s.ax.n) ? __ldg(arr + i) : (c == 2 || c == 5 ? 1.f : 0.f);
+    }
+  }
+  if (UY) {
+    for (int t = tid; t < 6 * G::RY; t += FNT) {
+      const int c = t / G::RY, j = j0 - 1 + (t - c * G::RY);
+      const float* arr = c == 0 ? s.ay.a : c == 1 ? s.ay.b : c == 2 ? s.ay.ik
+                       : c == 3 ? s.ay.ah : c == 4 ? s.ay.bh : s.ay.ikh;
+      cfy[t] = (j >= 0 && j < s.ay.n) ? __ldg(arr + j) : (c == 2 || c == 5 ? 1.f : 0.f);
+    }
   }
   __syncthreads();
   if (tid == 0) {
@@ -416,14 +440,15 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (hx) {
           if (EARLY) { qx0 = pre[0]; qx1 = pre[1]; qx2 = pre[2]; }
           else { qx0 = s.m.x[0][mxi]; qx1 = s.m.x[1][mxi]; qx2 = s.m.x[2][mxi]; }
-          xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
-          xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
+          const float* cx = cfx + (i - i0 + 4);
+          xa = cx[0]; xb = cx[BX]; xk = cx[2 * BX]; xah = cx[3 * BX]; xbh = cx[4 * BX]; xkh = cx[5 * BX];
         }
         if (hy) {
           if (EARLY) { qy0 = pre[0]; qy1 = pre[1]; qy2 = pre[2]; }
           else { qy0 = s.m.y[0][myi]; qy1 = s.m.y[1][myi]; qy2 = s.m.y[2][myi]; }
-          ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
-          yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
+          const float* cy = cfy + (j - j0 + 1);
+          ya = cy[0]; yb = cy[G::RY]; yk = cy[2 * G::RY]; yah = cy[3 * G::RY]; ybh = cy[4 * G::RY];
+          ykh = cy[5 * G::RY];
         }
         if (zs) {
           if (EARLY) { qz0 = pre[0]; qz1 = pre[1]; qz2 = pre[2]; }
@@ -613,14 +638,15 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           if (hx) {
             if (EARLY) { qx3 = e_vel[q][0]; qx4 = e_vel[q][1]; qx5 = e_vel[q][2]; }
             else { qx3 = s.m.x[3][mxi]; qx4 = s.m.x[4][mxi]; qx5 = s.m.x[5][mxi]; }
-            xa = __ldg(s.ax.a + i); xb = __ldg(s.ax.b + i); xk = __ldg(s.ax.ik + i);
-            xah = __ldg(s.ax.ah + i); xbh = __ldg(s.ax.bh + i); xkh = __ldg(s.ax.ikh + i);
+            const float* cx = cfx + (i - i0 + 4);
+            xa = cx[0]; xb = cx[BX]; xk = cx[2 * BX]; xah = cx[3 * BX]; xbh = cx[4 * BX]; xkh = cx[5 * BX];
           }
           if (hy) {
             if (EARLY) { qy3 = e_vel[q][0]; qy4 = e_vel[q][1]; qy5 = e_vel[q][2]; }
             else { qy3 = s.m.y[3][myi]; qy4 = s.m.y[4][myi]; qy5 = s.m.y[5][myi]; }
-            ya = __ldg(s.ay.a + j); yb = __ldg(s.ay.b + j); yk = __ldg(s.ay.ik + j);
-            yah = __ldg(s.ay.ah + j); ybh = __ldg(s.ay.bh + j); ykh = __ldg(s.ay.ikh + j);
+            const float* cy = cfy + (j - j0 + 1);
+            ya = cy[0]; yb = cy[G::RY]; yk = cy[2 * G::RY]; yah = cy[3 * G::RY]; ybh = cy[4 * G::RY];
+            ykh = cy[5 * G::RY];
           }
           if (zs) {
             if (EARLY) { qz3 = e_vel[q][0]; qz4 = e_vel[q][1]; qz5 = e_vel[q][2]; }
