@@ -247,15 +247,24 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
   const float src_y = has_src ? s.src_fy[it - 1] : 0.f;
 
   // ---- per-thread constants ---------------------------------------------------
+  // In-plane offsets, fixed for the whole item: fo = j * px + i of a cell's
+  // fields, and of its memory variables on each slab axis (-1 outside the
+  // slab): x slab [k][j][sx], y slab [k][sy][i], z slab [sz][j][i] (= fo).
+  // A plane's base is added per plane, so every access is one 32-bit offset
+  // from a plane pointer.
+  const int pxi = (int)px;
   const int oi = i0 + tx;
   const int osx = (oi < nx) ? s.ax.slab(oi) : -1;
-  int oj[NQ], osy[NQ];
+  int oj[NQ], ofo[NQ], omx[NQ], omy[NQ];
   bool ov[NQ], oe[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     oj[q] = j0 + ty + 8 * q;
     ov[q] = oi < nx && oj[q] < ny;
-    osy[q] = ov[q] ? s.ay.slab(oj[q]) : -1;
+    const int osy = ov[q] ? s.ay.slab(oj[q]) : -1;
+    ofo[q] = oj[q] * pxi + oi;
+    omx[q] = (UX && xs_tile && ov[q] && osx >= 0) ? oj[q] * wx + osx : -1;
+    omy[q] = (UY && ys_tile && osy >= 0) ? osy * pxi + oi : -1;
     oe[q] = e_full_xy || (oi >= n0 && oi < nx - n0 && oj[q] >= n0 && oj[q] < ny - n0);
   }
   const int b_own = (ty + 1) * BX + tx + 4;
@@ -268,8 +277,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
     else { hi = i0 + FTX; hj = j0 + tid - 2 * FTX - TY; hcomps = 2 | 4; }               // right: xy, xz
   }
   const bool hv = tid < G::NH && hi >= 0 && hi < nx && hj >= 0 && hj < ny;
-  const int hsx = hv ? s.ax.slab(hi) : -1;
-  const int hsy = hv ? s.ay.slab(hj) : -1;
+  const int hfo = hj * pxi + hi;
+  const int hmx = (UX && xs_tile && hv && s.ax.slab(hi) >= 0) ? hj * wx + s.ax.slab(hi) : -1;
+  const int hmy = (UY && ys_tile && hv && s.ay.slab(hj) >= 0) ? s.ay.slab(hj) * pxi + hi : -1;
   const int hb = (hj - j0 + 1) * BX + (hi - i0 + 4);
   const int hr = (hj - j0 + 1) * RX + (hi - i0 + 1);
 
@@ -294,36 +304,32 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       const bool sm_ok = m >= 0 && m < nz, vp_ok = p >= kb && p < ke;
       const int szm = (CLS == CLS_Z && sm_ok) ? s.az.slab(m) : -1;
       const int szp = (CLS == CLS_Z && vp_ok) ? s.az.slab(p) : -1;
-      // memory-variable index of cell (i, j, slab index sa) at plane k on the class axis
-      auto midx = [&](int k, int i, int j, int sx_, int sy_, int sz_) -> long long {
-        if (CLS == CLS_X) return (long long)k * ny * wx + (long long)j * wx + sx_;
-        if (CLS == CLS_Y) return (long long)k * wy * px + (long long)sy_ * px + i;
-        return (long long)sz_ * ny * px + (long long)j * px + i;
-      };
-      auto in_slab = [&](int sx_, int sy_, int sz_) {
-        if (CLS == CLS_X) return xs_tile && sx_ >= 0;
-        if (CLS == CLS_Y) return ys_tile && sy_ >= 0;
-        return sz_ >= 0;
+      // plane base of the class axis's memory variables (Z: the slab plane)
+      auto mbase = [&](int k, int sz_) -> long long {
+        if (CLS == CLS_X) return (long long)k * ny * wx;
+        if (CLS == CLS_Y) return (long long)k * wy * px;
+        return (long long)sz_ * ny * px;
       };
       const float* const* A = CLS == CLS_X ? s.m.x : (CLS == CLS_Y ? s.m.y : s.m.z);
+      const bool m_in = sm_ok && (CLS != CLS_Z || szm >= 0);
+      const bool p_in = vp_ok && (CLS != CLS_Z || szp >= 0);
+      const long long bm = m_in ? mbase(m, szm) : 0, bp = p_in ? mbase(p, szp) : 0;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         e_own[q][0] = e_own[q][1] = e_own[q][2] = 0.f;
         e_vel[q][0] = e_vel[q][1] = e_vel[q][2] = 0.f;
-        if (!ov[q]) continue;
-        if (sm_ok && in_slab(osx, osy[q], szm)) {
-          const long long mi = midx(m, oi, oj[q], osx, osy[q], szm);
-          e_own[q][0] = A[0][mi]; e_own[q][1] = A[1][mi]; e_own[q][2] = A[2][mi];
+        const int mo = CLS == CLS_X ? omx[q] : (CLS == CLS_Y ? omy[q] : (ov[q] ? ofo[q] : -1));
+        if (m_in && mo >= 0) {
+          e_own[q][0] = (A[0] + bm)[mo]; e_own[q][1] = (A[1] + bm)[mo]; e_own[q][2] = (A[2] + bm)[mo];
         }
-        if (vp_ok && in_slab(osx, osy[q], szp)) {
-          const long long mi = midx(p, oi, oj[q], osx, osy[q], szp);
-          e_vel[q][0] = A[3][mi]; e_vel[q][1] = A[4][mi]; e_vel[q][2] = A[5][mi];
+        if (p_in && mo >= 0) {
+          e_vel[q][0] = (A[3] + bp)[mo]; e_vel[q][1] = (A[4] + bp)[mo]; e_vel[q][2] = (A[5] + bp)[mo];
         }
       }
       e_halo[0] = e_halo[1] = e_halo[2] = 0.f;
-      if (hv && sm_ok && in_slab(hsx, hsy, szm)) {
-        const long long mi = midx(m, hi, hj, hsx, hsy, szm);
-        e_halo[0] = A[0][mi]; e_halo[1] = A[1][mi]; e_halo[2] = A[2][mi];
+      const int hmo = CLS == CLS_X ? hmx : (CLS == CLS_Y ? hmy : (hv ? hfo : -1));
+      if (m_in && hmo >= 0) {
+        e_halo[0] = (A[0] + bm)[hmo]; e_halo[1] = (A[1] + bm)[hmo]; e_halo[2] = (A[2] + bm)[hmo];
       }
     }
     // every thread waits for load group g(m) itself (try_wait suspends the
@@ -422,15 +428,15 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       const long long mzp = (long long)sz * ny * px;
       const long long cpl = (long long)m * pl;
 
-      // one stress cell: box/ring offsets, grid (i, j), slab indices,
+      // one stress cell: box/ring offsets, grid (i, j), in-plane offsets of
+      // its fields (fo) and x/y memory variables (-1 outside the slab),
       // components (1 normal, 2 xy, 4 xz, 8 yz); own = this CTA stores it
-      auto stress = [&](int b, int r, int i, int j, int sx, int sy, int comps, bool own, const float* pre) {
+      auto stress = [&](int b, int r, int i, int j, int fo, int mx_, int my_, int comps, bool own,
+                        const float* pre) {
         const bool st = own && st_plane;
-        const long long c = cpl + (long long)j * px + i;
-        const bool hx = xs_tile && sx >= 0, hy = ys_tile && sy >= 0;
-        const long long mxi = mxp + (long long)j * wx + sx;
-        const long long myi = myp + (long long)sy * px + i;
-        const long long mzi = mzp + (long long)j * px + i;
+        const long long c = cpl + fo;
+        const bool hx = UX && mx_ >= 0, hy = UY && my_ >= 0;
+        const int mxi = mx_, myi = my_, mzi = fo;
         // every time-n memory variable and coefficient of the cell, issued
         // together so their latencies overlap
         float qx0 = 0.f, qx1 = 0.f, qx2 = 0.f, qy0 = 0.f, qy1 = 0.f, qy2 = 0.f;
@@ -439,24 +445,24 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
         if (hx) {
           if (EARLY) { qx0 = pre[0]; qx1 = pre[1]; qx2 = pre[2]; }
-          else { qx0 = s.m.x[0][mxi]; qx1 = s.m.x[1][mxi]; qx2 = s.m.x[2][mxi]; }
+          else { qx0 = (s.m.x[0] + mxp)[mxi]; qx1 = (s.m.x[1] + mxp)[mxi]; qx2 = (s.m.x[2] + mxp)[mxi]; }
           const float* cx = cfx + (i - i0 + 4);
           xa = cx[0]; xb = cx[BX]; xk = cx[2 * BX]; xah = cx[3 * BX]; xbh = cx[4 * BX]; xkh = cx[5 * BX];
         }
         if (hy) {
           if (EARLY) { qy0 = pre[0]; qy1 = pre[1]; qy2 = pre[2]; }
-          else { qy0 = s.m.y[0][myi]; qy1 = s.m.y[1][myi]; qy2 = s.m.y[2][myi]; }
+          else { qy0 = (s.m.y[0] + myp)[myi]; qy1 = (s.m.y[1] + myp)[myi]; qy2 = (s.m.y[2] + myp)[myi]; }
           const float* cy = cfy + (j - j0 + 1);
           ya = cy[0]; yb = cy[G::RY]; yk = cy[2 * G::RY]; yah = cy[3 * G::RY]; ybh = cy[4 * G::RY];
           ykh = cy[5 * G::RY];
         }
         if (zs) {
           if (EARLY) { qz0 = pre[0]; qz1 = pre[1]; qz2 = pre[2]; }
-          else { qz0 = s.m.z[0][mzi]; qz1 = s.m.z[1][mzi]; qz2 = s.m.z[2][mzi]; }
+          else { qz0 = (s.m.z[0] + mzp)[mzi]; qz1 = (s.m.z[1] + mzp)[mzi]; qz2 = (s.m.z[2] + mzp)[mzi]; }
         }
         // psi(n+1) = b psi(n) + a d ; d' = d / K + psi(n+1) (3D:846-852 and
         // the other sweeps); unchanged where the component is not updated
-        auto psi = [&](float d, bool upd, float old, float* mB, long long mi, float a_, float b_, float k_) {
+        auto psi = [&](float d, bool upd, float old, float* mB, int mi, float a_, float b_, float k_) {
           const float nw = upd ? b_ * old + a_ * d : old;
           if (st) mB[mi] = nw;
           return d * k_ + nw;
@@ -467,9 +473,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float d2 = (vyc - VY0[b - BX]) * s.ody;
           float d3 = (vzc - VZm[b]) * s.odz;
           const bool upd = !edge || (m >= 1 && j >= 1 && i <= nx - 2);
-          if (hx) d1 = psi(d1, upd, qx0, s.mb.x[0], mxi, xah, xbh, xkh);
-          if (hy) d2 = psi(d2, upd, qy1, s.mb.y[1], myi, ya, yb, yk);
-          if (zs) d3 = psi(d3, upd, qz2, s.mb.z[2], mzi, za, zb, zk);
+          if (hx) d1 = psi(d1, upd, qx0, s.mb.x[0] + mxp, mxi, xah, xbh, xkh);
+          if (hy) d2 = psi(d2, upd, qy1, s.mb.y[1] + myp, myi, ya, yb, yk);
+          if (zs) d3 = psi(d3, upd, qz2, s.mb.z[2] + mzp, mzi, za, zb, zk);
           float dl = s.dt_lam, dl2m = s.dt_l2m;
           if (HET) {
             const float lh = 0.5f * (Lm[b + 1] + Lm[b]);
@@ -489,8 +495,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float d1 = (vyc - VY0[b - 1]) * s.odx;
           float d2 = (VX0[b + BX] - vxc) * s.ody;
           const bool upd = !edge || (j <= ny - 2 && i >= 1);
-          if (hx) d1 = psi(d1, upd, qx1, s.mb.x[1], mxi, xa, xb, xk);
-          if (hy) d2 = psi(d2, upd, qy0, s.mb.y[0], myi, yah, ybh, ykh);
+          if (hx) d1 = psi(d1, upd, qx1, s.mb.x[1] + mxp, mxi, xa, xb, xk);
+          if (hy) d2 = psi(d2, upd, qy0, s.mb.y[0] + myp, myi, yah, ybh, ykh);
           const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
           const float o = SO[3 * SLOT + b];
           const float n = upd ? o + dm * (d1 + d2) : o;
@@ -501,8 +507,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float d1 = (vzc - VZ0[b - 1]) * s.odx;
           float d2 = (VX1[b] - vxc) * s.odz;
           const bool upd = !edge || (m <= nz - 2 && i >= 1);
-          if (hx) d1 = psi(d1, upd, qx2, s.mb.x[2], mxi, xa, xb, xk);
-          if (zs) d2 = psi(d2, upd, qz0, s.mb.z[0], mzi, zah, zbh, zkh);
+          if (hx) d1 = psi(d1, upd, qx2, s.mb.x[2] + mxp, mxi, xa, xb, xk);
+          if (zs) d2 = psi(d2, upd, qz0, s.mb.z[0] + mzp, mzi, zah, zbh, zkh);
           const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
           const float o = SO[4 * SLOT + b];
           const float n = upd ? o + dm * (d1 + d2) : o;
@@ -513,8 +519,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float d1 = (VZ0[b + BX] - vzc) * s.ody;
           float d2 = (VY1[b] - vyc) * s.odz;
           const bool upd = !edge || (m <= nz - 2 && j <= ny - 2);
-          if (hy) d1 = psi(d1, upd, qy2, s.mb.y[2], myi, yah, ybh, ykh);
-          if (zs) d2 = psi(d2, upd, qz1, s.mb.z[1], mzi, zah, zbh, zkh);
+          if (hy) d1 = psi(d1, upd, qy2, s.mb.y[2] + myp, myi, yah, ybh, ykh);
+          if (zs) d2 = psi(d2, upd, qz1, s.mb.z[1] + mzp, mzi, zah, zbh, zkh);
           float dm = s.dt_mu;
           if (HET) {  // 8-point average at (i+1/2, j+1/2, k+1/2); i+1 clamped on the last column
             const int di = (i < nx - 1) ? 1 : 0;
@@ -534,9 +540,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (ov[q]) {
           const int b = b_own + q * 8 * BX;
           nvx[q] = VX0[b]; nvy[q] = VY0[b]; nvz[q] = VZ0[b];
-          stress(b, r_own + q * 8 * RX, oi, oj[q], osx, osy[q], 15, true, e_own[q]);
+          stress(b, r_own + q * 8 * RX, oi, oj[q], ofo[q], omx[q], omy[q], 15, true, e_own[q]);
         }
-      if (hv) stress(hb, hr, hi, hj, hsx, hsy, hcomps, false, e_halo);
+      if (hv) stress(hb, hr, hi, hj, hfo, hmx, hmy, hcomps, false, e_halo);
     }
     if (!__syncthreads_and(landed ? 1 : 0)) { ok_all = false; break; }
     // g(m+2) goes into slots whose last reader was stress(m) (own-cell
@@ -625,11 +631,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           if (!ov[q]) continue;
           const int i = oi, j = oj[q];
           const int b = b_own + q * 8 * BX, r = r_own + q * 8 * RX;
-          const long long c = cpl + (long long)j * px + i;
-          const bool hx = xs_tile && osx >= 0, hy = ys_tile && osy[q] >= 0;
-          const long long mxi = mxp + (long long)j * wx + osx;
-          const long long myi = myp + (long long)osy[q] * px + i;
-          const long long mzi = mzp + (long long)j * px + i;
+          const long long c = cpl + ofo[q];
+          const bool hx = UX && omx[q] >= 0, hy = UY && omy[q] >= 0;
+          const int mxi = omx[q], myi = omy[q], mzi = ofo[q];
           // the velocity sweep's memory variables and coefficients, issued together
           float qx3 = 0.f, qx4 = 0.f, qx5 = 0.f, qy3 = 0.f, qy4 = 0.f, qy5 = 0.f;
           float qz3 = 0.f, qz4 = 0.f, qz5 = 0.f;
@@ -637,20 +641,20 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float ya = 0.f, yb = 0.f, yk = 1.f, yah = 0.f, ybh = 0.f, ykh = 1.f;
           if (hx) {
             if (EARLY) { qx3 = e_vel[q][0]; qx4 = e_vel[q][1]; qx5 = e_vel[q][2]; }
-            else { qx3 = s.m.x[3][mxi]; qx4 = s.m.x[4][mxi]; qx5 = s.m.x[5][mxi]; }
+            else { qx3 = (s.m.x[3] + mxp)[mxi]; qx4 = (s.m.x[4] + mxp)[mxi]; qx5 = (s.m.x[5] + mxp)[mxi]; }
             const float* cx = cfx + (i - i0 + 4);
             xa = cx[0]; xb = cx[BX]; xk = cx[2 * BX]; xah = cx[3 * BX]; xbh = cx[4 * BX]; xkh = cx[5 * BX];
           }
           if (hy) {
             if (EARLY) { qy3 = e_vel[q][0]; qy4 = e_vel[q][1]; qy5 = e_vel[q][2]; }
-            else { qy3 = s.m.y[3][myi]; qy4 = s.m.y[4][myi]; qy5 = s.m.y[5][myi]; }
+            else { qy3 = (s.m.y[3] + myp)[myi]; qy4 = (s.m.y[4] + myp)[myi]; qy5 = (s.m.y[5] + myp)[myi]; }
             const float* cy = cfy + (j - j0 + 1);
             ya = cy[0]; yb = cy[G::RY]; yk = cy[2 * G::RY]; yah = cy[3 * G::RY]; ybh = cy[4 * G::RY];
             ykh = cy[5 * G::RY];
           }
           if (zs) {
             if (EARLY) { qz3 = e_vel[q][0]; qz4 = e_vel[q][1]; qz5 = e_vel[q][2]; }
-            else { qz3 = s.m.z[3][mzi]; qz4 = s.m.z[4][mzi]; qz5 = s.m.z[5][mzi]; }
+            else { qz3 = (s.m.z[3] + mzp)[mzi]; qz4 = (s.m.z[4] + mzp)[mzi]; qz5 = (s.m.z[5] + mzp)[mzi]; }
           }
           const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
           const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
@@ -667,25 +671,25 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           const bool uy = !edge || (p >= 1 && j <= ny - 2 && i <= nx - 2);
           const bool uz = !edge || (p <= nz - 2 && j >= 1 && i <= nx - 2);
           // in place: updated where the component is (3D:979-985 and the like)
-          auto psi = [&](float d, bool upd, float old, float* mm, long long mi, float a_, float b_, float k_) {
+          auto psi = [&](float d, bool upd, float old, float* mm, int mi, float a_, float b_, float k_) {
             float nw = old;
             if (upd) { nw = b_ * old + a_ * d; mm[mi] = nw; }
             return d * k_ + nw;
           };
           if (hx) {
-            d1 = psi(d1, ux, qx3, s.m.x[3], mxi, xa, xb, xk);
-            e1 = psi(e1, uy, qx4, s.m.x[4], mxi, xah, xbh, xkh);
-            f1 = psi(f1, uz, qx5, s.m.x[5], mxi, xah, xbh, xkh);
+            d1 = psi(d1, ux, qx3, s.m.x[3] + mxp, mxi, xa, xb, xk);
+            e1 = psi(e1, uy, qx4, s.m.x[4] + mxp, mxi, xah, xbh, xkh);
+            f1 = psi(f1, uz, qx5, s.m.x[5] + mxp, mxi, xah, xbh, xkh);
           }
           if (hy) {
-            d2 = psi(d2, ux, qy3, s.m.y[3], myi, ya, yb, yk);
-            e2 = psi(e2, uy, qy4, s.m.y[4], myi, yah, ybh, ykh);
-            f2 = psi(f2, uz, qy5, s.m.y[5], myi, ya, yb, yk);
+            d2 = psi(d2, ux, qy3, s.m.y[3] + myp, myi, ya, yb, yk);
+            e2 = psi(e2, uy, qy4, s.m.y[4] + myp, myi, yah, ybh, ykh);
+            f2 = psi(f2, uz, qy5, s.m.y[5] + myp, myi, ya, yb, yk);
           }
           if (zs) {
-            d3 = psi(d3, ux, qz3, s.m.z[3], mzi, za, zb, zk);
-            e3 = psi(e3, uy, qz4, s.m.z[4], mzi, za, zb, zk);
-            f3 = psi(f3, uz, qz5, s.m.z[5], mzi, zah, zbh, zkh);
+            d3 = psi(d3, ux, qz3, s.m.z[3] + mzp, mzi, za, zb, zk);
+            e3 = psi(e3, uy, qz4, s.m.z[4] + mzp, mzi, za, zb, zk);
+            f3 = psi(f3, uz, qz5, s.m.z[5] + mzp, mzi, zah, zbh, zkh);
           }
           float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
           if (HET) {
