@@ -371,6 +371,15 @@ int build_axis(cpml_handle* h, int axis, int n, double delta) {
   for (int i = n - 1; i >= n / 2; --i) if (nzero(i)) hi = n - i;
   for (int i = lo; i < n - hi; ++i)
     if (nzero(i)) { lo = n; hi = 0; break; }
+  // 3D x slab, stored [k][j][sx]: each side widened to whole 32-byte
+  // sectors, so that the two sides of a row never share a sector and a
+  // row's memory variables are read and written as full sectors. The added
+  // points lie outside the layer (a = 0, b = 1, 1/K = 1): their memory
+  // variables stay zero and leave the derivatives unchanged.
+  if (h->ndim == 3 && axis == 0 && lo < n) {
+    const int lo8 = (lo + 7) / 8 * 8, hi8 = (hi + 7) / 8 * 8;
+    if (lo8 + hi8 < n) { lo = lo8; hi = hi8; }
+  }
   Axis& A = h->axes[axis];
   const float* f = h->prof32[axis];
   A.a = f; A.b = f + n; A.ik = f + 2 * n; A.ah = f + 3 * n; A.bh = f + 4 * n; A.ikh = f + 5 * n;

@@ -63,6 +63,22 @@ constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
+// Which updates of a cell apply as far as its (i, j) go, for the general
+// path's face handling (the plane conditions are added per plane):
+//   bit 0 sigma_xx/yy/zz  j >= 1, i <= NX-2     bit 4 v_x   j >= 1, i >= 1
+//   bit 1 sigma_xy        j <= NY-2, i >= 1     bit 5 v_y   j <= NY-2, i <= NX-2
+//   bit 2 sigma_xz        i >= 1                bit 6 v_z   j >= 1, i <= NX-2
+//   bit 3 sigma_yz        j <= NY-2             bit 7 on an x or y face (rigid)
+__device__ __forceinline__ int cell_bits(int i, int j, int nx, int ny) {
+  const bool jl = j >= 1, jh = j <= ny - 2, il = i >= 1, ih = i <= nx - 2;
+  return (jl && ih ? 1 : 0) | (jh && il ? 2 : 0) | (il ? 4 : 0) | (jh ? 8 : 0) | (jl && il ? 16 : 0) |
+         (jh && ih ? 32 : 0) | (jl && ih ? 64 : 0) | (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 ? 128 : 0);
+}
+// position of the n-th (0-based) set bit of m
+__device__ __forceinline__ int nth_set(unsigned m, int n) {
+  for (int k = 0; k < n; ++k) m &= m - 1;
+  return __ffs(m) - 1;
+}
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
@@ -253,33 +269,57 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
   // A plane's base is added per plane, so every access is one 32-bit offset
   // from a plane pointer.
   const int pxi = (int)px;
-  const int oi = i0 + tx;
+  // The thread's own cell (cx, cy) in the tile: lanes are columns, except in
+  // X-class items, where the tile's x-slab columns are packed into the lowest
+  // warps (then its other columns inside the grid, then those past it) so
+  // that only those warps run the C-PML code -- a warp pays for a branch
+  // whether 10 or 32 of its lanes take it. Halo cells go to the highest
+  // warps (hid counts down from the last thread).
+  static_assert(CLS != CLS_X || TY * FTX == FNT, "X-class items are one cell per thread");
+  int cx = tx, cy = ty;
+  if (CLS == CLS_X) {
+    const int ci = i0 + tx;
+    const unsigned vmask = __ballot_sync(0xffffffffu, ci < nx);
+    const unsigned smask = __ballot_sync(0xffffffffu, ci < nx && s.ax.slab(ci) >= 0);
+    const unsigned grp[3] = {smask, vmask & ~smask, ~vmask};
+    int u = tid;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+      const int w = __popc(grp[g]);
+      if (u >= 0 && u < w * TY) { cy = u / w; cx = nth_set(grp[g], u % w); }
+      u -= w * TY;
+    }
+  }
+  const int oi = i0 + cx;
   const int osx = (oi < nx) ? s.ax.slab(oi) : -1;
-  int oj[NQ], ofo[NQ], omx[NQ], omy[NQ];
+  int oj[NQ], ofo[NQ], omx[NQ], omy[NQ], ocb[NQ];
   bool ov[NQ], oe[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
-    oj[q] = j0 + ty + 8 * q;
+    oj[q] = j0 + cy + 8 * q;
     ov[q] = oi < nx && oj[q] < ny;
     const int osy = ov[q] ? s.ay.slab(oj[q]) : -1;
     ofo[q] = oj[q] * pxi + oi;
     omx[q] = (UX && xs_tile && ov[q] && osx >= 0) ? oj[q] * wx + osx : -1;
     omy[q] = (UY && ys_tile && osy >= 0) ? osy * pxi + oi : -1;
     oe[q] = e_full_xy || (oi >= n0 && oi < nx - n0 && oj[q] >= n0 && oj[q] < ny - n0);
+    ocb[q] = cell_bits(oi, oj[q], nx, ny);
   }
-  const int b_own = (ty + 1) * BX + tx + 4;
-  const int r_own = (ty + 1) * RX + tx + 1;
+  const int b_own = (cy + 1) * BX + cx + 4;
+  const int r_own = (cy + 1) * RX + cx + 1;
+  const int hid = FNT - 1 - tid;
   int hi = 0, hj = 0, hcomps = 0;
-  if (tid < G::NH) {
-    if (tid < FTX) { hi = i0 + tid; hj = j0 + TY; hcomps = 1; }                        // top: yy
-    else if (tid < 2 * FTX) { hi = i0 + tid - FTX; hj = j0 - 1; hcomps = 2 | 8; }       // bottom: xy, yz
-    else if (tid < 2 * FTX + TY) { hi = i0 - 1; hj = j0 + tid - 2 * FTX; hcomps = 1; }  // left: xx
-    else { hi = i0 + FTX; hj = j0 + tid - 2 * FTX - TY; hcomps = 2 | 4; }               // right: xy, xz
+  if (hid < G::NH) {
+    if (hid < FTX) { hi = i0 + hid; hj = j0 + TY; hcomps = 1; }                        // top: yy
+    else if (hid < 2 * FTX) { hi = i0 + hid - FTX; hj = j0 - 1; hcomps = 2 | 8; }       // bottom: xy, yz
+    else if (hid < 2 * FTX + TY) { hi = i0 - 1; hj = j0 + hid - 2 * FTX; hcomps = 1; }  // left: xx
+    else { hi = i0 + FTX; hj = j0 + hid - 2 * FTX - TY; hcomps = 2 | 4; }               // right: xy, xz
   }
-  const bool hv = tid < G::NH && hi >= 0 && hi < nx && hj >= 0 && hj < ny;
+  const bool hv = hid < G::NH && hi >= 0 && hi < nx && hj >= 0 && hj < ny;
   const int hfo = hj * pxi + hi;
   const int hmx = (UX && xs_tile && hv && s.ax.slab(hi) >= 0) ? hj * wx + s.ax.slab(hi) : -1;
   const int hmy = (UY && ys_tile && hv && s.ay.slab(hj) >= 0) ? s.ay.slab(hj) * pxi + hi : -1;
+  const int hcb = cell_bits(hi, hj, nx, ny);
   const int hb = (hj - j0 + 1) * BX + (hi - i0 + 4);
   const int hr = (hj - j0 + 1) * RX + (hi - i0 + 1);
 
@@ -407,7 +447,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       for (int q = 0; q < NQ; ++q)
         cell(b_own + q * 8 * BX, r_own + q * 8 * RX, 15, st_plane, cpl + (long long)(ty + 8 * q) * px + tx,
              nvx[q], nvy[q], nvz[q]);
-      if (tid < G::NH) {
+      if (hid < G::NH) {
         float dx, dy, dz;
         cell(hb, hr, hcomps, false, 0, dx, dy, dz);
       }
@@ -431,9 +471,13 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       // one stress cell: box/ring offsets, grid (i, j), in-plane offsets of
       // its fields (fo) and x/y memory variables (-1 outside the slab),
       // components (1 normal, 2 xy, 4 xz, 8 yz); own = this CTA stores it
-      auto stress = [&](int b, int r, int i, int j, int fo, int mx_, int my_, int comps, bool own,
+      // updates that apply at plane m (bits 0-3 of cell_bits): all of them
+      // away from the faces
+      const int sbits = edge ? (m >= 1 ? 1 : 0) | 2 | (m <= nz - 2 ? 12 : 0) : 15;
+      auto stress = [&](int b, int r, int i, int j, int fo, int mx_, int my_, int cb, int comps, bool own,
                         const float* pre) {
         const bool st = own && st_plane;
+        const int ok = edge ? (cb & sbits) : 15;
         const long long c = cpl + fo;
         const bool hx = UX && mx_ >= 0, hy = UY && my_ >= 0;
         const int mxi = mx_, myi = my_, mzi = fo;
@@ -472,7 +516,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float d1 = (VX0[b + 1] - vxc) * s.odx;
           float d2 = (vyc - VY0[b - BX]) * s.ody;
           float d3 = (vzc - VZm[b]) * s.odz;
-          const bool upd = !edge || (m >= 1 && j >= 1 && i <= nx - 2);
+          const bool upd = ok & 1;
           if (hx) d1 = psi(d1, upd, qx0, s.mb.x[0] + mxp, mxi, xah, xbh, xkh);
           if (hy) d2 = psi(d2, upd, qy1, s.mb.y[1] + myp, myi, ya, yb, yk);
           if (zs) d3 = psi(d3, upd, qz2, s.mb.z[2] + mzp, mzi, za, zb, zk);
@@ -494,7 +538,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (comps & 2) {  // sigma_xy: k = 1..NZ, j = 1..NY-1, i = 2..NX (3D:877-894)
           float d1 = (vyc - VY0[b - 1]) * s.odx;
           float d2 = (VX0[b + BX] - vxc) * s.ody;
-          const bool upd = !edge || (j <= ny - 2 && i >= 1);
+          const bool upd = ok & 2;
           if (hx) d1 = psi(d1, upd, qx1, s.mb.x[1] + mxp, mxi, xa, xb, xk);
           if (hy) d2 = psi(d2, upd, qy0, s.mb.y[0] + myp, myi, yah, ybh, ykh);
           const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
@@ -506,7 +550,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (comps & 4) {  // sigma_xz: k = 1..NZ-1, j = 1..NY, i = 2..NX (3D:908-925)
           float d1 = (vzc - VZ0[b - 1]) * s.odx;
           float d2 = (VX1[b] - vxc) * s.odz;
-          const bool upd = !edge || (m <= nz - 2 && i >= 1);
+          const bool upd = ok & 4;
           if (hx) d1 = psi(d1, upd, qx2, s.mb.x[2] + mxp, mxi, xa, xb, xk);
           if (zs) d2 = psi(d2, upd, qz0, s.mb.z[0] + mzp, mzi, zah, zbh, zkh);
           const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
@@ -518,7 +562,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (comps & 8) {  // sigma_yz: k = 1..NZ-1, j = 1..NY-1, i = 1..NX (3D:927-942)
           float d1 = (VZ0[b + BX] - vzc) * s.ody;
           float d2 = (VY1[b] - vyc) * s.odz;
-          const bool upd = !edge || (m <= nz - 2 && j <= ny - 2);
+          const bool upd = ok & 8;
           if (hy) d1 = psi(d1, upd, qy2, s.mb.y[2] + myp, myi, yah, ybh, ykh);
           if (zs) d2 = psi(d2, upd, qz1, s.mb.z[1] + mzp, mzi, zah, zbh, zkh);
           float dm = s.dt_mu;
@@ -540,9 +584,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         if (ov[q]) {
           const int b = b_own + q * 8 * BX;
           nvx[q] = VX0[b]; nvy[q] = VY0[b]; nvz[q] = VZ0[b];
-          stress(b, r_own + q * 8 * RX, oi, oj[q], ofo[q], omx[q], omy[q], 15, true, e_own[q]);
+          stress(b, r_own + q * 8 * RX, oi, oj[q], ofo[q], omx[q], omy[q], ocb[q], 15, true, e_own[q]);
         }
-      if (hv) stress(hb, hr, hi, hj, hfo, hmx, hmy, hcomps, false, e_halo);
+      if (hv) stress(hb, hr, hi, hj, hfo, hmx, hmy, hcb, hcomps, false, e_halo);
     }
     if (!__syncthreads_and(landed ? 1 : 0)) { ok_all = false; break; }
     // g(m+2) goes into slots whose last reader was stress(m) (own-cell
@@ -615,6 +659,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         const float* R0 = rhs + (p & 3) * SLOT;
         const float* R1 = rhs + ((p + 1) & 3) * SLOT;
         const bool edge = edge_tile || p < 1 || p > nz - 2;
+        // updates that apply at plane p (bits 4-7 of cell_bits)
+        const int vbits = (p >= 1 ? 48 : 0) | (p <= nz - 2 ? 64 : 0) | 128;
+        const bool pface = p == 0 || p == nz - 1;
         const int sz = UZ ? s.az.slab(p) : -1;
         const bool zs = UZ && sz >= 0;
         float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
@@ -667,9 +714,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           float f1 = (Sxz0[r + 1] - sxz) * s.odx;  // v_z (3D:1031-1052)
           float f2 = (syz - Syz0[r - RX]) * s.ody;
           float f3 = (Szz1[r] - szz) * s.odz;
-          const bool ux = !edge || (p >= 1 && j >= 1 && i >= 1);
-          const bool uy = !edge || (p >= 1 && j <= ny - 2 && i <= nx - 2);
-          const bool uz = !edge || (p <= nz - 2 && j >= 1 && i <= nx - 2);
+          const int ok = edge ? (ocb[q] & vbits) : 112;
+          const bool ux = ok & 16, uy = ok & 32, uz = ok & 64;
           // in place: updated where the component is (3D:979-985 and the like)
           auto psi = [&](float d, bool upd, float old, float* mm, int mi, float a_, float b_, float k_) {
             float nw = old;
@@ -710,7 +756,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
             vx += src_x;
             vy += src_y;
           }
-          if (edge && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || p == 0 || p == nz - 1)) {
+          if (edge && ((ok & 128) || pface)) {
             vx = 0.f; vy = 0.f; vz = 0.f;  // rigid faces (3D:1087-1121)
           }
           s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
@@ -782,7 +828,8 @@ static EncodeTiledFn encode_fn() {
 
 // 3D map over one padded FP32 field: dims (nx, ny, nz), row pitch px floats;
 // box (32 + 8) x (TY + 2) x 1; out-of-range elements read as zero.
-static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int px, int ty) {
+static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int px, int ty,
+                     CUtensorMapL2promotion promo) {
   EncodeTiledFn fn = encode_fn();
   if (!fn || !base) return false;
   cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
@@ -790,7 +837,7 @@ static bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, 
   cuuint32_t box[3] = {FTX + 8, (cuuint32_t)(ty + 2), 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, promo,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -936,12 +983,18 @@ bool fused3d_make_maps(void* plan_mem, float* const fields[2][9], const float* l
     for (int pass = 0; pass < 2; ++pass) {
       TmapSet& M = pass == 0 ? P->maps[q] : P->gmaps[q];
       const int rows = pass == 0 ? ty : 8;
+      // Interior boxes promote their L2 fills to whole 128-byte lines (the
+      // neighbouring tiles read the rest of those lines at about the same
+      // time); the general classes' neighbours are mostly interior tiles of
+      // another kernel, so their halo columns fetch 64-byte pieces only.
+      const CUtensorMapL2promotion promo =
+          pass == 0 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B : CU_TENSOR_MAP_L2_PROMOTION_L2_64B;
       for (int f = 0; f < 9; ++f)
-        if (!make_map(&M.f[f], fields[q][f], nx, ny, nz, px, rows)) return false;
+        if (!make_map(&M.f[f], fields[q][f], nx, ny, nz, px, rows, promo)) return false;
       if (het) {
-        if (!make_map(&M.lam, lam, nx, ny, nz, px, rows)) return false;
-        if (!make_map(&M.mu, mu, nx, ny, nz, px, rows)) return false;
-        if (!make_map(&M.rho, rho, nx, ny, nz, px, rows)) return false;
+        if (!make_map(&M.lam, lam, nx, ny, nz, px, rows, promo)) return false;
+        if (!make_map(&M.mu, mu, nx, ny, nz, px, rows, promo)) return false;
+        if (!make_map(&M.rho, rho, nx, ny, nz, px, rows, promo)) return false;
       } else {
         M.lam = M.f[0];
         M.mu = M.f[0];
