@@ -96,10 +96,14 @@ __device__ __forceinline__ void stage_shot(const Shot2D* shots, int id, Shot2D& 
   cur = id;
 }
 
-// 6 resident CTAs per SM (40 registers, no spills): the kernel is bound by
-// memory latency, and 48 warps per SM hide more of it than the 40 the
-// unconstrained register count (48) allows; 8 CTAs would spill.
-__global__ void __launch_bounds__(BNT, 6) batch2d_kernel(BatchArgs a) {
+// 5 resident CTAs per SM (48 registers, no spills): the kernel is bound by
+// memory latency. The cell updates issue all of a cell's loads before its
+// stores, which takes more registers than 6 CTAs per SM leave (40) but
+// covers a cell's reads with one latency instead of two or three (36.6 ->
+// 39.6 Gcell-updates/s on a 32-shot batch). Taking two items per loop
+// iteration with both cells' loads first needs ~90 registers per thread and
+// spilled at every occupancy.
+__global__ void __launch_bounds__(BNT, 5) batch2d_kernel(BatchArgs a) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   __shared__ Shot2D shw[BNT / 32];  // one descriptor copy per warp
   Shot2D& sh = shw[ty];

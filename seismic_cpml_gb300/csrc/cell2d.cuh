@@ -24,6 +24,17 @@ __device__ __forceinline__ float pml2(float d, int sidx, float* __restrict__ mem
   return fmaf(d, __ldg(ik + idx), m);                                            // 2D:577-578
 }
 
+// pml2 with the memory variable's old value already loaded (old); the same
+// arithmetic.
+__device__ __forceinline__ float pml2v(float d, int sidx, float old, float* __restrict__ mem, long long midx,
+                                       const float* __restrict__ a, const float* __restrict__ b,
+                                       const float* __restrict__ ik, int idx) {
+  if (sidx < 0) return d;
+  const float m = fmaf(__ldg(b + idx), old, __fmul_rn(__ldg(a + idx), d));  // 2D:574-575
+  mem[midx] = m;
+  return fmaf(d, __ldg(ik + idx), m);                                      // 2D:577-578
+}
+
 // Everything one 2D shot's cell updates read or write.
 struct Shot2D {
   int nx, ny, px;              // grid and row pitch (floats)
@@ -73,45 +84,83 @@ struct GlobalView {
   }
 };
 
-// Stress update of cell (i, j), 0-based.
+// Stress update of cell (i, j), 0-based, in two halves: stress2d_load
+// issues every load of the cell (fields, memory variables, per-cell model),
+// stress2d_store computes and stores. The arrays never overlap, but the
+// compiler cannot know that and would hold each load behind the stores
+// before it; with the loads first, one memory latency covers the cell (or,
+// in a kernel that loads two cells before storing either, both cells). The
+// arithmetic does not depend on the order.
+struct StressIn {
+  int sx, sy;
+  long long c, mx, my;
+  bool un, us;   // sigma_xx/yy and sigma_xy updated
+  float vxc, vyc, vxe, vys, oxx, oyy, vyw, vxn, oxy;
+  float qx0, qy1, qx1, qy0;
+  float l0, l1, m0, m1, mn;
+};
 template <bool HET, class V>
-__device__ __forceinline__ void stress2d_cell(const Shot2D& s, const V& v, int i, int j) {
-  const int sx = s.ax.slab(i), sy = s.ay.slab(j);
+__device__ __forceinline__ StressIn stress2d_load(const Shot2D& s, const V& v, int i, int j) {
+  StressIn r;
+  r.sx = s.ax.slab(i); r.sy = s.ay.slab(j);
   const long long px = v.pitch();
-  const long long c = v.at(i, j);
-  const long long mx = v.mxi(i, j, sx);
-  const long long my = v.myi(i, j, sy);
-  float* const VX = v.vx();
-  float* const VY = v.vy();
-  const float vxc = VX[c], vyc = VY[c];
-  // sigma_xx, sigma_yy: j = 2..NY, i = 1..NX-1
-  if (j >= 1 && i <= s.nx - 2) {
-    float d1 = __fmul_rn(__fsub_rn(VX[c + 1], vxc), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(vyc, VY[c - px]), s.ody);
-    d1 = pml2(d1, sx, v.mx(0), mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-    d2 = pml2(d2, sy, v.my(1), my, s.ay.a, s.ay.b, s.ay.ik, j);
+  r.c = v.at(i, j);
+  r.mx = v.mxi(i, j, r.sx);
+  r.my = v.myi(i, j, r.sy);
+  const long long c = r.c;
+  const float* const VX = v.vx();
+  const float* const VY = v.vy();
+  r.un = j >= 1 && i <= s.nx - 2;  // sigma_xx, sigma_yy: j = 2..NY, i = 1..NX-1
+  r.us = j <= s.ny - 2 && i >= 1;  // sigma_xy: j = 1..NY-1, i = 2..NX
+  r.vxc = VX[c]; r.vyc = VY[c];
+  r.vxe = r.vys = r.oxx = r.oyy = r.vyw = r.vxn = r.oxy = 0.f;
+  r.qx0 = r.qy1 = r.qx1 = r.qy0 = 0.f;
+  r.l0 = r.l1 = r.m0 = r.m1 = r.mn = 0.f;
+  if (r.un) {
+    r.vxe = VX[c + 1]; r.vys = VY[c - px]; r.oxx = v.sxx()[c]; r.oyy = v.syy()[c];
+    if (r.sx >= 0) r.qx0 = v.mx(0)[r.mx];
+    if (r.sy >= 0) r.qy1 = v.my(1)[r.my];
+    if (HET) { r.l1 = v.lam()[c + 1]; r.l0 = v.lam()[c]; r.m1 = v.mu()[c + 1]; }
+  }
+  if (r.us) {
+    r.vyw = VY[c - 1]; r.vxn = VX[c + px]; r.oxy = v.sxy()[c];
+    if (r.sx >= 0) r.qx1 = v.mx(1)[r.mx];
+    if (r.sy >= 0) r.qy0 = v.my(0)[r.my];
+    if (HET) r.mn = v.mu()[c + px];
+  }
+  if (HET && (r.un || r.us)) r.m0 = v.mu()[c];
+  return r;
+}
+template <bool HET, class V>
+__device__ __forceinline__ void stress2d_store(const Shot2D& s, const V& v, int i, int j, const StressIn& r) {
+  const long long c = r.c;
+  if (r.un) {
+    float d1 = __fmul_rn(__fsub_rn(r.vxe, r.vxc), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(r.vyc, r.vys), s.ody);
+    d1 = pml2v(d1, r.sx, r.qx0, v.mx(0), r.mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
+    d2 = pml2v(d2, r.sy, r.qy1, v.my(1), r.my, s.ay.a, s.ay.b, s.ay.ik, j);
     float dl = s.dt_lam, dl2m = s.dt_l2m;
     if (HET) {
-      const float lh = __fmul_rn(0.5f, __fadd_rn(v.lam()[c + 1], v.lam()[c]));
-      const float mh = __fmul_rn(0.5f, __fadd_rn(v.mu()[c + 1], v.mu()[c]));
+      const float lh = __fmul_rn(0.5f, __fadd_rn(r.l1, r.l0));
+      const float mh = __fmul_rn(0.5f, __fadd_rn(r.m1, r.m0));
       dl = __fmul_rn(s.dt, lh);
       dl2m = __fmul_rn(s.dt, fmaf(2.0f, mh, lh));
     }
-    float* const SXX = v.sxx();
-    float* const SYY = v.syy();
-    SXX[c] = __fadd_rn(SXX[c], fmaf(dl2m, d1, __fmul_rn(dl, d2)));
-    SYY[c] = __fadd_rn(SYY[c], fmaf(dl, d1, __fmul_rn(dl2m, d2)));
+    v.sxx()[c] = __fadd_rn(r.oxx, fmaf(dl2m, d1, __fmul_rn(dl, d2)));
+    v.syy()[c] = __fadd_rn(r.oyy, fmaf(dl, d1, __fmul_rn(dl2m, d2)));
   }
-  // sigma_xy: j = 1..NY-1, i = 2..NX
-  if (j <= s.ny - 2 && i >= 1) {
-    float d1 = __fmul_rn(__fsub_rn(vyc, VY[c - 1]), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(VX[c + px], vxc), s.ody);
-    d1 = pml2(d1, sx, v.mx(1), mx, s.ax.a, s.ax.b, s.ax.ik, i);
-    d2 = pml2(d2, sy, v.my(0), my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
-    const float dm = HET ? __fmul_rn(s.dt, __fmul_rn(0.5f, __fadd_rn(v.mu()[c + px], v.mu()[c]))) : s.dt_mu;
-    float* const SXY = v.sxy();
-    SXY[c] = fmaf(dm, __fadd_rn(d1, d2), SXY[c]);
+  if (r.us) {
+    float d1 = __fmul_rn(__fsub_rn(r.vyc, r.vyw), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(r.vxn, r.vxc), s.ody);
+    d1 = pml2v(d1, r.sx, r.qx1, v.mx(1), r.mx, s.ax.a, s.ax.b, s.ax.ik, i);
+    d2 = pml2v(d2, r.sy, r.qy0, v.my(0), r.my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
+    const float dm = HET ? __fmul_rn(s.dt, __fmul_rn(0.5f, __fadd_rn(r.mn, r.m0))) : s.dt_mu;
+    v.sxy()[c] = fmaf(dm, __fadd_rn(d1, d2), r.oxy);
   }
+}
+template <bool HET, class V>
+__device__ __forceinline__ void stress2d_cell(const Shot2D& s, const V& v, int i, int j) {
+  stress2d_store<HET>(s, v, i, j, stress2d_load<HET>(s, v, i, j));
 }
 
 template <bool HET>
@@ -120,41 +169,75 @@ __device__ __forceinline__ void stress2d_cell(const Shot2D& s, int i, int j) {
 }
 
 // Velocity update of cell (i, j) at 1-based step it, with source, rigid
-// edges, and the cell's energy and |v|^2 contributions.
+// edges, and the cell's energy and |v|^2 contributions; split into loads
+// and the rest as the stress update is.
+struct VelocityIn {
+  int sx, sy;
+  long long c, mx, my;
+  bool ux, uy, en;   // v_x, v_y updated; cell inside the energy interior
+  float vx, vy, sxx, syy, sxy, sxw, sys, sye, syn;
+  float qx2, qy2, qx3, qy3;
+  float r0, r1, r1n, rn, lc, mc;
+};
 template <bool HET, class V>
-__device__ __forceinline__ void velocity2d_cell(const Shot2D& s, const V& v, int i, int j, int it, float& ek,
-                                                float& ep, float& vm2, int& bad) {
-  const int sx = s.ax.slab(i), sy = s.ay.slab(j);
+__device__ __forceinline__ VelocityIn velocity2d_load(const Shot2D& s, const V& v, int i, int j) {
+  VelocityIn r;
+  r.sx = s.ax.slab(i); r.sy = s.ay.slab(j);
   const long long px = v.pitch();
-  const long long c = v.at(i, j);
-  const long long mx = v.mxi(i, j, sx);
-  const long long my = v.myi(i, j, sy);
-  float* const VX = v.vx();
-  float* const VY = v.vy();
+  r.c = v.at(i, j);
+  r.mx = v.mxi(i, j, r.sx);
+  r.my = v.myi(i, j, r.sy);
+  const long long c = r.c;
   const float* const SXX = v.sxx();
   const float* const SYY = v.syy();
   const float* const SXY = v.sxy();
-  float vx = VX[c], vy = VY[c];
-  const float sxx = SXX[c], syy = SYY[c], sxy = SXY[c];
-  // v_x: j = 2..NY, i = 2..NX
-  if (j >= 1 && i >= 1) {
-    float d1 = __fmul_rn(__fsub_rn(sxx, SXX[c - 1]), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(sxy, SXY[c - px]), s.ody);
-    d1 = pml2(d1, sx, v.mx(2), mx, s.ax.a, s.ax.b, s.ax.ik, i);
-    d2 = pml2(d2, sy, v.my(2), my, s.ay.a, s.ay.b, s.ay.ik, j);
-    const float f = HET ? __fdiv_rn(s.dt, v.rho()[c]) : s.dt_over_rho;
+  r.ux = j >= 1 && i >= 1;                  // v_x: j = 2..NY, i = 2..NX
+  r.uy = j <= s.ny - 2 && i <= s.nx - 2;    // v_y: j = 1..NY-1, i = 1..NX-1
+  const int n0 = s.npml;
+  r.en = i >= n0 && i < s.nx - n0 && j >= n0 && j < s.ny - n0;
+  r.vx = v.vx()[c]; r.vy = v.vy()[c];
+  r.sxx = SXX[c]; r.syy = SYY[c]; r.sxy = SXY[c];
+  r.sxw = r.sys = r.sye = r.syn = 0.f;
+  r.qx2 = r.qy2 = r.qx3 = r.qy3 = 0.f;
+  r.r0 = r.r1 = r.r1n = r.rn = r.lc = r.mc = 0.f;
+  if (r.ux) {
+    r.sxw = SXX[c - 1]; r.sys = SXY[c - px];
+    if (r.sx >= 0) r.qx2 = v.mx(2)[r.mx];
+    if (r.sy >= 0) r.qy2 = v.my(2)[r.my];
+  }
+  if (r.uy) {
+    r.sye = SXY[c + 1]; r.syn = SYY[c + px];
+    if (r.sx >= 0) r.qx3 = v.mx(3)[r.mx];
+    if (r.sy >= 0) r.qy3 = v.my(3)[r.my];
+    if (HET) { r.r1 = v.rho()[c + 1]; r.r1n = v.rho()[c + 1 + px]; r.rn = v.rho()[c + px]; }
+  }
+  if (HET) {
+    if (r.ux || r.uy || r.en) r.r0 = v.rho()[c];
+    if (r.en) { r.lc = v.lam()[c]; r.mc = v.mu()[c]; }
+  }
+  return r;
+}
+template <bool HET, class V>
+__device__ __forceinline__ void velocity2d_store(const Shot2D& s, const V& v, int i, int j, int it,
+                                                 const VelocityIn& r, float& ek, float& ep, float& vm2, int& bad) {
+  const long long c = r.c;
+  float vx = r.vx, vy = r.vy;
+  if (r.ux) {
+    float d1 = __fmul_rn(__fsub_rn(r.sxx, r.sxw), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(r.sxy, r.sys), s.ody);
+    d1 = pml2v(d1, r.sx, r.qx2, v.mx(2), r.mx, s.ax.a, s.ax.b, s.ax.ik, i);
+    d2 = pml2v(d2, r.sy, r.qy2, v.my(2), r.my, s.ay.a, s.ay.b, s.ay.ik, j);
+    const float f = HET ? __fdiv_rn(s.dt, r.r0) : s.dt_over_rho;
     vx = fmaf(__fadd_rn(d1, d2), f, vx);
   }
-  // v_y: j = 1..NY-1, i = 1..NX-1
-  if (j <= s.ny - 2 && i <= s.nx - 2) {
-    float d1 = __fmul_rn(__fsub_rn(SXY[c + 1], sxy), s.odx);
-    float d2 = __fmul_rn(__fsub_rn(SYY[c + px], syy), s.ody);
-    d1 = pml2(d1, sx, v.mx(3), mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
-    d2 = pml2(d2, sy, v.my(3), my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
+  if (r.uy) {
+    float d1 = __fmul_rn(__fsub_rn(r.sye, r.sxy), s.odx);
+    float d2 = __fmul_rn(__fsub_rn(r.syn, r.syy), s.ody);
+    d1 = pml2v(d1, r.sx, r.qx3, v.mx(3), r.mx, s.ax.ah, s.ax.bh, s.ax.ikh, i);
+    d2 = pml2v(d2, r.sy, r.qy3, v.my(3), r.my, s.ay.ah, s.ay.bh, s.ay.ikh, j);
     float f = s.dt_over_rho;
     if (HET) {
-      const float* r = v.rho();
-      const float r4 = __fadd_rn(__fadd_rn(__fadd_rn(r[c], r[c + 1]), r[c + 1 + px]), r[c + px]);
+      const float r4 = __fadd_rn(__fadd_rn(__fadd_rn(r.r0, r.r1), r.r1n), r.rn);
       f = __fdiv_rn(s.dt, __fmul_rn(0.25f, r4));
     }
     vy = fmaf(__fadd_rn(d1, d2), f, vy);
@@ -164,27 +247,32 @@ __device__ __forceinline__ void velocity2d_cell(const Shot2D& s, const V& v, int
     vy = __fadd_rn(vy, s.src_fy[it - 1]);
   }
   if (i == 0 || i == s.nx - 1 || j == 0 || j == s.ny - 1) { vx = 0.f; vy = 0.f; }  // 2D:670-680
-  VX[c] = vx;
-  VY[c] = vy;
+  v.vx()[c] = vx;
+  v.vy()[c] = vy;
   const float v2 = vx * vx + vy * vy;
   vm2 = fmaxf(vm2, v2);
   bad |= not_finite(v2);
-  const int n0 = s.npml;
-  if (i >= n0 && i < s.nx - n0 && j >= n0 && j < s.ny - n0) {
+  if (r.en) {
     float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
     if (HET) {
-      const float l = v.lam()[c], m = v.mu()[c];
+      const float l = r.lc, m = r.mc;
       const float den = 1.0f / (4.0f * m * (l + m));
-      hr = 0.5f * v.rho()[c];
+      hr = 0.5f * r.r0;
       c1 = (l + 2.0f * m) * den;
       c2 = l * den;
       i2m = 1.0f / (2.0f * m);
     }
     ek += hr * v2;
+    const float sxx = r.sxx, syy = r.syy, sxy = r.sxy;
     const float exx = c1 * sxx - c2 * syy;
     const float eyy = c1 * syy - c2 * sxx;
     ep += 0.5f * (exx * sxx + eyy * syy) + i2m * (sxy * sxy);
   }
+}
+template <bool HET, class V>
+__device__ __forceinline__ void velocity2d_cell(const Shot2D& s, const V& v, int i, int j, int it, float& ek,
+                                                float& ep, float& vm2, int& bad) {
+  velocity2d_store<HET>(s, v, i, j, it, velocity2d_load<HET>(s, v, i, j), ek, ep, vm2, bad);
 }
 
 template <bool HET>
