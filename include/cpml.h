@@ -62,9 +62,7 @@ extern "C" {
                                     homogeneous model, DELTAX = DELTAY, second order */
 
 /* ---- step kernels (cpml_set_tuning) ----------------------------------- */
-#define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: persistent when the
-                                     grid has more 32 x 8 tiles than the GPU holds
-                                     resident CTAs, else two-sweep                      */
+#define CPML_KERNEL_AUTO       0  /* 3D: fused one-sweep kernel; 2D: two-sweep         */
 #define CPML_KERNEL_TWO_SWEEP  1  /* stress kernel + velocity kernel, in place          */
 #define CPML_KERNEL_FUSED      2  /* 3D only: one kernel per step, two buffer sets, TMA  */
 #define CPML_KERNEL_PERSISTENT 3  /* 2D only: the two sweeps of a whole chunk of steps in

@@ -567,13 +567,13 @@ int configure_path_impl(cpml_handle* h) {
   if (!h->cluster && is_standard2d(h) && h->kernel != CPML_KERNEL_TWO_SWEEP) {
     const StepArgs s = make_args(h);
     h->persist_grid = persist2d_grid(s, h->het);
-    // automatic choice: persistent only when the grid has more tiles than
-    // the GPU holds resident CTAs; a grid that fits in one wave is latency-
-    // bound, and there the two kernels per step replayed from a CUDA graph
-    // measured faster than two grid barriers per step
+    // persistent only on request (or when the autotuner picks it): the two
+    // kernels per step replayed from a CUDA graph measured faster on every
+    // grid above 280 x 280 (440^2: 20.4 against 15.3 Gcell-updates/s,
+    // 1280^2: 36.7 against 30.9) and on the 101 x 641 reference grid
     if (h->persist_grid < 1) {
       if (h->kernel == CPML_KERNEL_PERSISTENT) return CPML_ERR_CUDA;
-    } else if (h->kernel == CPML_KERNEL_PERSISTENT || h->nblocks > h->persist_grid) {
+    } else if (h->kernel == CPML_KERNEL_PERSISTENT) {
       if (!h->bar && (st = dalloc(h, &h->bar, 2))) return st;
       h->persist = true;
     }

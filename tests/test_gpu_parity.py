@@ -131,7 +131,9 @@ def test_2d_kernel_choice_and_launch_accounting():
     with Solver(p, rec, tuning=(3, 8, 32, 2)) as s:
         assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
     pb, recb = P.small_2d(nx=4000, ny=400, nstep=20)  # 6250 tiles: more than the resident CTAs
-    with Solver(pb, recb) as s:                      # automatic: persistent
+    with Solver(pb, recb) as s:                      # automatic: still two-sweep
+        assert s.tuning()[0] == 1 and s.launches_per_step() == (2, 2)
+    with Solver(pb, recb, tuning=(3, 8, 32, 2)) as s:
         assert s.tuning()[0] == 3 and s.launches_per_step() == (0, 3)
     with Solver(p, rec) as s:
         with pytest.raises(RuntimeError):
