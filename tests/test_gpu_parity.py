@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from seismic_cpml_gb300 import params as P
+from seismic_cpml_gb300.lib import CpmlError
 from seismic_cpml_gb300.solver import Solver
 from oracle import oracle_c
 from tests.models import layered_2d, layered_3d
@@ -144,6 +145,29 @@ def test_2d_kernel_choice_and_launch_accounting():
             s.set_tuning(3, 8, 32, 2)                # the persistent kernel is 2D only
         with pytest.raises(RuntimeError):
             s.set_tuning(4, 8, 32, 2)                # so is the cluster kernel
+
+
+def test_failed_replan_blocks_runs_until_a_valid_one():
+    """A tuning request whose plan cannot be built (the cluster kernel on a
+    grid too large for one cluster's shared memory) leaves the handle
+    refusing to run (CPML_ERR_NOT_READY) instead of running a half-built
+    plan; the next valid request restores it, with the same results as a
+    handle that never failed."""
+    p, rec = P.small_2d(nx=600, ny=600, nstep=40)
+    with Solver(p, rec) as ref:
+        ref.run()
+        want = ref.seismograms()
+    with Solver(p, rec) as s:
+        with pytest.raises(CpmlError) as e:
+            s.set_tuning(4, 8, 32, 2)
+        assert e.value.status == -1                  # CPML_ERR_INVALID
+        with pytest.raises(CpmlError) as e:
+            s.run()
+        assert e.value.status == -7                  # CPML_ERR_NOT_READY
+        s.set_tuning(1, 8, 32, 2)
+        s.run()
+        got = s.seismograms()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
 
 
 TUNINGS_3D = [(1, 8, 32, 2), (2, 16, 32, 2), (2, 8, 7, 2), (2, 16, 5, 2), (2, 8, 9, 2), (2, 8, 11, 2)]
