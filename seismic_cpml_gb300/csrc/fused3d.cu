@@ -48,6 +48,7 @@
 #include <vector>
 #include "cpml_internal.cuh"
 #include "kutil.cuh"
+#include "tma.cuh"
 
 namespace cpml {
 
@@ -60,9 +61,6 @@ constexpr int FTX = 32;            // tile width in i (one warp)
 constexpr int FNT = 256;           // threads per CTA: 32 x 8
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
 // Which updates of a cell apply as far as its (i, j) go, for the general
 // path's face handling (the plane conditions are added per plane):
 //   bit 0 sigma_xx/yy/zz  j >= 1, i <= NX-2     bit 4 v_x   j >= 1, i >= 1
@@ -78,38 +76,6 @@ __device__ __forceinline__ int cell_bits(int i, int j, int nx, int ny) {
 __device__ __forceinline__ int nth_set(unsigned m, int n) {
   for (int k = 0; k < n; ++k) m &= m - 1;
   return __ffs(m) - 1;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
-  return true;
-}
-__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
 }
 
 template <int TY, bool HET>
@@ -374,7 +340,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
     }
     // every thread waits for load group g(m) itself (try_wait suspends the
     // thread in hardware), so there is one CTA barrier per plane
-    const bool landed = mbar_wait_bounded(&bar[use & 1], (uint32_t)((use >> 1) & 1));
+    const bool landed = mbar_wait_bounded(&bar[use & 1], (uint32_t)((use >> 1) & 1), kWaitCycles);
     // ======================= stress at plane m ==============================
     const float* VX0 = vxs + (m & 3) * SLOT;
     const float* VX1 = vxs + ((m + 1) & 3) * SLOT;
@@ -791,8 +757,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       atomicOr(s.err, 1);
       // let copies still in flight into this CTA's shared memory land
       for (int q = 0; q < 2; ++q) {
-        mbar_wait_bounded(&bar[q], 0);
-        mbar_wait_bounded(&bar[q], 1);
+        mbar_wait_bounded(&bar[q], 0, kWaitCycles);
+        mbar_wait_bounded(&bar[q], 1, kWaitCycles);
       }
     }
     __syncthreads();
@@ -803,28 +769,6 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
-                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
-                                  CUtensorMapFloatOOBfill);
-
-// Resolved once per process (a function-local static's initialisation is
-// thread-safe) through the runtime's versioned driver entry-point query, at
-// the ABI of CUDA 12.0 where cuTensorMapEncodeTiled first appeared; nullptr
-// when the driver has no tensor-map encoder.
-static EncodeTiledFn encode_fn() {
-  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess && p)
-      return reinterpret_cast<EncodeTiledFn>(p);
-    cudaGetLastError();
-    return nullptr;
-  }();
-  return fn;
-}
 
 // 3D map over one padded FP32 field: dims (nx, ny, nz), row pitch px floats;
 // box (32 + 8) x (TY + 2) x 1; out-of-range elements read as zero.
