@@ -86,11 +86,13 @@ struct Geo {
   static constexpr int SLOT = (BOX * 4 + 127) / 128 * 32;  // slot stride, 128-byte aligned
   static constexpr int RX = FTX + 2, RY = TY + 2, REG = RX * RY;  // stress ring plane
   // Power-of-two rings, a plane's slot is (m & (S-1)). Loads run two planes
-  // ahead: v_x/v_y/v_z, mu and rho need at most 4 live planes, old stresses
-  // and lambda 2. The six stress rings hold 4 planes each, so the stress
+  // ahead: v_x/v_y/v_z and rho need at most 4 live planes, old stresses 2.
+  // lambda (4) and mu (8: plane m+3 is requested while the velocity sweep of
+  // plane m-1 still reads plane m-1) also serve the energy of the velocity
+  // sweep's plane. The six stress rings hold 4 planes each, so the stress
   // sweep of plane m+1 never overwrites a plane the velocity sweep of plane
   // m-1 still reads (they may overlap in time: one CTA barrier per plane).
-  static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 2 + 4 + 4 : 0);
+  static constexpr int NBOX = 4 + 4 + 4 + 12 + (HET ? 4 + 8 + 4 : 0);
   static constexpr int RING = 24 * REG;
   // the tile's C-PML coefficients: a, b, 1/K at grid and half points, for
   // x = i0-4 .. i0+FTX+3 and y = j0-1 .. j0+TY
@@ -123,9 +125,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
   float* vys = vxs + 4 * SLOT;           // [4]
   float* vzs = vys + 4 * SLOT;           // [4]
   float* sos = vzs + 4 * SLOT;           // [2][6]
-  float* lms = sos + 12 * SLOT;          // per-cell model: lam[2], mu[4], rho[4]
-  float* mus = lms + 2 * SLOT;
-  float* rhs = mus + 4 * SLOT;
+  float* lms = sos + 12 * SLOT;          // per-cell model: lam[4], mu[8], rho[4]
+  float* mus = lms + 4 * SLOT;
+  float* rhs = mus + 8 * SLOT;
   float* ring = sm + G::NBOX * SLOT;
   float* r_sxx = ring;                   // [4] each
   float* r_syy = r_sxx + 4 * REG;
@@ -172,15 +174,15 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
 #pragma unroll
     for (int c = 0; c < 6; ++c) tma_load_3d(sos + ((m & 1) * 6 + c) * SLOT, &tm.f[3 + c], x, y, m, b);
     if (HET) {
-      tma_load_3d(lms + (m & 1) * SLOT, &tm.lam, x, y, m, b);
-      tma_load_3d(mus + ((m + 1) & 3) * SLOT, &tm.mu, x, y, m + 1, b);
+      tma_load_3d(lms + (m & 3) * SLOT, &tm.lam, x, y, m, b);
+      tma_load_3d(mus + ((m + 1) & 7) * SLOT, &tm.mu, x, y, m + 1, b);
       tma_load_3d(rhs + (m & 3) * SLOT, &tm.rho, x, y, m, b);
     }
     if (prologue) {
       tma_load_3d(vxs + (m & 3) * SLOT, &tm.f[0], x, y, m, b);
       tma_load_3d(vys + (m & 3) * SLOT, &tm.f[1], x, y, m, b);
       tma_load_3d(vzs + ((m - 1) & 3) * SLOT, &tm.f[2], x, y, m - 1, b);
-      if (HET) tma_load_3d(mus + (m & 3) * SLOT, &tm.mu, x, y, m, b);
+      if (HET) tma_load_3d(mus + (m & 7) * SLOT, &tm.mu, x, y, m, b);
     }
   };
 
@@ -360,9 +362,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
       // nothing to compute on boxes that did not arrive
     } else if (FAST) {
       const long long cpl = (long long)m * pl + (long long)j0 * px + i0;
-      const float* Lm = lms + (m & 1) * SLOT;
-      const float* M0 = mus + (m & 3) * SLOT;
-      const float* M1 = mus + ((m + 1) & 3) * SLOT;
+      const float* Lm = lms + (m & 3) * SLOT;
+      const float* M0 = mus + (m & 7) * SLOT;
+      const float* M1 = mus + ((m + 1) & 7) * SLOT;
       // interior tiles never touch the last column, so the 8-point mu
       // average of sigma_yz always takes i+1 (the general path clamps it)
       auto cell = [&](int b, int r, int comps, bool store, long long c, float& ox, float& oy, float& oz) {
@@ -418,9 +420,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         cell(hb, hr, hcomps, false, 0, dx, dy, dz);
       }
     } else if (m >= 0 && m < nz) {
-      const float* Lm = lms + (m & 1) * SLOT;
-      const float* M0 = mus + (m & 3) * SLOT;
-      const float* M1 = mus + ((m + 1) & 3) * SLOT;
+      const float* Lm = lms + (m & 3) * SLOT;
+      const float* M0 = mus + (m & 7) * SLOT;
+      const float* M1 = mus + ((m + 1) & 7) * SLOT;
       const bool edge = edge_tile || m < 1 || m > nz - 2;
       const int sz = UZ ? s.az.slab(m) : -1;
       const bool zs = UZ && sz >= 0;
@@ -606,8 +608,8 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           bad |= not_finite(v2);
           if (e_z) {
             float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
-            if (HET) {  // per-cell model of plane p (its smem slots may already hold later planes)
-              const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
+            if (HET) {  // per-cell model of plane p
+              const float l = lms[(p & 3) * SLOT + b], mu = mus[(p & 7) * SLOT + b];
               const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
               hr = 0.5f * R0[b];
               c1 = 2.0f * (l + mu) * den;
@@ -732,7 +734,7 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
           if (e_z && oe[q]) {  // energy interior (3D:1136-1143)
             float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
             if (HET) {
-              const float l = __ldg(s.mdl.lam + c), mu = __ldg(s.mdl.mu + c);
+              const float l = lms[(p & 3) * SLOT + b], mu = mus[(p & 7) * SLOT + b];
               const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
               hr = 0.5f * R0[b];
               c1 = 2.0f * (l + mu) * den;
