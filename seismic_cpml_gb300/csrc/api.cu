@@ -1206,7 +1206,7 @@ int cpml_autotune(cpml_handle* h, int trial_steps, const char* cache_path, int* 
     std::vector<TuneVal> cand;
     if (h->ndim == 3 && fused3d_supported())
       for (int ty : {8, 16})
-        for (int lz : {16, 24, 32, 48, 64}) cand.push_back(TuneVal{CPML_KERNEL_FUSED, ty, lz, 2, 0.0});
+        for (int lz : {16, 24, 32, 40, 48, 64}) cand.push_back(TuneVal{CPML_KERNEL_FUSED, ty, lz, 2, 0.0});
     cand.push_back(TuneVal{CPML_KERNEL_TWO_SWEEP, 8, 32, 2, 0.0});
     if (is_standard2d(h)) {
       if (persist2d_grid(make_args(h), h->het) > 0) cand.push_back(TuneVal{CPML_KERNEL_PERSISTENT, 8, 32, 2, 0.0});

@@ -854,14 +854,12 @@ void fused3d_items(int nx, int ny, int nz, const Axis& ax, const Axis& ay, const
   const int zi0 = az.lo > 1 ? az.lo : 1;                              // first interior plane
   const int zi1 = (nz - az.hi) < (nz - 1) ? (nz - az.hi) : (nz - 1);  // one past the last
   const int f0 = zi0 + 1, f1 = zi1 - 1;
+  // chunks of lz planes from the bottom of each range, the shorter
+  // remainder last: the items that start last in the launch order finish
+  // soonest, which shortens the step's tail (276^3: 0.4287 ms at lz = 40
+  // against 0.4331 for the best even split)
   auto chunks = [&](int a, int b, std::vector<int2>& out) {
-    if (b <= a) return;
-    const int n = (b - a + lz - 1) / lz;
-    for (int q = 0; q < n; ++q) {
-      const int k0 = a + (int)((long long)(b - a) * q / n);
-      const int k1 = a + (int)((long long)(b - a) * (q + 1) / n);
-      if (k1 > k0) out.push_back(make_int2(k0, k1));
-    }
+    for (int k0 = a; k0 < b; k0 += lz) out.push_back(make_int2(k0, k0 + lz < b ? k0 + lz : b));
   };
   auto interior_tile = [&](int i0, int j0) {
     const bool xs = ax.width() > 0 && (i0 - 1 < ax.lo || i0 + FTX >= nx - ax.hi);
