@@ -248,7 +248,8 @@ int cpml_get_stream(cpml_handle* h, void** stream);
 /* Select the step kernel (CPML_KERNEL_*; FUSED is 3D only, PERSISTENT and
    CLUSTER are 2D second order only: CPML_ERR_INVALID otherwise) and its
    launch shape: tile_y (rows of the 32-wide tile), zchunk (planes per CTA in
-   the z sweep) and lookahead (planes the fused kernel's TMA loads run ahead
+   the z sweep; each z range is cut into chunks of zchunk planes from its
+   bottom, the shorter remainder last) and lookahead (planes the fused kernel's TMA loads run ahead
    of the plane being computed: 2, the only supported value). The shape only
    matters to the fused kernel. Supported (tile_y, lookahead): (8,2) (16,2).
    Single-shot kernels advance one time step per sweep: temporal blocking
@@ -264,8 +265,9 @@ int cpml_get_tuning(cpml_handle* h, int* kernel, int* tile_y, int* zchunk, int* 
 int cpml_launches_per_step(cpml_handle* h, int* step_kernels, int* chunk_kernels);
 
 /* Autotune the step kernel for this handle's grid: every candidate (3D: the
-   one-sweep kernel with tile_y in {8,16} x zchunk in {16,24,32,48,64}; 2D: the
-   persistent kernel; both: the two-sweep kernel) runs 2 untimed then trial_steps timed steps (CUDA events on the
+   one-sweep kernel with tile_y in {8,16} x zchunk in {16,24,32,40,48,64}; 2D:
+   the persistent kernel and the on-chip cluster kernel where the grid fits;
+   both: the two-sweep kernel) runs 2 untimed then trial_steps timed steps (CUDA events on the
    handle's stream); the fastest is applied. Results are cached per shape
    class (ndim, grid, per-cell model, NPML, PML faces) for the process and,
    when cache_path is not NULL, in that text file (one line per class). Leaves
