@@ -117,6 +117,9 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
   constexpr bool UY = CLS == CLS_Y || CLS == CLS_GEN;
   constexpr bool UZ = CLS == CLS_Z || CLS == CLS_GEN;
   constexpr bool EARLY = CLS == CLS_X || CLS == CLS_Y || CLS == CLS_Z;
+  // Z-class items away from the z faces take a lean copy of the interior
+  // code with only the z-axis memory variables added
+  constexpr bool LEANZ = CLS == CLS_Z;
   using G = Geo<TY, HET>;
   constexpr int BX = G::BX, SLOT = G::SLOT, RX = G::RX, REG = G::REG;
   constexpr int NQ = TY / 8;             // own rows per thread
@@ -419,6 +422,89 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
         float dx, dy, dz;
         cell(hb, hr, hcomps, false, 0, dx, dy, dz);
       }
+    } else if (LEANZ && m >= 1 && m <= nz - 2 && !edge_tile) {
+      // Z-class items away from the z faces: the interior path's code with
+      // only the z-derivative terms through the C-PML memory variables (the
+      // same arithmetic as the general path, whose face handling and x/y
+      // slab code these items never need)
+      const long long cpl = (long long)m * pl;
+      const float* Lm = lms + (m & 3) * SLOT;
+      const float* M0 = mus + (m & 7) * SLOT;
+      const float* M1 = mus + ((m + 1) & 7) * SLOT;
+      const int sz = s.az.slab(m);
+      const bool zs = sz >= 0;
+      float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
+      if (zs) {
+        za = __ldg(s.az.a + m); zb = __ldg(s.az.b + m); zk = __ldg(s.az.ik + m);
+        zah = __ldg(s.az.ah + m); zbh = __ldg(s.az.bh + m); zkh = __ldg(s.az.ikh + m);
+      }
+      const long long mzp = (long long)sz * ny * px;
+      auto cellz = [&](int b, int r, int fo, int comps, bool store, const float* pre) {
+        const long long c = cpl + fo;
+        auto psi = [&](float d, float old, int k, float a_, float b_, float k_) {
+          const float nw = b_ * old + a_ * d;
+          if (store) (s.mb.z[k] + mzp)[fo] = nw;
+          return d * k_ + nw;
+        };
+        const float vxc = VX0[b], vyc = VY0[b], vzc = VZ0[b];
+        if (comps & 1) {
+          const float dxx = (VX0[b + 1] - vxc) * s.odx;
+          const float dyy = (vyc - VY0[b - BX]) * s.ody;
+          float dzz = (vzc - VZm[b]) * s.odz;
+          if (zs) dzz = psi(dzz, pre[2], 2, za, zb, zk);
+          float dl = s.dt_lam, dl2m = s.dt_l2m;
+          if (HET) {
+            const float lh = 0.5f * (Lm[b + 1] + Lm[b]);
+            const float mh = 0.5f * (M0[b + 1] + M0[b]);
+            dl = s.dt * lh;
+            dl2m = s.dt * (lh + 2.0f * mh);
+          }
+          const float nxx = SO[b] + (dl2m * dxx + dl * (dyy + dzz));
+          const float nyy = SO[SLOT + b] + (dl * (dxx + dzz) + dl2m * dyy);
+          const float nzz = SO[2 * SLOT + b] + (dl * (dxx + dyy) + dl2m * dzz);
+          Rxx[r] = nxx; Ryy[r] = nyy; Rzz[r] = nzz;
+          if (store) { s.g.sxx[c] = nxx; s.g.syy[c] = nyy; s.g.szz[c] = nzz; }
+        }
+        if (comps & 2) {
+          const float dm = HET ? s.dt * (0.5f * (M0[b + BX] + M0[b])) : s.dt_mu;
+          const float d1 = (vyc - VY0[b - 1]) * s.odx;
+          const float d2 = (VX0[b + BX] - vxc) * s.ody;
+          const float n = SO[3 * SLOT + b] + dm * (d1 + d2);
+          Rxy[r] = n;
+          if (store) s.g.sxy[c] = n;
+        }
+        if (comps & 4) {
+          const float dm = HET ? s.dt * (0.5f * (M1[b] + M0[b])) : s.dt_mu;
+          const float d1 = (vzc - VZ0[b - 1]) * s.odx;
+          float d2 = (VX1[b] - vxc) * s.odz;
+          if (zs) d2 = psi(d2, pre[0], 0, zah, zbh, zkh);
+          const float n = SO[4 * SLOT + b] + dm * (d1 + d2);
+          Rxz[r] = n;
+          if (store) s.g.sxz[c] = n;
+        }
+        if (comps & 8) {
+          float dm = s.dt_mu;
+          if (HET) {
+            const float sm8 = ((((((M0[b] + M0[b + 1]) + M0[b + BX]) + M0[b + BX + 1]) + M1[b]) + M1[b + 1]) +
+                               M1[b + BX]) + M1[b + BX + 1];
+            dm = s.dt * (0.125f * sm8);
+          }
+          const float d1 = (VZ0[b + BX] - vzc) * s.ody;
+          float d2 = (VY1[b] - vyc) * s.odz;
+          if (zs) d2 = psi(d2, pre[1], 1, zah, zbh, zkh);
+          const float n = SO[5 * SLOT + b] + dm * (d1 + d2);
+          Ryz[r] = n;
+          if (store) s.g.syz[c] = n;
+        }
+      };
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        if (ov[q]) {
+          const int b = b_own + q * 8 * BX;
+          nvx[q] = VX0[b]; nvy[q] = VY0[b]; nvz[q] = VZ0[b];
+          cellz(b, r_own + q * 8 * RX, ofo[q], 15, st_plane, e_own[q]);
+        }
+      if (hv) cellz(hb, hr, hfo, hcomps, false, e_halo);
     } else if (m >= 0 && m < nz) {
       const float* Lm = lms + (m & 3) * SLOT;
       const float* M0 = mus + (m & 7) * SLOT;
@@ -619,6 +705,81 @@ __global__ void __launch_bounds__(FNT, HET ? 2 : ((CLS == CLS_INTERIOR || TY == 
             ek.add(hr * v2);
             const float exx = c1 * sxx - c2 * (syy + szz);
             const float eyy = c1 * syy - c2 * (sxx + szz);
+            const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
+            ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
+          }
+        }
+      } else if (LEANZ && p >= 1 && p <= nz - 2 && !edge_tile) {
+        // Z-class items away from the z faces (see the stress sweep)
+        const long long cpl = (long long)p * pl;
+        const float* R0 = rhs + (p & 3) * SLOT;
+        const float* R1 = rhs + ((p + 1) & 3) * SLOT;
+        const int sz = s.az.slab(p);
+        const bool zs = sz >= 0;
+        float za = 0.f, zb = 0.f, zk = 1.f, zah = 0.f, zbh = 0.f, zkh = 1.f;
+        if (zs) {
+          za = __ldg(s.az.a + p); zb = __ldg(s.az.b + p); zk = __ldg(s.az.ik + p);
+          zah = __ldg(s.az.ah + p); zbh = __ldg(s.az.bh + p); zkh = __ldg(s.az.ikh + p);
+        }
+        const long long mzp = (long long)sz * ny * px;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          if (!ov[q]) continue;
+          const int r = r_own + q * 8 * RX;
+          const int b = b_own + q * 8 * BX;
+          const long long c = cpl + ofo[q];
+          const float sxx = Sxx[r], syy = Syy[r], szz = Szz0[r];
+          const float sxy = Sxy[r], sxz = Sxz0[r], syz = Syz0[r];
+          float d1 = (sxx - Sxx[r - 1]) * s.odx;   // v_x (3D:976-993)
+          float d2 = (sxy - Sxy[r - RX]) * s.ody;
+          float d3 = (sxz - Sxzm[r]) * s.odz;
+          float e1 = (Sxy[r + 1] - sxy) * s.odx;   // v_y (3D:995-1014)
+          float e2 = (Syy[r + RX] - syy) * s.ody;
+          float e3 = (syz - Syzm[r]) * s.odz;
+          float f1 = (Sxz0[r + 1] - sxz) * s.odx;  // v_z (3D:1031-1052)
+          float f2 = (syz - Syz0[r - RX]) * s.ody;
+          float f3 = (Szz1[r] - szz) * s.odz;
+          if (zs) {   // in place (3D:979-985 and the like)
+            auto psi = [&](float d, float old, int k, float a_, float b_, float k_) {
+              const float nw = b_ * old + a_ * d;
+              (s.m.z[k] + mzp)[ofo[q]] = nw;
+              return d * k_ + nw;
+            };
+            d3 = psi(d3, e_vel[q][0], 3, za, zb, zk);
+            e3 = psi(e3, e_vel[q][1], 4, za, zb, zk);
+            f3 = psi(f3, e_vel[q][2], 5, zah, zbh, zkh);
+          }
+          float fx = s.dt_over_rho, fy = s.dt_over_rho, fz = s.dt_over_rho;
+          if (HET) {
+            fx = s.dt / R0[b];
+            fy = s.dt / (0.25f * (R0[b] + R0[b + 1] + R0[b + 1 + BX] + R0[b + BX]));
+            fz = s.dt / (0.25f * (R0[b] + R0[b + 1] + R1[b + 1] + R1[b]));
+          }
+          float vx = cvx[q] + fx * (d1 + d2 + d3);
+          float vy = cvy[q] + fy * (e1 + e2 + e3);
+          const float vz = cvz[q] + fz * (f1 + f2 + f3);
+          if (has_src && p == s.ksrc && oi == s.isrc && oj[q] == s.jsrc) {  // 3D:1080-1081
+            vx += src_x;
+            vy += src_y;
+          }
+          s.g.vx[c] = vx; s.g.vy[c] = vy; s.g.vz[c] = vz;
+          const float v2 = vx * vx + vy * vy + vz * vz;
+          vm2 = fmaxf(vm2, v2);
+          bad |= not_finite(v2);
+          if (e_z && oe[q]) {  // energy interior (3D:1136-1143)
+            float hr = s.half_rho, c1 = s.e_c1, c2 = s.e_c2, i2m = s.inv_2mu;
+            if (HET) {
+              const float l = lms[(p & 3) * SLOT + b], mu = mus[(p & 7) * SLOT + b];
+              const float den = 1.0f / (2.0f * mu * (3.0f * l + 2.0f * mu));
+              hr = 0.5f * R0[b];
+              c1 = 2.0f * (l + mu) * den;
+              c2 = l * den;
+              i2m = 1.0f / (2.0f * mu);
+            }
+            ek.add(hr * v2);
+            const float exx = c1 * sxx - c2 * (syy + szz);
+            const float eyy = c1 * syy - c2 * (sxx + szz);
+            // the reference adds eps_yy*sigma_yy twice and no zz term (3D:1170-1171)
             const float third = s.ep_physical ? (c1 * szz - c2 * (sxx + syy)) * szz : eyy * syy;
             ep.add(0.5f * (exx * sxx + eyy * syy + third) + i2m * (sxy * sxy + sxz * sxz + syz * syz));
           }
