@@ -19,10 +19,11 @@ last plane), with the source and receivers on global plane k = NZ/2 (the last
 local plane of rank nb_procs/2-1, 3D:346, 1080-1081, 1126-1127).
 
 Parity of this restatement is cross-checked against the independent C++
-restatement in oracle/cpml_oracle.cpp (agreement to ~1e-13). Neither can be
-checked against the reference itself: the reference is Fortran, no Fortran
-compiler exists in this environment and the reference ships no tests or
-golden vectors. Parity against the reference is therefore unpinned.
+restatement in oracle/cpml_oracle.cpp, and both are checked against the
+reference programs' own statements. oracle/ref_f90c.py translated those
+from their Fortran source and gcc ran them (tests/test_ref_pin.py). This
+file reproduces their seismograms bit for bit, and their energies to
+summation order.
 
 `dtype=np.float32` runs the identical algorithm in single precision (profiles
 still built in float64 and rounded), which measures the FP32 rounding floor

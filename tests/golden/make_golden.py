@@ -1,12 +1,15 @@
 """Generate the golden fixtures of tests/golden/ with the FP64 C++ oracle.
 
-The reference ships no tests, golden vectors or known-answer files, and it
-cannot be compiled here (Fortran, no compiler in this environment), so these
-fixtures are outputs of the oracle restatement (oracle/cpml_oracle.cpp),
-cross-checked at generation time against the independent numpy restatement
-(oracle/oracle_np.py) on every case small enough to run it. They pin the
-oracle against regressions and give the GPU tests FP64 answers at the
-reference's own sizes.
+These fixtures are outputs of the oracle restatement (oracle/cpml_oracle.cpp).
+At generation time they are cross-checked against the independent numpy
+restatement (oracle/oracle_np.py) on every case small enough to run it. They
+pin the oracle against regressions and give the GPU tests FP64 answers at the
+reference's own sizes. The reference ships no tests, golden vectors or
+known-answer files. Its own outputs, from its Fortran statements translated
+by oracle/ref_f90c.py, are the refpin_*.npz fixtures of
+make_ref_vectors.py. tests/test_ref_pin.py checks that those equal the
+fixtures made here (ref2d_*, config_3d_plain) bit for bit, in traces and
+2D energies.
 
 Run:  python tests/golden/make_golden.py [name ...]   (no name: every fixture)
 

@@ -1,0 +1,167 @@
+"""Generate tests/golden/refpin_*.npz: golden vectors from the reference itself.
+
+The reference programs are Fortran, and no Fortran compiler exists on either
+machine this project runs on. oracle/ref_f90c.py translates each program's
+own source, read where it lies, into C. gcc compiles it, and oracle/ref_mpi.c
+runs it on emulated MPI ranks. This script runs those programs and saves:
+  - the parameters each run used (as the program evaluated them);
+  - the receiver grid points from the program's own nearest-point search;
+  - the seismograms and energies;
+  - SHA-256 digests of the final wavefields. The small 2D cases also keep
+    the fields themselves. For the full-size 3D case only digests of the
+    traces are kept: they equal config_3d_plain.npz's bit for bit.
+tests/test_ref_pin.py checks the C++ oracle against these vectors, bit for
+bit where the arithmetic order is the same.
+
+Parameters are overridden as a user edits the `parameter` lines, and the
+source-time function is chosen among the program's three `source_term`
+lines. Nothing else in the programs changes.
+
+Run (needs the reference sources and gcc):
+    python tests/golden/make_ref_vectors.py [--ref-dir DIR] [name ...]
+The full-size 3D case (276^3 x 2500 steps on 12 ranks) takes several
+minutes. The other cases take seconds.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_f90c  # noqa: E402
+
+PROGRAMS = ref_f90c.REFERENCE_PROGRAMS
+
+_COMMON = ["nx", "ny", "npoints_pml", "cp", "cs", "nstep", "deltat", "f0", "t0", "factor",
+           "isource", "jsource", "angle_force", "nrec", "it_display"]
+PARAMS = {
+    "cpml2d": _COMMON + ["deltax", "deltay", "density", "use_pml_xmin", "use_pml_xmax",
+                         "use_pml_ymin", "use_pml_ymax"],
+    "pml2d": _COMMON + ["h", "rho"],
+    "cpml3d": _COMMON + ["nz", "nproc", "deltax", "deltay", "deltaz", "rho", "use_pml_xmin",
+                         "use_pml_xmax", "use_pml_ymin", "use_pml_ymax", "use_pml_zmin",
+                         "use_pml_zmax"],
+}
+PARAMS["cpml2d4"] = PARAMS["cpml2d"]
+
+# final wavefields: oracle name -> the program's array name(s); the split
+# program's total field is the sum of its two parts (PML:153-159)
+FIELDS = {
+    "cpml2d": {"vx": ["vx"], "vy": ["vy"], "sxx": ["sigma_xx"], "syy": ["sigma_yy"],
+               "sxy": ["sigma_xy"]},
+    "cpml2d4": {"vx": ["vx"], "vy": ["vy"], "sxx": ["sigmaxx"], "syy": ["sigmayy"],
+                "sxy": ["sigmaxy"]},
+    "pml2d": {"vx": ["vx_1", "vx_2"], "vy": ["vy_1", "vy_2"], "sxx": ["sigmaxx_1", "sigmaxx_2"],
+              "syy": ["sigmayy_1", "sigmayy_2"], "sxy": ["sigmaxy_1", "sigmaxy_2"]},
+    "cpml3d": {"vx": ["vx"], "vy": ["vy"], "vz": ["vz"], "sxx": ["sigmaxx"], "syy": ["sigmayy"],
+               "szz": ["sigmazz"], "sxy": ["sigmaxy"], "sxz": ["sigmaxz"], "syz": ["sigmayz"]},
+}
+
+# name -> (program, overrides, source-time function or None for the
+#          program's active line, emulated ranks, keep full fields)
+CASES = {
+    # the programs exactly as shipped
+    "refpin_2d_shipped": ("cpml2d", {}, None, 1, False),
+    "refpin_2d4_shipped": ("cpml2d4", {}, None, 1, False),
+    "refpin_pml2d_shipped": ("pml2d", {}, None, 1, False),
+    # small grids with the parameters moved: one PML face off, another
+    # angle, three receivers, the Ricker wavelet (as in the 2D plain workload)
+    "refpin_2d_small": ("cpml2d", {"NX": 41, "NY": 61, "NSTEP": 400, "USE_PML_YMAX": ".false.",
+                                   "ANGLE_FORCE": "45.d0", "NREC": 3, "xdeb": "60.d0",
+                                   "ydeb": "450.d0", "xfin": "330.d0", "yfin": "120.d0"},
+                        "ricker", 1, True),
+    "refpin_2d4_small": ("cpml2d4", {"NX": 43, "NY": 57, "NSTEP": 600, "USE_PML_XMIN": ".false.",
+                                     "ANGLE_FORCE": "20.d0", "ydeb": "400.d0",
+                                     "yfin": "150.d0"}, "gaussian", 1, True),
+    "refpin_pml2d_small": ("pml2d", {"NX": 41, "NY": 61, "NSTEP": 400, "ydeb": "400.d0",
+                                     "yfin": "150.d0"}, None, 1, True),
+    # 3D on 2 and 4 ranks: the z-slab exchanges of 3D:811-823 and 951-963 run
+    "refpin_3d_2ranks": ("cpml3d", {"NX": 36, "NY": 40, "NZ": 40, "NPROC": 2, "NSTEP": 200,
+                                    "ydeb": "300.d0", "yfin": "100.d0"}, None, 2, False),
+    "refpin_3d_4ranks": ("cpml3d", {"NX": 30, "NY": 34, "NZ": 48, "NPROC": 4, "NSTEP": 240,
+                                    "USE_PML_ZMAX": ".false.", "USE_PML_XMIN": ".false.",
+                                    "ANGLE_FORCE": "60.d0", "NREC": 3, "xdeb": "40.d0",
+                                    "ydeb": "250.d0", "xfin": "200.d0", "yfin": "90.d0"},
+                         "ricker", 4, False),
+    # the 3D plain workload at full size: 276^3, 2500 steps, Ricker at the
+    # centre, 64 receivers on the x line through it
+    "refpin_3d_plain_full": ("cpml3d", ref_f90c.plain_3d_overrides(2500), "ricker",
+                             ref_f90c.PLAIN_3D_RANKS, False),
+}
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
+    prog, overrides, stf, nprocs, keep = CASES[name]
+    src = os.path.join(ref_dir, PROGRAMS[prog])
+    three_d = prog == "cpml3d"
+    fields = FIELDS[prog]
+    arrays = sorted({a for parts in fields.values() for a in parts})
+    outs = ["sisvx", "sisvy", "ix_rec", "iy_rec"]
+    outs += ["total_energy", "rank_cut_plane"] if three_d else ["total_energy_kinetic",
+                                                               "total_energy_potential"]
+    big = name.endswith("_full")
+    dump = outs + PARAMS[prog] + ([] if big else arrays)
+    t0 = time.time()
+    exe = ref_f90c.build(src, name, overrides, dump, bounds=not big, stf=stf)
+    ranks = exe.run(nprocs=nprocs, timeout=7200)
+    cut = int(ranks[0]["rank_cut_plane"]) if three_d else 0
+    d = ranks[cut]
+    out = {"program": np.array(PROGRAMS[prog]), "stf": np.array(stf or "program default"),
+           "nprocs": np.array(nprocs),
+           "overrides": np.array(repr(sorted(overrides.items())))}
+    for k in PARAMS[prog]:
+        out["p_" + k] = np.array(d[k])
+    out["rec"] = np.stack([d["ix_rec"], d["iy_rec"]], axis=1).astype(np.int32)
+    for k in ("sisvx", "sisvy"):
+        tr = np.ascontiguousarray(d[k].T)
+        if big:   # 64 x 2500 traces: their digest (config_3d_plain.npz holds the values)
+            out["sha_" + k] = np.array(digest(tr))
+        else:
+            out[k] = tr
+    if three_d:
+        out["energy"] = d["total_energy"]
+    else:
+        out["ek"] = d["total_energy_kinetic"]
+        out["ep"] = d["total_energy_potential"]
+    if not big:
+        for fname, parts in fields.items():
+            if three_d:   # local planes 1..NZ_LOCAL of every rank, in rank order
+                full = np.concatenate([r[parts[0]][:, :, 1:-1] for r in ranks], axis=2)
+                c = full.transpose(2, 1, 0)
+            else:
+                a = d[parts[0]] if len(parts) == 1 else d[parts[0]] + d[parts[1]]
+                nx, ny = int(d["nx"]), int(d["ny"])
+                lo = 1 if a.shape[0] == nx + 2 else 0   # 0:NX+1 arrays of the 4th-order program
+                c = a[lo:lo + nx, lo:lo + ny].T
+            out["sha_" + fname] = np.array(digest(c))
+            if keep:
+                out["f_" + fname] = np.ascontiguousarray(c)
+    path = os.path.join(out_dir, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {name} in {time.time() - t0:.1f} s")
+    return path
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-dir", default=ref_f90c.DEFAULT_REF_DIR)
+    ap.add_argument("names", nargs="*")
+    a = ap.parse_args()
+    for n in a.names or list(CASES):
+        generate(n, a.ref_dir)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,8 +1,9 @@
-"""bench.py's reference arm runs on the host cores only (the FP64 C++
-restatement of the 3D time loop): its JSON line keeps the benchmark
-contract's keys, checked here on a one-time-step sample, and the workloads
-whose CPU figure lives inside their own line print one `unavailable` line and
-exit 0. No GPU work."""
+"""bench.py's reference arm runs on the host cores only. It times the
+reference 3D program's own statements, translated to C (oracle/_ref), or
+the FP64 C++ restatement where that C is absent or --reference-port asks
+for it. Its JSON line keeps the benchmark contract's keys in both forms,
+checked here on short samples. The workloads whose CPU figure lives inside
+their own line print one `unavailable` line and exit 0. No GPU work."""
 import json
 import os
 import subprocess
@@ -25,8 +26,7 @@ def bench_line(*args):
     return json.loads(lines[0])
 
 
-def test_reference_arm_line_keeps_the_contract():
-    d = bench_line("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample-steps", "1")
+def check_contract(d, kind):
     for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
               "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
@@ -34,8 +34,26 @@ def test_reference_arm_line_keeps_the_contract():
     assert d["metric"] == d["unit"] == "Mcell-updates/s" and d["steps"] == 1 and d["n_gpus"] == 1
     assert d["config"]["workload"] == "3d_plain_276cube" and d["config"]["grid"] == [276, 276, 276]
     cb = d["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["kind"] == kind and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "note" not in d, d.get("note")
+
+
+def test_reference_arm_port_line_keeps_the_contract():
+    d = bench_line("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample-steps", "1",
+                   "--reference-port")
+    check_contract(d, "port")
+
+
+def test_reference_arm_times_the_translated_reference_program():
+    sys.path.insert(0, ROOT)
+    from oracle import ref_f90c
+    if not ref_f90c.translated_exists(ref_f90c.BENCH_TAG):
+        pytest.skip("no translated reference program in oracle/_ref (built from the reference sources)")
+    d = bench_line("--impl", "reference", "--steps", "1", "--warmup", "0")
+    check_contract(d, "reference")
+    assert d["cpu_baseline"]["cores"] == ref_f90c.PLAIN_3D_RANKS
+    assert d["config"]["nstep_per_bench_step"] == ref_f90c.BENCH_SAMPLE_STEPS
 
 
 @pytest.mark.parametrize("workload", ["2d_plain", "batch2d", "surrogate", "3d_large"])

@@ -1,11 +1,11 @@
 """CPU checks of the oracle (the FP64 restatements of the reference programs).
 
-The reference ships no tests or golden vectors and cannot be compiled here
-(Fortran), so the oracle is pinned by (1) two independent restatements that
-must agree, C++ (oracle/cpml_oracle.cpp) and numpy (oracle/oracle_np.py);
-(2) the committed golden fixtures (tests/golden/, made by make_golden.py);
-(3) physical properties the reference's own diagnostics rely on (energy decay
-in the C-PML, 2D:741-777; source wavelet shapes, 2D:644-654).
+The oracle is pinned to the reference's own outputs in tests/test_ref_pin.py.
+Here it is held by (1) two independent restatements that must agree, C++
+(oracle/cpml_oracle.cpp) and numpy (oracle/oracle_np.py); (2) the committed
+golden fixtures (tests/golden/, made by make_golden.py); (3) physical
+properties the reference's own diagnostics rely on (energy decay in the
+C-PML, 2D:741-777; source wavelet shapes, 2D:644-654).
 """
 import math
 

@@ -1,0 +1,310 @@
+"""The oracle against the reference programs themselves (CPU).
+
+tests/golden/refpin_*.npz hold what the reference programs compute. Each
+program's own Fortran statements were translated to C by oracle/ref_f90c.py,
+compiled with gcc, and run, the 3D program on 2, 4 and 12 emulated MPI ranks
+(tests/golden/make_ref_vectors.py). Here the C++ oracle runs the same
+parameters and must reproduce those outputs:
+  - bit for bit: fields, seismograms, and the 2D energies, which the oracle
+    sums in the programs' order;
+  - the 3D total energy within 1e-14 relative on the small grids and 1e-12
+    on the 276^3 grid. The program reduces its per-rank sums over MPI
+    (3D:1179), while the oracle sums plane partials in z order.
+The full-size 3D plain fixture (config_3d_plain.npz, made by the oracle) is
+checked against the reference's run of the same workload. So the GPU tests,
+which compare the product with the oracle, are anchored to the reference.
+
+The last tests check the translator itself on a small program written for
+this file, and, where the reference sources exist, regenerate two of the
+vectors from them.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle_c, oracle_np, ref_f90c
+from seismic_cpml_gb300 import params as P
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF_DIR = ref_f90c.DEFAULT_REF_DIR
+SMALL = ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small", "refpin_3d_2ranks",
+         "refpin_3d_4ranks"]
+SHIPPED = ["refpin_2d_shipped", "refpin_2d4_shipped", "refpin_pml2d_shipped"]
+STF = {"ricker": P.STF_RICKER, "gaussian": P.STF_GAUSSIAN, "program default": P.STF_DGAUSSIAN}
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name + ".npz")))
+
+
+def params_of(fx):
+    """CpmlParams for the run a fixture records, from the parameter values
+    the program itself evaluated."""
+    prog = str(fx["program"])
+    g = lambda k: fx["p_" + k].item()  # noqa: E731
+    three_d = "3D" in prog
+    if "fourth" in prog:
+        p = P.default_2d_fourth()
+    elif "Collino" in prog:
+        p = P.default_2d_split()
+    elif three_d:
+        p = P.default_3d()
+    else:
+        p = P.default_2d()
+    p.nx, p.ny, p.nstep, p.npoints_pml = g("nx"), g("ny"), g("nstep"), g("npoints_pml")
+    p.cp, p.cs, p.deltat, p.f0, p.t0, p.factor = (g(k) for k in ("cp", "cs", "deltat", "f0",
+                                                                  "t0", "factor"))
+    p.isource, p.jsource, p.angle_force = g("isource"), g("jsource"), g("angle_force")
+    p.it_display = g("it_display")
+    p.stf = STF[str(fx["stf"])]
+    if "Collino" in prog:
+        p.deltax = p.deltay = g("h")
+        p.rho = g("rho")
+    else:
+        p.deltax, p.deltay = g("deltax"), g("deltay")
+        p.rho = g("rho") if three_d else g("density")
+        faces = ["xmin", "xmax", "ymin", "ymax"] + (["zmin", "zmax"] if three_d else [])
+        p.use_pml[:] = [int(g("use_pml_" + f)) for f in faces] + [0] * (6 - len(faces))
+    rec = [tuple(int(v) for v in r) for r in fx["rec"]]
+    if three_d:
+        p.nz, p.deltaz = g("nz"), g("deltaz")
+        p.ksource = p.nz // 2                      # the cut plane, 3D:346, 1080
+        rec = [(i, j, p.nz // 2) for i, j in rec]  # recorded on the cut plane, 3D:1126
+    return p, rec
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def check(fx, r):
+    assert np.array_equal(r.sisvx, fx["sisvx"]), "vx seismograms differ"
+    assert np.array_equal(r.sisvy, fx["sisvy"]), "vy seismograms differ"
+    if "energy" in fx:
+        e = r.ek + r.ep
+        rel = np.abs(e - fx["energy"]).max() / np.abs(fx["energy"]).max()
+        assert rel <= 1e-14, rel
+    else:
+        assert np.array_equal(r.ek, fx["ek"]), "kinetic energy differs"
+        assert np.array_equal(r.ep, fx["ep"]), "potential energy differs"
+    for k in fx:
+        if k.startswith("f_"):
+            assert np.array_equal(r.fields[k[2:]], fx[k]), f"field {k[2:]} differs"
+        if k.startswith("sha_"):
+            assert digest(r.fields[k[4:]]) == str(fx[k]), f"field {k[4:]} differs"
+
+
+@pytest.mark.parametrize("name", SMALL + SHIPPED)
+def test_oracle_reproduces_reference(name):
+    fx = load(name)
+    p, rec = params_of(fx)
+    check(fx, oracle_c.run(p, rec=rec, keep_fields=True))
+
+
+@pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small",
+                                  "refpin_3d_2ranks"])
+def test_numpy_restatement_reproduces_reference(name):
+    fx = load(name)
+    p, rec = params_of(fx)
+    run = oracle_np.run3d if p.ndim == 3 else (
+        oracle_np.run2d4 if p.order == 4 else
+        oracle_np.run_split if p.scheme == P.SCHEME_SPLIT else oracle_np.run2d)
+    r = run(p, rec=rec)
+    assert np.array_equal(r.sisvx, fx["sisvx"])
+    assert np.array_equal(r.sisvy, fx["sisvy"])
+    e_ref = fx["energy"] if "energy" in fx else fx["ek"] + fx["ep"]
+    assert np.abs(r.ek + r.ep - e_ref).max() <= 1e-14 * np.abs(e_ref).max()
+
+
+def test_shipped_fixtures_are_the_reference():
+    """The oracle's fixtures of the programs as shipped (used by the GPU
+    tests) equal the reference's own outputs."""
+    for ours, ref in (("ref2d_default", "refpin_2d_shipped"), ("ref2d_fourth", "refpin_2d4_shipped"),
+                      ("ref2d_split", "refpin_pml2d_shipped")):
+        a, b = load(ours), load(ref)
+        assert np.array_equal(a["rec"][:, :2], b["rec"]), ours
+        for k in ("sisvx", "sisvy", "ek", "ep"):
+            assert np.array_equal(a[k], b[k]), (ours, k)
+
+
+def test_full_size_3d_plain_fixture_is_the_reference():
+    """config_3d_plain.npz (276^3, 2500 steps, 64 receivers; the fixture the
+    GPU run of the benchmarked kernels is compared with) against the
+    reference's own run of that workload on 12 ranks."""
+    a, b = load("config_3d_plain"), load("refpin_3d_plain_full")
+    assert np.array_equal(a["rec"][:, :2], b["rec"])
+    assert int(b["p_nx"]) == int(b["p_ny"]) == int(b["p_nz"]) == 276
+    assert int(b["p_nstep"]) == 2500 and str(b["stf"]) == "ricker"
+    for k in ("sisvx", "sisvy"):
+        if k in b:
+            assert np.array_equal(a[k], b[k]), k
+        else:
+            assert digest(a[k]) == str(b["sha_" + k]), k
+    # 16.7 M interior cells summed in another order (12 per-rank sums and an
+    # MPI reduction against per-plane partials): 8e-14 measured
+    e = a["ek"] + a["ep"]
+    assert np.abs(e - b["energy"]).max() <= 1e-12 * np.abs(b["energy"]).max()
+
+
+# ---------------------------------------------------------------------------
+# the translator itself
+# ---------------------------------------------------------------------------
+SELF_TEST = """\
+program selftest
+  implicit none
+  include 'mpif.h'
+  integer, parameter :: N = 5, M = 2 * N / 3 + 1
+  double precision, parameter :: X = 1.d0 / 3.d0, BIG = 1.d+30
+  double precision, dimension(0:N,2) :: a
+  double precision, dimension(4) :: buf
+  double precision :: s, mx, e, part, tot
+  real :: r
+  integer :: i, k, cnt, rank, nprocs, code, left, right
+  call MPI_INIT(code)
+  call MPI_COMM_SIZE(MPI_COMM_WORLD, nprocs, code)
+  call MPI_COMM_RANK(MPI_COMM_WORLD, rank, code)
+  do i = 0, N
+    a(i,1) = dble(i) * X - 2.d0**2  ! comment
+    a(i,2) = - a(i,1)**2
+  enddo
+  s = sum(a(1:N,1))
+  mx = maxval(abs(a))
+  r = 0.1
+  e = r
+  k = -7 / 2
+  cnt = 0
+  do i = 10, 1, -3
+    cnt = cnt + 1
+  end do
+  if (k == -3 .and. .not. (cnt /= 4)) then
+    a(0,1) = BIG
+  else if (k > 0) then
+    a(0,1) = 1
+  else
+    a(0,1) = 2
+  endif
+  a(:,2) = a(:,2) / 2.d0
+  left = rank - 1
+  right = rank + 1
+  if (rank == 0) left = MPI_PROC_NULL
+  if (rank == nprocs - 1) right = MPI_PROC_NULL
+  buf(:) = 0.d0
+  buf(1:2) = dble(rank + 1)
+  call MPI_SENDRECV(buf(1:2),2,MPI_DOUBLE_PRECISION,right,0,buf(3:4),2, &
+         MPI_DOUBLE_PRECISION,left,0,MPI_COMM_WORLD,i,code)
+  part = dble(rank + 1) / 7.d0
+  call MPI_REDUCE(part + 0.d0,tot,1,MPI_DOUBLE_PRECISION,MPI_SUM,0,MPI_COMM_WORLD,code)
+  call MPI_FINALIZE(code)
+end program selftest
+"""
+
+
+@pytest.fixture(scope="module")
+def selftest(tmp_path_factory):
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    d = tmp_path_factory.mktemp("ref")
+    src = d / "selftest.f90"
+    src.write_text(SELF_TEST)
+    code, manifest = ref_f90c.translate_file(str(src), {"N": 6}, ["a", "s", "mx", "e", "k", "cnt",
+                                                                    "m", "buf", "tot"])
+    c = d / "selftest.c"
+    c.write_text(code)
+    exe = d / "selftest"
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-w", "-o", str(exe), str(c),
+                    ref_f90c.MPI_RUNTIME, "-lm", "-lpthread"], check=True)
+    return ref_f90c.RefProgram(str(exe), manifest)
+
+
+def test_translator_semantics(selftest):
+    d = selftest.run(nprocs=1)[0]
+    n = 6                                              # the overridden parameter
+    assert int(d["m"]) == 2 * n // 3 + 1
+    x = 1.0 / 3.0
+    col = np.array([float(i) * x - 4.0 for i in range(n + 1)])
+    s = 0.0
+    for v in col[1:]:                                  # SUM in element order
+        s = s + v
+    assert d["s"] == s
+    assert d["mx"] == max(np.abs(col).max(), (col ** 2).max())
+    assert d["e"] == float(np.float32(0.1))            # 0.1 is a single-precision literal
+    assert int(d["k"]) == -3                           # integer division truncates
+    assert int(d["cnt"]) == 4                          # 10, 7, 4, 1
+    assert d["a"][0, 0] == 1.0e30                      # the IF branch taken
+    assert np.array_equal(d["a"][1:, 1], -(col[1:] ** 2) / 2.0)
+    assert d["a"].shape == (n + 1, 2)
+
+
+def test_mpi_stand_in(selftest):
+    out = selftest.run(nprocs=3)
+    for r, d in enumerate(out):
+        assert list(d["buf"][:2]) == [r + 1.0] * 2
+        assert list(d["buf"][2:]) == ([0.0, 0.0] if r == 0 else [float(r)] * 2)
+    tot = 0.0
+    for r in range(3):                                 # rank order
+        tot = tot + (r + 1) / 7.0
+    assert out[0]["tot"] == tot
+
+
+def test_translator_rejects_what_it_does_not_know(tmp_path):
+    src = tmp_path / "bad.f90"
+    src.write_text("program bad\n  implicit none\n  integer :: i\n  i = 1\n  goto 10\n"
+                   "end program bad\n")
+    with pytest.raises(ref_f90c.TranslateError, match="line 5"):
+        ref_f90c.translate_file(str(src))
+    with pytest.raises(ref_f90c.TranslateError, match="not parameters"):
+        src.write_text("program ok\n  implicit none\n  integer :: i\n  i = 1\nend program ok\n")
+        ref_f90c.translate_file(str(src), {"NX": 3})
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
+                    reason="needs the reference sources and gcc")
+@pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_3d_4ranks"])
+def test_vectors_regenerate_from_reference_source(name, tmp_path):
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_ref_vectors as M
+    path = M.generate(name, REF_DIR, str(tmp_path))
+    a, b = dict(np.load(path)), load(name)
+    assert sorted(a) == sorted(b)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+# ---------------------------------------------------------------------------
+# FP32 runs against the reference (the GPU twin is test_gpu_ref_pin.py)
+# ---------------------------------------------------------------------------
+TRACE_TOL = 1e-5     # relative L2 over all receivers and recorded components
+ENERGY_TOL = 1e-6    # relative L2 of the energy curve
+
+
+def rl2(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+def compare_fp32(fx, vx, vy, ek, ep):
+    """Trace and energy rel-L2 of an FP32 run against a reference fixture.
+    The 3D program records vx and vy only (3D:1126-1127)."""
+    et = rl2(np.concatenate([vx, vy]), np.concatenate([fx["sisvx"], fx["sisvy"]]))
+    e_ref = fx["energy"] if "energy" in fx else fx["ek"] + fx["ep"]
+    ee = rl2(ek + ep, e_ref)
+    assert et <= TRACE_TOL, f"trace rel-L2 {et:.3e}"
+    assert ee <= ENERGY_TOL, f"energy rel-L2 {ee:.3e}"
+    return et, ee
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_fp32_restatement_within_tolerance_of_reference(name):
+    """The algorithm in FP32 (the oracle's float instantiation) stays within
+    the GPU tolerances of the reference's FP64 outputs: the same check the
+    GPU runs, here on the CPU."""
+    fx = load(name)
+    p, rec = params_of(fx)
+    r = oracle_c.run(p, rec=rec, double=False)
+    compare_fp32(fx, r.sisvx, r.sisvy, r.ek, r.ep)
