@@ -1161,29 +1161,36 @@ class RefProgram:
     def run(self, nprocs: int = 1, workdir: str | None = None, timeout: float = 900.0):
         """Run the translated program on nprocs emulated MPI ranks; returns
         one {name: array} per rank (Fortran-ordered arrays, shaped by their
-        declared bounds), plus `loop_seconds` when the program times a loop."""
-        workdir = workdir or self.exe + ".out"
-        os.makedirs(workdir, exist_ok=True)
-        for f in os.listdir(workdir):
-            if f.endswith(".bin"):
-                os.remove(os.path.join(workdir, f))
-        proc = subprocess.run([self.exe, "-np", str(nprocs), "-o", workdir, "-t", str(int(timeout))],
-                              capture_output=True, text=True, timeout=timeout + 30)
-        if proc.returncode != 0:
-            raise RuntimeError(f"{os.path.basename(self.exe)} exited with {proc.returncode}: "
-                               f"{proc.stderr.strip()[-2000:]}")
-        out = []
-        for r in range(nprocs):
-            d = {}
-            for name, m in self.manifest.items():
-                a = np.fromfile(os.path.join(workdir, f"{name}.{r}.bin"), dtype=m["dtype"])
-                shp = [hi - lo + 1 for lo, hi in m["dims"]]
-                d[name] = a.reshape(shp, order="F") if shp else a[0]
-            t = os.path.join(workdir, f"loop_seconds.{r}.bin")
-            if os.path.exists(t):
-                d["loop_seconds"] = float(np.fromfile(t, dtype="<f8")[0])
-            out.append(d)
-        return out
+        declared bounds), plus `loop_seconds` when the program times a loop.
+        The dump files go to workdir, by default a temporary directory that
+        is removed once they are read."""
+        import shutil
+        import tempfile
+        own = workdir is None
+        workdir = tempfile.mkdtemp(prefix="ref_run_") if own else workdir
+        try:
+            os.makedirs(workdir, exist_ok=True)
+            proc = subprocess.run([self.exe, "-np", str(nprocs), "-o", workdir, "-t",
+                                   str(int(timeout))], capture_output=True, text=True,
+                                  timeout=timeout + 30)
+            if proc.returncode != 0:
+                raise RuntimeError(f"{os.path.basename(self.exe)} exited with {proc.returncode}: "
+                                   f"{proc.stderr.strip()[-2000:]}")
+            out = []
+            for r in range(nprocs):
+                d = {}
+                for name, m in self.manifest.items():
+                    a = np.fromfile(os.path.join(workdir, f"{name}.{r}.bin"), dtype=m["dtype"])
+                    shp = [hi - lo + 1 for lo, hi in m["dims"]]
+                    d[name] = a.reshape(shp, order="F") if shp else a[0]
+                t = os.path.join(workdir, f"loop_seconds.{r}.bin")
+                if os.path.exists(t):
+                    d["loop_seconds"] = float(np.fromfile(t, dtype="<f8")[0])
+                out.append(d)
+            return out
+        finally:
+            if own:
+                shutil.rmtree(workdir, ignore_errors=True)
 
 
 PARITY_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math"]
