@@ -550,8 +550,8 @@ class Translator:
             if param:
                 if init_text is None:
                     raise TranslateError(f"line {self.ln}: parameter {name} without a value")
-                if name in self.overrides:
-                    init_text = str(self.overrides[name])
+                if name in self.overrides:   # case-folded like the source text
+                    init_text = _lower_outside_strings(str(self.overrides[name]))
                     self.used_overrides.add(name)
                 sym.init = parse_expr(init_text, self.ln)
                 if sym.dims:
@@ -847,7 +847,7 @@ class Translator:
         """Pass-by-reference address of an actual argument: a variable, an
         array element, a contiguous section, or a temporary holding an
         expression's value."""
-        if a[0] == "name":
+        if a[0] == "name" and not self.sym(a[1]).param:
             s = self.sym(a[1])
             return f"(void*)&{s.cname}" if not s.dims else f"(void*){s.cname}"
         if a[0] == "ref" and a[1] in self.syms:
@@ -997,29 +997,33 @@ class Translator:
             s = self.syms[name]
             if s.dims:
                 self.emit(f'ref_dump("{name}", {s.cname}, sizeof({s.cname}));')
+            elif s.param:   # a compile-time constant: dump a copy
+                self.emit(f'{{ {CTYPE[s.ftype]} _p = {s.cname}; ref_dump("{name}", &_p, sizeof _p); }}')
             else:
                 self.emit(f'ref_dump("{name}", &{s.cname}, sizeof({s.cname}));')
         dumps = self.out
-        self.out, self.ind = [], 1
-        for name in self.order:                  # parameters, in declaration order
+        # Parameters are compile-time constants, as in Fortran: macros that
+        # gcc folds, so that e.g. x**NPOWER with NPOWER = 2.d0 is pow(x, 2.0)
+        # with a literal exponent, which gcc (like gfortran) turns into x*x.
+        params = []
+        for name in self.order:                  # in declaration order
             s = self.syms[name]
             if s.param:
                 self.ln = 0
                 c, _ = self.scalar(s.init)
-                self.emit(f"{s.cname} = ({CTYPE[s.ftype]})({c});")
-        params = self.out
+                params.append(f"#define {s.cname} (({CTYPE[s.ftype]})({c}))")
         glob, cap = [], 1
         for name in self.order:
             s = self.syms[name]
-            if s.ftype == "c":
+            if s.ftype == "c" or s.param:
                 continue
             if s.dims:
                 glob.append(f"static {CTYPE[s.ftype]} {s.cname}[{max(s.size, 1)}];")
                 cap = max(cap, s.size)
             else:
                 glob.append(f"static {CTYPE[s.ftype]} {s.cname};")
-        src = [C_PRELUDE, f"const long ref_message_capacity = {cap}L;", *glob, "",
-               "void ref_main(void) {", *params, *body, *dumps, "}", ""]
+        src = [C_PRELUDE, f"const long ref_message_capacity = {cap}L;", *params, *glob, "",
+               "void ref_main(void) {", *body, *dumps, "}", ""]
         manifest = {}
         for name in dump:
             s = self.syms[name]

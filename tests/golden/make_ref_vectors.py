@@ -50,6 +50,8 @@ PARAMS = {
                          "use_pml_xmax", "use_pml_ymin", "use_pml_ymax", "use_pml_zmin",
                          "use_pml_zmax"],
 }
+for _k in ("cpml2d", "cpml3d"):
+    PARAMS[_k] += ["npower", "k_max_pml", "alpha_max_pml"]
 PARAMS["cpml2d4"] = PARAMS["cpml2d"]
 
 # final wavefields: oracle name -> the program's array name(s); the split
@@ -83,6 +85,23 @@ CASES = {
                                      "yfin": "150.d0"}, "gaussian", 1, True),
     "refpin_pml2d_small": ("pml2d", {"NX": 41, "NY": 61, "NSTEP": 400, "ydeb": "400.d0",
                                      "yfin": "150.d0"}, None, 1, True),
+    # the C-PML profile parameters moved (R1): K_MAX_PML > 1 (the 1/K terms),
+    # other NPOWER (non-integer: pow), ALPHA_MAX_PML = 0 (classical PML
+    # profile), unequal grid spacings, another PML width
+    "refpin_2d_profiles": ("cpml2d", {"NX": 47, "NY": 53, "NSTEP": 500, "NPOINTS_PML": 8,
+                                      "DELTAY": "7.5d0", "DELTAT": "1.d-3", "NPOWER": "3.d0",
+                                      "K_MAX_PML": "7.d0", "ALPHA_MAX_PML": "0.d0", "f0": "12.d0",
+                                      "cp": "2800.d0", "density": "2200.d0", "ydeb": "300.d0",
+                                      "yfin": "100.d0"}, None, 1, True),
+    "refpin_2d4_profiles": ("cpml2d4", {"NX": 45, "NY": 51, "NSTEP": 700, "DELTAX": "9.d0",
+                                        "NPOWER": "1.5d0", "K_MAX_PML": "3.d0", "ydeb": "300.d0",
+                                        "yfin": "100.d0"}, "ricker", 1, True),
+    "refpin_3d_profiles": ("cpml3d", {"NX": 34, "NY": 30, "NZ": 36, "NPROC": 2, "NSTEP": 220,
+                                      "DELTAY": "9.d0", "ONE_OVER_DELTAY": "1.d0 / DELTAY",
+                                      "DELTAZ": "8.d0", "ONE_OVER_DELTAZ": "1.d0 / DELTAZ",
+                                      "DELTAT": "1.2d-3", "NPOWER": "2.5d0", "K_MAX_PML": "4.d0",
+                                      "NPOINTS_PML": 9, "ANGLE_FORCE": "200.d0", "ydeb": "220.d0",
+                                      "yfin": "80.d0"}, "gaussian", 2, False),
     # 3D on 2 and 4 ranks: the z-slab exchanges of 3D:811-823 and 951-963 run
     "refpin_3d_2ranks": ("cpml3d", {"NX": 36, "NY": 40, "NZ": 40, "NPROC": 2, "NSTEP": 200,
                                     "ydeb": "300.d0", "yfin": "100.d0"}, None, 2, False),

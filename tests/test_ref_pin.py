@@ -21,6 +21,7 @@ vectors from them.
 from __future__ import annotations
 
 import hashlib
+import math
 import os
 import shutil
 import subprocess
@@ -34,7 +35,7 @@ from seismic_cpml_gb300 import params as P
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 REF_DIR = ref_f90c.DEFAULT_REF_DIR
 SMALL = ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small", "refpin_3d_2ranks",
-         "refpin_3d_4ranks"]
+         "refpin_3d_4ranks", "refpin_2d_profiles", "refpin_2d4_profiles", "refpin_3d_profiles"]
 SHIPPED = ["refpin_2d_shipped", "refpin_2d4_shipped", "refpin_pml2d_shipped"]
 STF = {"ricker": P.STF_RICKER, "gaussian": P.STF_GAUSSIAN, "program default": P.STF_DGAUSSIAN}
 
@@ -71,6 +72,11 @@ def params_of(fx):
         p.rho = g("rho") if three_d else g("density")
         faces = ["xmin", "xmax", "ymin", "ymax"] + (["zmin", "zmax"] if three_d else [])
         p.use_pml[:] = [int(g("use_pml_" + f)) for f in faces] + [0] * (6 - len(faces))
+    if "p_npower" in fx:      # the C-PML profile parameters (the split program has none)
+        p.npower, p.k_max_pml = g("npower"), g("k_max_pml")
+        amax = g("alpha_max_pml")
+        # the programs' own value 2 pi (f0 / 2) is the oracle's default (-1)
+        p.alpha_max_pml = -1.0 if amax == 2.0 * math.pi * (p.f0 / 2.0) else amax
     rec = [tuple(int(v) for v in r) for r in fx["rec"]]
     if three_d:
         p.nz, p.deltaz = g("nz"), g("deltaz")
