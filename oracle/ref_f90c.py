@@ -19,18 +19,23 @@ checked against (tests/golden/make_ref_vectors.py, tests/test_ref_pin.py).
 
 The supported subset is what the four programs on the path use:
   - declarations: integer, double precision, real, logical (scalars, arrays
-    with declared bounds, `parameter`), and character, which is declared
-    only for skipped output code;
+    with declared bounds, `parameter`), and character variables;
   - `include 'mpif.h'` and the MPI calls that oracle/ref_mpi.c provides;
   - statements: assignment (scalar, element, section, whole array), DO loops
     with a fixed trip count, block IF/ELSE IF/ELSE, logical IF, CALL, STOP;
   - expressions: Fortran operator precedence with left-to-right evaluation,
     and these intrinsics: dble, sngl, real, int, nint, abs, sqrt, exp, log,
-    log10, sin, cos, tan, atan, mod, max, min, sum, maxval, minval.
+    log10, sin, cos, tan, atan, mod, max, min, sum, maxval, minval;
+  - subroutine units, translated on request beside a main program. Their
+    dummy arguments arrive by reference, and their arrays may have bounds
+    that are dummy arguments (adjustable arrays). The output subroutines
+    use WRITE (to a unit or a character variable, with literal strings and
+    Iw / Iw.m edits, or list-directed integers and strings), OPEN and
+    CLOSE.
 Anything outside the subset raises TranslateError with its line number, so
-nothing is dropped silently. Statements that only produce text (print,
-write, open, close, format) are skipped, and so are calls of the output
-subroutines named in SKIPPED_CALLS.
+nothing is dropped silently. In a main program, statements that only
+produce text (print, write, open, close, format) are skipped unless `io` is
+set, and so are calls of the output subroutines named in SKIPPED_CALLS.
 
 Fortran semantics kept:
   - arrays are column-major with their declared lower bounds, in static
@@ -408,13 +413,12 @@ def parse_expr(text: str, ln: int):
 class Sym:
     name: str
     ftype: str                      # 'i' integer, 'r' real, 'd' double, 'l' logical, 'c' character
-    dims: list | None = None        # [(lo, hi)] as Python ints
+    dims: list | None = None        # [(lo, hi)]: Python ints, or C expressions (dummy arrays)
     param: bool = False
     init: tuple | None = None       # parameter initialiser (AST)
-
-    @property
-    def cname(self):
-        return "v_" + self.name
+    cname: str = ""                 # the C name it is accessed by
+    clen: int = 0                   # character length
+    dummy: bool = False             # a dummy argument of a subroutine
 
     @property
     def size(self):
@@ -438,7 +442,12 @@ def _promote(a, b):
 # ---------------------------------------------------------------------------
 class Translator:
     def __init__(self, overrides: dict | None = None, bounds: bool = True,
-                 timed_loop: str | None = None):
+                 timed_loop: str | None = None, prefix: str = "v_", dummies=(),
+                 subs: dict | None = None, io: bool = False):
+        self.prefix = prefix           # C prefix of this unit's variables and parameters
+        self.dummies = list(dummies)   # dummy arguments, when translating a subroutine
+        self.subs = dict(subs or {})   # translated subroutines callable here: name -> arity
+        self.io = io                   # translate WRITE/OPEN/CLOSE instead of skipping them
         self.timed_loop = timed_loop   # DO variable of the loop whose wall time is dumped
         self.timer_used = False
         self.syms: dict[str, Sym] = {}
@@ -537,16 +546,21 @@ class Translator:
             name, edims = m2.group(1), m2.group(2) or dims
             if name in self.syms:
                 raise TranslateError(f"line {self.ln}: {name} declared twice")
-            sym = Sym(name, ftype, param=param)
+            sym = Sym(name, ftype, param=param, dummy=name in self.dummies)
+            if ftype == "c":
+                if sym.dummy:
+                    raise TranslateError(f"line {self.ln}: character dummy arguments are outside the subset")
+                mlen = re.search(r"\d+", tname)
+                sym.clen = int(mlen.group(0)) if mlen else 1
             if edims is not None and ftype != "c":
                 sym.dims = []
                 for d in _split_top(edims, ","):
-                    if ":" in d:
-                        lo, hi = d.split(":", 1)
-                        sym.dims.append((self.const_int(parse_expr(lo, self.ln)),
-                                         self.const_int(parse_expr(hi, self.ln))))
-                    else:
-                        sym.dims.append((1, self.const_int(parse_expr(d, self.ln))))
+                    lo, hi = d.split(":", 1) if ":" in d else ("1", d)
+                    sym.dims.append((self.bound(lo, sym), self.bound(hi, sym)))
+            if sym.dummy:
+                sym.cname = f"d_{name}" if sym.dims else f"(*d_{name})"
+            else:
+                sym.cname = self.prefix + name
             if param:
                 if init_text is None:
                     raise TranslateError(f"line {self.ln}: parameter {name} without a value")
@@ -560,6 +574,21 @@ class Translator:
                 raise TranslateError(f"line {self.ln}: initialised variables are outside the subset")
             self.syms[name] = sym
             self.order.append(name)
+
+    def bound(self, text, sym):
+        """An array bound: a Python int when it is a constant expression, else
+        (for a dummy array only) the C expression of the dummy arguments it
+        names, evaluated at each reference as in Fortran's adjustable arrays."""
+        e = parse_expr(text, self.ln)
+        try:
+            return self.const_int(e)
+        except TranslateError:
+            if not sym.dummy:
+                raise
+            c, t = self.scalar(e)
+            if t != "i":
+                raise TranslateError(f"line {self.ln}: non-integer bound of {sym.name}")
+            return c
 
     # ---- expression code ----------------------------------------------------
     def sym(self, name):
@@ -627,11 +656,13 @@ class Translator:
                 ic = c
             if self.bounds:
                 ic = f'ref_chk({ic}, {lo}, {hi}, "{s.name}", {self.ln})'
-            terms.append((f"(({ic}) - ({lo}))", hi - lo + 1))
+            ext = hi - lo + 1 if isinstance(lo, int) and isinstance(hi, int) \
+                else f"(long)(({hi}) - ({lo}) + 1)"
+            terms.append((f"(({ic}) - ({lo}))", ext))
         code, stride = terms[0][0], terms[0][1]
         for t, ext in terms[1:]:
-            code = f"{code} + {stride}L * {t}"
-            stride *= ext
+            code = f"{code} + ({stride}L) * {t}" if isinstance(stride, int) else f"{code} + {stride} * {t}"
+            stride = stride * ext if isinstance(stride, int) and isinstance(ext, int) else f"({stride} * {ext})"
         return code
 
     def gen(self, e, el):
@@ -814,12 +845,16 @@ class Translator:
         if not m:
             raise TranslateError(f"line {self.ln}: cannot read call {text!r}")
         name = m.group(1)
-        if name in SKIPPED_CALLS:
+        if name in self.subs:                     # a translated subroutine unit
+            arity, target = self.subs[name], f"ref_sub_{name}"
+        elif name in SKIPPED_CALLS:
             self.emit(f"/* line {self.ln}: call {name} skipped (output only) */")
             return
-        if name not in MPI_CALLS:
+        elif name in MPI_CALLS:
+            arity, target = MPI_CALLS[name], f"ref_{name}"
+            self.uses_mpi = True
+        else:
             raise TranslateError(f"line {self.ln}: call of {name} is outside the subset")
-        self.uses_mpi = True
         p = Parser(tokenize("(" + (m.group(2) or "") + ")", self.ln), self.ln)
         p.expect("(")
         args = []
@@ -831,8 +866,8 @@ class Translator:
                     continue
                 break
         p.expect(")")
-        if len(args) != MPI_CALLS[name]:
-            raise TranslateError(f"line {self.ln}: {name} takes {MPI_CALLS[name]} arguments")
+        if len(args) != arity:
+            raise TranslateError(f"line {self.ln}: {name} takes {arity} arguments")
         pre, ptrs = [], []
         for a in args:
             ptr = self.address(a, pre)
@@ -840,7 +875,7 @@ class Translator:
         self.emit("{")
         for line in pre:
             self.emit("  " + line)
-        self.emit(f"  ref_{name}({', '.join(ptrs)});")
+        self.emit(f"  {target}({', '.join(ptrs)});")
         self.emit("}")
 
     def address(self, a, pre):
@@ -880,13 +915,18 @@ class Translator:
             return
         if re.match(r"include\s+['\"]mpif\.h['\"]$", s):
             for k, v in MPIF_PARAMETERS.items():
-                self.syms[k] = Sym(k, "i", param=True, init=("num", str(v), "i"))
+                self.syms[k] = Sym(k, "i", param=True, init=("num", str(v), "i"),
+                                   cname=self.prefix + k)
                 self.order.append(k)
             return
         if self.TYPE_RE.match(s):
             self.declaration(s)
             return
-        if re.match(r"(print\b|write\s*\(|open\s*\(|close\s*\(|format\s*\()", s):
+        if re.match(r"(print\b|format\s*\()", s):
+            return
+        if re.match(r"(write|open|close)\s*\(", s):
+            if self.io:
+                self.io_statement(s)
             return
         m = re.match(r"do\s+(\w+)\s*=\s*(.+)$", s)
         if m:
@@ -971,6 +1011,77 @@ class Translator:
             return
         raise TranslateError(f"line {self.ln}: statement outside the subset: {s!r}")
 
+    def io_statement(self, s):
+        """WRITE to a unit or a character variable (formatted with literal
+        strings and I edit descriptors, or list-directed integers and
+        strings), OPEN of a file by name, CLOSE."""
+        kw = re.match(r"(write|open|close)", s).group(1)
+        ctrl, rest = _paren_prefix(s[len(kw):].lstrip(), self.ln)
+        parts = [x.strip() for x in _split_top(ctrl, ",")]
+        keyed = {}
+        for k, x in enumerate(parts):
+            m = re.match(r"(\w+)\s*=(?!=)\s*(.*)$", x)
+            keyed[m.group(1) if m else ("unit", "fmt")[min(k, 1)]] = m.group(2) if m else x
+        if kw == "close":
+            self.emit(f"ref_close({self.scalar(parse_expr(keyed['unit'], self.ln))[0]});")
+            return
+        if kw == "open":
+            unit = self.scalar(parse_expr(keyed["unit"], self.ln))[0]
+            self.emit(f"ref_open({unit}, {self.char_arg(keyed['file'])});")
+            return
+        unit, fmt = keyed.get("unit"), keyed.get("fmt")
+        if unit is None or fmt is None or set(keyed) - {"unit", "fmt"}:
+            raise TranslateError(f"line {self.ln}: WRITE control list outside the subset")
+        if unit == "*":
+            return                                 # standard output: progress messages only
+        items = [x.strip() for x in _split_top(rest.strip(), ",")] if rest.strip() else []
+        code = ["ref_rec_begin();"]
+        if fmt == "*":
+            for it in items:
+                e = parse_expr(it, self.ln)
+                if e[0] == "str":
+                    code.append(f"ref_ld_s({json.dumps(e[1])});")
+                else:
+                    c, t = self.scalar(e)
+                    if t != "i":
+                        raise TranslateError(f"line {self.ln}: list-directed output of non-integers "
+                                             "is outside the subset")
+                    code.append(f"ref_ld_i({c});")
+        else:
+            tok = tokenize(fmt, self.ln)
+            if len(tok) != 1 or tok[0][0] != "str":
+                raise TranslateError(f"line {self.ln}: formats other than literals are outside the subset")
+            k = 0
+            for d in parse_format(tok[0][1], self.ln):
+                if d[0] == "lit":
+                    code.append(f"ref_put_s({json.dumps(d[1])});")
+                    continue
+                if k == len(items):   # output ends at the first data edit without an item
+                    break
+                c, t = self.scalar(parse_expr(items[k], self.ln))
+                if t != "i":
+                    raise TranslateError(f"line {self.ln}: I editing of a non-integer")
+                code.append(f"ref_put_i({c}, {d[1]}, {d[2]});")
+                k += 1
+            if k < len(items):
+                raise TranslateError(f"line {self.ln}: format reversion is outside the subset")
+        target = self.syms.get(unit)
+        if target is not None and target.ftype == "c":
+            code.append(f"ref_rec_internal({target.cname}, {target.clen});")
+        else:
+            code.append(f"ref_rec_unit({self.scalar(parse_expr(unit, self.ln))[0]});")
+        self.emit("{ " + " ".join(code) + " }")
+
+    def char_arg(self, text):
+        """C (pointer, length) arguments of a character variable or literal."""
+        e = parse_expr(text, self.ln)
+        if e[0] == "str":
+            return f"{json.dumps(e[1])}, -1"
+        s = self.syms.get(e[1]) if e[0] == "name" else None
+        if s is None or s.ftype != "c":
+            raise TranslateError(f"line {self.ln}: file names must be character variables or literals")
+        return f"{s.cname}, {s.clen}"
+
     def close(self, kind):
         if not self.blocks or self.blocks[-1] != kind:
             raise TranslateError(f"line {self.ln}: unbalanced END {kind.split()[0].upper()}")
@@ -978,7 +1089,8 @@ class Translator:
         self.ind -= 1
 
     # ---- whole program ------------------------------------------------------------
-    def translate(self, stmts, dump=()):
+    def body(self, stmts):
+        """Translate the executable statements of one unit; returns its C lines."""
         for ln, s in stmts:
             self.ln = ln
             self.statement(s)
@@ -989,8 +1101,68 @@ class Translator:
         missing = set(self.overrides) - self.used_overrides
         if missing:
             raise TranslateError(f"overridden names that are not parameters: {sorted(missing)}")
-        body = self.out
-        self.out, self.ind = [], 1
+        out, self.out = self.out, []
+        return out
+
+    def declarations(self):
+        """(parameter macros, static variables, largest array) of this unit.
+        Parameters are compile-time constants, as in Fortran: macros that gcc
+        folds, so that e.g. x**NPOWER with NPOWER = 2.d0 is pow(x, 2.0) with a
+        literal exponent, which gcc (like gfortran) turns into x*x."""
+        params, glob, cap = [], [], 1
+        for name in self.order:                  # in declaration order
+            s = self.syms[name]
+            if s.param:
+                self.ln = 0
+                c, _ = self.scalar(s.init)
+                params.append(f"#define {s.cname} (({CTYPE[s.ftype]})({c}))")
+            elif s.dummy:
+                continue
+            elif s.ftype == "c":
+                glob.append(f"static char {s.cname}[{s.clen + 1}];")
+            elif s.dims:
+                glob.append(f"static {CTYPE[s.ftype]} {s.cname}[{max(s.size, 1)}];")
+                cap = max(cap, s.size)
+            else:
+                glob.append(f"static {CTYPE[s.ftype]} {s.cname};")
+        return params, glob, cap
+
+    def function(self, name, stmts):
+        """C function ref_sub_<name>(void* ...) of a subroutine unit: every
+        dummy argument arrives by reference, as in Fortran."""
+        body = self.body(stmts)
+        head = [f"static void ref_sub_{name}({', '.join(f'void* p{k}' for k in range(len(self.dummies))) or 'void'}) {{"]
+        for k, a in enumerate(self.dummies):
+            sym = self.syms.get(a)
+            if sym is None:
+                raise TranslateError(f"subroutine {name}: dummy argument {a} is not declared")
+            head.append(f"  {CTYPE[sym.ftype]}* d_{a} = ({CTYPE[sym.ftype]}*)p{k};")
+        return head + body + ["}", ""]
+
+    def translate(self, stmts, dump=(), load=(), subroutines=()):
+        """C source of the main program (and of the subroutine units given as
+        (name, dummy names, statements)), with `load`ed variables read from
+        the input directory before the first statement and `dump`ed ones
+        written after the last; returns (C source, dump manifest)."""
+        sub_params, sub_glob, sub_funcs, cap = [], [], [], 1
+        for k, (sname, args, sstmts) in enumerate(subroutines):
+            T = Translator(bounds=self.bounds, prefix=f"s{k}_", dummies=args, io=True)
+            fn = T.function(sname, sstmts)
+            p_, g_, c_ = T.declarations()
+            sub_params += p_
+            sub_glob += g_
+            sub_funcs += fn
+            cap = max(cap, c_)
+            self.subs[sname] = len(args)
+        body = self.body(stmts)
+        self.ind = 1
+        for name in load:
+            s = self.syms.get(name)
+            if s is None or s.param or s.ftype == "c":
+                raise TranslateError(f"cannot load {name}: not a numeric variable")
+            ref = s.cname if s.dims else "&" + s.cname
+            self.emit(f'ref_load("{name}", {ref}, sizeof({s.cname}));')
+        loads, self.out = self.out, []
         for name in dump:
             if name not in self.syms or self.syms[name].ftype == "c":
                 raise TranslateError(f"cannot dump {name}: not a numeric variable")
@@ -1002,28 +1174,11 @@ class Translator:
             else:
                 self.emit(f'ref_dump("{name}", &{s.cname}, sizeof({s.cname}));')
         dumps = self.out
-        # Parameters are compile-time constants, as in Fortran: macros that
-        # gcc folds, so that e.g. x**NPOWER with NPOWER = 2.d0 is pow(x, 2.0)
-        # with a literal exponent, which gcc (like gfortran) turns into x*x.
-        params = []
-        for name in self.order:                  # in declaration order
-            s = self.syms[name]
-            if s.param:
-                self.ln = 0
-                c, _ = self.scalar(s.init)
-                params.append(f"#define {s.cname} (({CTYPE[s.ftype]})({c}))")
-        glob, cap = [], 1
-        for name in self.order:
-            s = self.syms[name]
-            if s.ftype == "c" or s.param:
-                continue
-            if s.dims:
-                glob.append(f"static {CTYPE[s.ftype]} {s.cname}[{max(s.size, 1)}];")
-                cap = max(cap, s.size)
-            else:
-                glob.append(f"static {CTYPE[s.ftype]} {s.cname};")
-        src = [C_PRELUDE, f"const long ref_message_capacity = {cap}L;", *params, *glob, "",
-               "void ref_main(void) {", *body, *dumps, "}", ""]
+        params, glob, cap_main = self.declarations()
+        cap = max(cap, cap_main)
+        src = [C_PRELUDE, f"const long ref_message_capacity = {cap}L;", *params, *sub_params,
+               *glob, *sub_glob, "", *sub_funcs,
+               "void ref_main(void) {", *loads, *body, *dumps, "}", ""]
         manifest = {}
         for name in dump:
             s = self.syms[name]
@@ -1043,6 +1198,16 @@ C_PRELUDE = r"""/* Generated from a reference Fortran program by oracle/ref_f90c
 void ref_stop(const char* msg, int line);
 void ref_dump(const char* name, const void* data, size_t bytes);
 void ref_timer(int end);
+void ref_load(const char* name, void* data, size_t bytes);
+void ref_rec_begin(void);
+void ref_put_s(const char* s);
+void ref_put_i(long v, int w, int m);
+void ref_ld_i(long v);
+void ref_ld_s(const char* s);
+void ref_rec_internal(char* buf, int len);
+void ref_rec_unit(int unit);
+void ref_open(int unit, const char* name, int len);
+void ref_close(int unit);
 void ref_mpi_init(void*);
 void ref_mpi_finalize(void*);
 void ref_mpi_comm_size(void*, void*, void*);
@@ -1067,6 +1232,42 @@ static inline int ref_ipow(int b, int e) {
   return r;
 }
 """
+
+
+def parse_format(text: str, ln: int):
+    """A format specification of literal strings and Iw / Iw.m edit
+    descriptors -> [("lit", text) | ("i", w, m)] (m = -1 when absent)."""
+    t = text.strip()
+    if not (t.startswith("(") and t.endswith(")")):
+        raise TranslateError(f"line {ln}: bad format {text!r}")
+    out = []
+    for part in _split_top(t[1:-1], ","):
+        part = part.strip()
+        if part[:1] in ("'", '"'):
+            q = part[0]
+            out.append(("lit", part[1:-1].replace(q + q, q)))
+            continue
+        m = re.fullmatch(r"i(\d+)(?:\.(\d+))?", part, re.I)
+        if not m:
+            raise TranslateError(f"line {ln}: format item {part!r} is outside the subset")
+        out.append(("i", int(m.group(1)), int(m.group(2)) if m.group(2) else -1))
+    return out
+
+
+def subroutine_unit(stmts, name: str):
+    """(dummy argument names, statements) of SUBROUTINE name."""
+    inside, body, args = False, [], []
+    for ln, s in stmts:
+        if not inside:
+            m = re.match(r"subroutine\s+(\w+)\s*(?:\((.*)\))?$", s)
+            if m and m.group(1) == name:
+                inside = True
+                args = [a.strip() for a in (m.group(2) or "").split(",") if a.strip()]
+            continue
+        if re.match(r"end\s*subroutine\b", s) or s == "end":
+            return args, body
+        body.append((ln, s))
+    raise TranslateError(f"no subroutine {name}")
 
 
 def _same_section_only(e, lhs):
@@ -1151,9 +1352,15 @@ def _assign_pos(s: str):
 # build and run
 # ---------------------------------------------------------------------------
 def translate_file(src: str, overrides: dict | None = None, dump=(), bounds=True,
-                   stf: str | None = None, timed_loop: str | None = None):
+                   stf: str | None = None, timed_loop: str | None = None, load=(),
+                   subroutines=(), io: bool = False):
+    """C source and dump manifest of src's main program. subroutines lists
+    (file, name) units to translate beside it and call; io translates the
+    main program's WRITE/OPEN/CLOSE as well (always done in subroutines)."""
     stmts = main_program(read_statements(src, stf))
-    return Translator(overrides, bounds, timed_loop).translate(stmts, dump)
+    units = [(name, *subroutine_unit(read_statements(path), name)) for path, name in subroutines]
+    T = Translator(overrides, bounds, timed_loop, io=io)
+    return T.translate(stmts, dump, load, units)
 
 
 @dataclass
@@ -1162,21 +1369,30 @@ class RefProgram:
     manifest: dict
     overrides: dict = field(default_factory=dict)
 
-    def run(self, nprocs: int = 1, workdir: str | None = None, timeout: float = 900.0):
+    def run(self, nprocs: int = 1, workdir: str | None = None, timeout: float = 900.0,
+            inputs: dict | None = None, files=()):
         """Run the translated program on nprocs emulated MPI ranks; returns
         one {name: array} per rank (Fortran-ordered arrays, shaped by their
         declared bounds), plus `loop_seconds` when the program times a loop.
-        The dump files go to workdir, by default a temporary directory that
-        is removed once they are read."""
+        The program runs in workdir, by default a temporary directory that
+        is removed afterwards: its dump files and the files it opens go
+        there. inputs maps the names the program loads to arrays, written
+        in Fortran order; `files` names files it writes, returned as text
+        under out[0]["files"]."""
         import shutil
         import tempfile
         own = workdir is None
         workdir = tempfile.mkdtemp(prefix="ref_run_") if own else workdir
         try:
             os.makedirs(workdir, exist_ok=True)
-            proc = subprocess.run([self.exe, "-np", str(nprocs), "-o", workdir, "-t",
-                                   str(int(timeout))], capture_output=True, text=True,
-                                  timeout=timeout + 30)
+            indir = os.path.join(workdir, "inputs")
+            os.makedirs(indir, exist_ok=True)
+            for name, a in (inputs or {}).items():
+                with open(os.path.join(indir, name + ".bin"), "wb") as f:
+                    f.write(np.asarray(a).tobytes(order="F"))
+            proc = subprocess.run([os.path.abspath(self.exe), "-np", str(nprocs), "-o", workdir,
+                                   "-i", indir, "-t", str(int(timeout))], capture_output=True,
+                                  text=True, timeout=timeout + 30, cwd=workdir)
             if proc.returncode != 0:
                 raise RuntimeError(f"{os.path.basename(self.exe)} exited with {proc.returncode}: "
                                    f"{proc.stderr.strip()[-2000:]}")
@@ -1191,6 +1407,11 @@ class RefProgram:
                 if os.path.exists(t):
                     d["loop_seconds"] = float(np.fromfile(t, dtype="<f8")[0])
                 out.append(d)
+            if files:
+                out[0]["files"] = {}
+                for name in files:
+                    with open(os.path.join(workdir, name)) as f:
+                        out[0]["files"][name] = f.read()
             return out
         finally:
             if own:
@@ -1206,12 +1427,13 @@ TIMING_FLAGS = ["-O3"]
 
 def build(src: str, tag: str, overrides: dict | None = None, dump=(), bounds=True,
           stf: str | None = None, timed_loop: str | None = None, cc: str = "gcc",
-          flags: list | None = None) -> RefProgram:
+          flags: list | None = None, load=(), subroutines=(), io: bool = False) -> RefProgram:
     """Translate src with the given parameter overrides (and source-time
     function, when stf names one) into oracle/_ref/<tag>.c, then compile it
     for this machine (compile_translated) with `flags` (PARITY_FLAGS by
     default)."""
-    code, manifest = translate_file(src, overrides, dump, bounds, stf, timed_loop)
+    code, manifest = translate_file(src, overrides, dump, bounds, stf, timed_loop, load,
+                                    subroutines, io)
     os.makedirs(REF_OUT, exist_ok=True)
     cpath = os.path.join(REF_OUT, tag + ".c")
     if not (os.path.exists(cpath) and open(cpath).read() == code):

@@ -21,7 +21,11 @@
  * on all ranks in the same order. The numbers behind the mpif.h constants
  * match MPIF_PARAMETERS in ref_f90c.py.
  *
- * Usage: <program> [-np N] [-o outdir] [-t seconds]. The parent waits for
+ * It also holds the runtime of the translated programs: STOP, the dump
+ * and load hooks of the tests, the timer of the CPU reference timing, and
+ * formatted WRITE/OPEN/CLOSE for translated output subroutines.
+ *
+ * Usage: <program> [-np N] [-o outdir] [-i indir] [-t seconds]. The parent waits for
  * the ranks. If one fails, or the time limit passes, it kills the rest and
  * exits non-zero.
  */
@@ -53,6 +57,7 @@ typedef struct {
 
 static int g_rank = 0, g_size = 1;
 static const char* g_outdir = ".";
+static const char* g_indir = ".";
 static shared_t* g_sh = NULL;
 static unsigned char* g_box = NULL; /* g_size mailboxes of g_cap bytes */
 static size_t g_cap = 0;
@@ -86,6 +91,87 @@ void ref_dump(const char* name, const void* data, size_t bytes) {
   FILE* f = fopen(path, "wb");
   if (!f || fwrite(data, 1, bytes, f) != bytes) fail("cannot write a dump file");
   fclose(f);
+}
+
+/* variables a test fills before the first statement: <indir>/<name>.bin,
+   exactly the variable's size */
+void ref_load(const char* name, void* data, size_t bytes) {
+  char path[4096];
+  snprintf(path, sizeof path, "%s/%s.bin", g_indir, name);
+  FILE* f = fopen(path, "rb");
+  if (!f || fread(data, 1, bytes, f) != bytes || fgetc(f) != EOF) fail("cannot load an input file");
+  fclose(f);
+}
+
+/* Formatted output: one record is built, then written to a unit (a line
+   of its file) or into a character variable (blank-padded). Iw.m edits
+   right-justify in w columns with at least m digits (w asterisks when the
+   number does not fit); list-directed integers take 12 columns and strings
+   a leading blank, the layout of gfortran's list-directed records. */
+static char g_rec[16384];
+static size_t g_rec_n;
+static FILE* g_units[128];
+
+static void rec_put(const char* s, size_t n) {
+  if (g_rec_n + n >= sizeof g_rec) fail("output record too long");
+  memcpy(g_rec + g_rec_n, s, n);
+  g_rec_n += n;
+}
+void ref_rec_begin(void) { g_rec_n = 0; }
+void ref_put_s(const char* s) { rec_put(s, strlen(s)); }
+void ref_put_i(long v, int w, int m) {
+  char digits[32], body[64];
+  int nd = snprintf(digits, sizeof digits, "%ld", v < 0 ? -v : v);
+  if (v == 0 && m == 0) nd = 0;
+  const int mm = m < 0 ? 1 : m;
+  size_t n = 0;
+  if (v < 0) body[n++] = '-';
+  for (int k = nd; k < mm && n < 40; ++k) body[n++] = '0';
+  memcpy(body + n, digits, (size_t)nd);
+  n += (size_t)nd;
+  if ((int)n > w) {
+    for (int k = 0; k < w; ++k) rec_put("*", 1);
+    return;
+  }
+  for (int k = (int)n; k < w; ++k) rec_put(" ", 1);
+  rec_put(body, n);
+}
+void ref_ld_i(long v) {
+  char b[32];
+  const int n = snprintf(b, sizeof b, "%12ld", v);
+  rec_put(b, (size_t)n);
+}
+void ref_ld_s(const char* s) {
+  rec_put(" ", 1);
+  ref_put_s(s);
+}
+void ref_rec_internal(char* buf, int len) {
+  const size_t n = g_rec_n < (size_t)len ? g_rec_n : (size_t)len;
+  memcpy(buf, g_rec, n);
+  memset(buf + n, ' ', (size_t)len - n);
+  buf[len] = 0;
+}
+void ref_open(int unit, const char* name, int len) {
+  char path[4096];
+  size_t n = len < 0 ? strlen(name) : (size_t)len;
+  while (n > 0 && name[n - 1] == ' ') --n;        /* Fortran names are blank-padded */
+  if (unit < 0 || unit >= 128 || n == 0 || n >= sizeof path) fail("bad OPEN");
+  memcpy(path, name, n);
+  path[n] = 0;
+  if (g_units[unit]) fclose(g_units[unit]);
+  g_units[unit] = fopen(path, "w");
+  if (!g_units[unit]) fail("OPEN failed");
+}
+void ref_rec_unit(int unit) {
+  if (unit < 0 || unit >= 128 || !g_units[unit]) fail("WRITE to a unit that is not open");
+  if (fwrite(g_rec, 1, g_rec_n, g_units[unit]) != g_rec_n || fputc('\n', g_units[unit]) == EOF)
+    fail("WRITE failed");
+}
+void ref_close(int unit) {
+  if (unit >= 0 && unit < 128 && g_units[unit]) {
+    fclose(g_units[unit]);
+    g_units[unit] = NULL;
+  }
 }
 
 /* wall time of the loop the translator marked (the time loop), written as
@@ -201,9 +287,10 @@ int main(int argc, char** argv) {
   for (int a = 1; a + 1 < argc; a += 2) {
     if (!strcmp(argv[a], "-np")) np = atoi(argv[a + 1]);
     else if (!strcmp(argv[a], "-o")) g_outdir = argv[a + 1];
+    else if (!strcmp(argv[a], "-i")) g_indir = argv[a + 1];
     else if (!strcmp(argv[a], "-t")) limit = atoi(argv[a + 1]);
     else {
-      fprintf(stderr, "usage: %s [-np N] [-o outdir] [-t seconds]\n", argv[0]);
+      fprintf(stderr, "usage: %s [-np N] [-o outdir] [-i indir] [-t seconds]\n", argv[0]);
       return 2;
     }
   }

@@ -17,6 +17,10 @@ Parameters are overridden as a user edits the `parameter` lines, and the
 source-time function is chosen among the program's three `source_term`
 lines. Nothing else in the programs changes.
 
+refpin_pnm.npz holds PNM snapshots from the programs' create_color_image
+subroutine (2D:861-999, the same in all four programs), run by a small
+driver of this project's own on planes given to it.
+
 Run (needs the reference sources and gcc):
     python tests/golden/make_ref_vectors.py [--ref-dir DIR] [name ...]
 The full-size 3D case (276^3 x 2500 steps on 12 ranks) takes several
@@ -173,13 +177,98 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
     return path
 
 
+# ---------------------------------------------------------------------------
+# PNM snapshots (2D:861-999; the same subroutine in all four programs)
+# ---------------------------------------------------------------------------
+# A driver of this project's own that hands one plane to the programs'
+# create_color_image subroutine, translated from the reference source; the
+# plane and the receiver indices are loaded from files before it runs.
+PNM_HARNESS = """\
+program pnm_harness
+  implicit none
+  integer, parameter :: NX = 8, NY = 8, NREC = 1, IT = 1, ISRC = 4, JSRC = 4, NPML = 2
+  integer, parameter :: FIELD = 1
+  logical, parameter :: UXMIN = .true., UXMAX = .true., UYMIN = .true., UYMAX = .true.
+  double precision, dimension(NX,NY) :: plane
+  integer, dimension(NREC) :: ix_rec, iy_rec
+  call create_color_image(plane,NX,NY,IT,ISRC,JSRC,ix_rec,iy_rec,NREC,NPML, &
+                          UXMIN,UXMAX,UYMIN,UYMAX,FIELD)
+end program pnm_harness
+"""
+
+
+def pnm_cases():
+    """(name, plane [ny][nx] float32, parameters, receivers) per snapshot: wavefields of the
+    small reference runs and seeded planes, with sources and receivers on and
+    off the frame, each PML face off in turn, both fields, and an all-zero
+    plane (0/0 normalisation)."""
+    g = lambda n: dict(np.load(os.path.join(HERE, n + ".npz")))  # noqa: E731
+    a, b, c = g("refpin_2d_small"), g("refpin_2d4_small"), g("refpin_pml2d_small")
+    rng = np.random.default_rng(7)
+    syn = (rng.standard_normal((29, 37)) * 3.0).astype(np.float32)
+    syn[10, 10], syn[20, 30] = 7.0, -7.0                  # the extremes: +-1 after normalising
+    syn[5, 5:9] = np.float32(0.07)                        # about the 1 % cut
+    out = []
+    def case(name, plane, it, isrc, jsrc, npml, field, use, rec):
+        out.append((name, np.ascontiguousarray(plane, np.float32),
+                    dict(IT=it, ISRC=isrc, JSRC=jsrc, NPML=npml, FIELD=field, UXMIN=use[0],
+                         UXMAX=use[1], UYMIN=use[2], UYMAX=use[3]), np.asarray(rec, np.int32)))
+    case("vx_small", a["f_vx"], 400, int(a["p_isource"]), int(a["p_jsource"]), 10, 1, (1, 1, 1, 0),
+         a["rec"])
+    case("vy_corner", a["f_vy"], 400, 3, 4, 10, 2, (0, 1, 1, 1), [[4, 6], [1, 1], [40, 60]])
+    case("vx_fourth", b["f_vx"], 600, int(b["p_isource"]), int(b["p_jsource"]), 7, 1, (1, 0, 0, 1),
+         b["rec"])
+    case("sxy_split", c["f_sxy"], 5, 30, 50, 10, 2, (1, 1, 1, 1), c["rec"])
+    case("seeded", syn, 123456, 20, 14, 4, 1, (1, 1, 0, 1), [[10, 10]])
+    case("zero", np.zeros((23, 19), np.float32), 0, 9, 11, 3, 2, (1, 1, 1, 1), [[2, 2], [17, 21]])
+    return out
+
+
+def generate_pnm(ref_dir: str, out_dir: str = HERE) -> str:
+    import tempfile
+    t0 = time.time()
+    with tempfile.TemporaryDirectory() as tmp:
+        harness = os.path.join(tmp, "pnm_harness.f90")
+        with open(harness, "w") as f:
+            f.write(PNM_HARNESS)
+        out = {}
+        for name, plane, par, rec in pnm_cases():
+            ny, nx = plane.shape
+            ov = {"NX": nx, "NY": ny, "NREC": len(rec)}
+            ov.update({k: (".true." if v else ".false.") if k.startswith("U") else v
+                       for k, v in par.items()})
+            exe = ref_f90c.build(harness, "pnm_" + name, ov, (), load=["plane", "ix_rec", "iy_rec"],
+                                 subroutines=[(os.path.join(ref_dir, PROGRAMS["cpml2d"]),
+                                               "create_color_image")])
+            fname = f"image{par['IT']:06d}_{'Vx' if par['FIELD'] == 1 else 'Vy'}.pnm"
+            r = exe.run(inputs={"plane": plane.T.astype(np.float64),
+                                "ix_rec": rec[:, 0].copy(), "iy_rec": rec[:, 1].copy()},
+                        files=[fname])
+            out[name + "_plane"] = plane
+            out[name + "_rec"] = rec
+            out[name + "_par"] = np.array([par[k] for k in PNM_PAR], np.int32)
+            out[name + "_file"] = np.array(fname)
+            out[name + "_pnm"] = np.frombuffer(r[0]["files"][fname].encode(), np.uint8)
+    out["par_names"] = np.array(PNM_PAR)
+    path = os.path.join(out_dir, "refpin_pnm.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote refpin_pnm in {time.time() - t0:.1f} s")
+    return path
+
+
+PNM_PAR = ["IT", "ISRC", "JSRC", "NPML", "FIELD", "UXMIN", "UXMAX", "UYMIN", "UYMAX"]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-dir", default=ref_f90c.DEFAULT_REF_DIR)
     ap.add_argument("names", nargs="*")
     a = ap.parse_args()
-    for n in a.names or list(CASES):
-        generate(n, a.ref_dir)
+    for n in a.names or list(CASES) + ["refpin_pnm"]:
+        if n == "refpin_pnm":
+            generate_pnm(a.ref_dir)
+        else:
+            generate(n, a.ref_dir)
 
 
 if __name__ == "__main__":

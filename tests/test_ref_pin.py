@@ -269,6 +269,53 @@ def test_translator_rejects_what_it_does_not_know(tmp_path):
         ref_f90c.translate_file(str(src), {"NX": 3})
 
 
+IO_TEST = """\
+program iotest
+  implicit none
+  integer :: k
+  character(len=20) :: fname
+  k = 42
+  write(fname,"('out',i3.3,'.txt')") k
+  open(unit=12, file=fname, status='unknown')
+  write(12,"(i3,' ',i2,' x',i6.4)") 7, 123, -42
+  write(12,"('no items ',i4,' after')")
+  write(12,*) k, -3
+  write(12,*) 'abc'
+  close(12)
+end program iotest
+"""
+
+
+def test_translator_io(tmp_path):
+    """WRITE with I editing (the standard's rules: right-justified, at least
+    m digits, asterisks when the field is too narrow), output that stops at
+    the first data edit without an item, internal WRITE into a file name,
+    OPEN/CLOSE, and list-directed integers and strings."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "iotest.f90"
+    src.write_text(IO_TEST)
+    code, manifest = ref_f90c.translate_file(str(src), io=True)
+    (tmp_path / "iotest.c").write_text(code)
+    exe = tmp_path / "iotest"
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-w", "-o", str(exe), str(tmp_path / "iotest.c"),
+                    ref_f90c.MPI_RUNTIME, "-lm", "-lpthread"], check=True)
+    out = ref_f90c.RefProgram(str(exe), manifest).run(files=["out042.txt"])[0]["files"]["out042.txt"]
+    assert out.splitlines() == ["  7 ** x -0042", "no items ", "          42          -3", " abc"]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
+                    reason="needs the reference sources and gcc")
+def test_pnm_vectors_regenerate_from_reference_source(tmp_path):
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_ref_vectors as M
+    a, b = dict(np.load(M.generate_pnm(REF_DIR, str(tmp_path)))), load("refpin_pnm")
+    assert sorted(a) == sorted(b)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
 @pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
                     reason="needs the reference sources and gcc")
 @pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_3d_4ranks"])
@@ -314,3 +361,47 @@ def test_fp32_restatement_within_tolerance_of_reference(name):
     p, rec = params_of(fx)
     r = oracle_c.run(p, rec=rec, double=False)
     compare_fp32(fx, r.sisvx, r.sisvy, r.ek, r.ep)
+
+
+# ---------------------------------------------------------------------------
+# PNM snapshots
+# ---------------------------------------------------------------------------
+PNM_CASES = ["vx_small", "vy_corner", "vx_fourth", "sxy_split", "seeded", "zero"]
+
+
+@pytest.fixture(scope="module")
+def cpml_lib():
+    from seismic_cpml_gb300 import lib as L
+    from seismic_cpml_gb300.build import build
+    build()
+    return L.load()
+
+
+@pytest.mark.parametrize("case", PNM_CASES)
+def test_pnm_writer_reproduces_reference(case, cpml_lib, tmp_path):
+    """cpml_write_pnm against the programs' own create_color_image
+    (2D:861-999, translated and run on the same plane; refpin_pnm.npz).
+    The pixel records, written with the explicit format (i3,' ',i3,' ',i3),
+    must match byte for byte. The header lines are list-directed, whose
+    spacing is the compiler's choice, so only their tokens are compared."""
+    import ctypes
+    fx = load("refpin_pnm")
+    plane, rec = fx[case + "_plane"], fx[case + "_rec"]
+    par = dict(zip([str(n) for n in fx["par_names"]], (int(v) for v in fx[case + "_par"])))
+    ny, nx = plane.shape
+    use = np.array([par[k] for k in ("UXMIN", "UXMAX", "UYMIN", "UYMAX")], np.int32)
+    ix, iy = np.ascontiguousarray(rec[:, 0]), np.ascontiguousarray(rec[:, 1])
+    ip = ctypes.POINTER(ctypes.c_int)
+    st = cpml_lib.cpml_write_pnm(str(tmp_path).encode(),
+                                 plane.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), nx, ny,
+                                 par["IT"], par["ISRC"], par["JSRC"], ix.ctypes.data_as(ip),
+                                 iy.ctypes.data_as(ip), len(rec), par["NPML"], use.ctypes.data_as(ip),
+                                 par["FIELD"])
+    assert st == 0
+    ours = (tmp_path / str(fx[case + "_file"])).read_text().splitlines()
+    ref = bytes(fx[case + "_pnm"]).decode().splitlines()
+    assert [ln.split() for ln in ours[:3]] == [ln.split() for ln in ref[:3]]
+    assert len(ours) == len(ref) == 3 + nx * ny
+    bad = [k for k in range(3, len(ref)) if ours[k] != ref[k]]
+    assert not bad, f"{len(bad)} pixels differ, first at record {bad[0]}: {ours[bad[0]]!r} vs {ref[bad[0]]!r}"
+
