@@ -285,7 +285,8 @@ const char* cpml_strerror(int status);
    seismograms and fields are bit-identical to a single-shot handle running
    the same parameters (same per-cell arithmetic). No counterpart in the
    reference, which runs one shot per program execution; energy is not
-   recorded by the batched engine. */
+   recorded by the batched engine. Shots run the second-order C-PML program:
+   a shot with order 4 or the split-field scheme is CPML_ERR_INVALID. */
 typedef struct cpml_batch cpml_batch;
 int cpml_batch_create(int nshots, const cpml_params* params, cpml_batch** out);
 int cpml_batch_set_model(cpml_batch* b, int shot, const float* lambda, const float* mu,

@@ -202,6 +202,7 @@ int validate(const cpml_params* p) {
   if (!(p->cp > 0) || !(p->cs > 0) || !(p->rho > 0) || !(p->rcoef > 0 && p->rcoef < 1))
     return CPML_ERR_INVALID;
   if (p->npower < 1) return CPML_ERR_INVALID;  // 2D:293
+  if (p->stf < CPML_STF_DGAUSSIAN || p->stf > CPML_STF_RICKER) return CPML_ERR_INVALID;
   if (p->isource < 1 || p->isource > p->nx - 1 || p->jsource < 1 || p->jsource > p->ny - 1)
     return CPML_ERR_INVALID;
   if (p->ndim == 3 && (p->ksource < 1 || p->ksource > nz)) return CPML_ERR_INVALID;

@@ -648,6 +648,10 @@ int validate2d(const cpml_params& p) {
   if (!(p.deltax > 0) || !(p.deltay > 0) || !(p.deltat > 0) || !(p.cp > 0) || !(p.cs > 0) || !(p.rho > 0))
     return CPML_ERR_INVALID;
   if (!(p.rcoef > 0 && p.rcoef < 1) || p.npower < 1) return CPML_ERR_INVALID;
+  if (p.stf < CPML_STF_DGAUSSIAN || p.stf > CPML_STF_RICKER) return CPML_ERR_INVALID;
+  // the batched engine runs the second-order C-PML program only: a
+  // fourth-order or split-field shot would otherwise run the wrong program
+  if ((p.order != 0 && p.order != 2) || p.scheme != CPML_SCHEME_CPML) return CPML_ERR_INVALID;
   if (p.isource < 1 || p.isource > p.nx - 1 || p.jsource < 1 || p.jsource > p.ny - 1) return CPML_ERR_INVALID;
   if (cpml_courant(&p, p.cp) > 1.0) return CPML_ERR_CFL;
   return CPML_OK;

@@ -152,11 +152,27 @@ def test_create_validates_before_touching_the_device(lib):
     p.deltat = 4e-3                     # Courant 1.87 > 1: the reference stops (2D:516)
     assert lib.cpml_create(ctypes.byref(p), ctypes.byref(h)) == -2
     for field, value in (("nx", 2), ("npoints_pml", 0), ("isource", 0), ("ndim", 4), ("rcoef", 1.5),
-                         ("it_display", 0)):
+                         ("it_display", 0), ("stf", 3), ("stf", -1)):
         q = P.default_2d()
         setattr(q, field, value)
         assert lib.cpml_create(ctypes.byref(q), ctypes.byref(h)) == -1, field
     assert lib.cpml_create(None, ctypes.byref(h)) == -1
+
+
+def test_batch_create_validates_before_touching_the_device(lib):
+    """Every shot is checked first; the batched engine runs the second-order
+    C-PML program only, so fourth-order and split-field shots are refused
+    rather than run as another program."""
+    b = ctypes.c_void_p()
+    ok = P.default_2d()
+    for field, value in (("stf", 5), ("order", 4), ("scheme", P.SCHEME_SPLIT), ("isource", 0)):
+        q = P.default_2d()
+        setattr(q, field, value)
+        arr = (P.CpmlParams * 2)(ok, q)
+        assert lib.cpml_batch_create(2, arr, ctypes.byref(b)) == -1, field
+    q = P.default_2d()
+    q.deltat = 4e-3
+    assert lib.cpml_batch_create(1, (P.CpmlParams * 1)(q), ctypes.byref(b)) == -2
 
 
 def test_create_without_gpu_reports_cuda(lib):
