@@ -1089,11 +1089,23 @@ class Translator:
         self.ind -= 1
 
     # ---- whole program ------------------------------------------------------------
-    def body(self, stmts):
-        """Translate the executable statements of one unit; returns its C lines."""
+    def body(self, stmts, load_after=None):
+        """Translate the executable statements of one unit; returns its C lines.
+        load_after = (line, names): the named arrays are loaded from the input
+        directory right after the statement that starts on that source line."""
+        hit = 0
         for ln, s in stmts:
             self.ln = ln
             self.statement(s)
+            if load_after and ln == load_after[0]:
+                hit += 1
+                for name in load_after[1]:
+                    sym = self.syms.get(name)
+                    if sym is None or not sym.dims or sym.param:
+                        raise TranslateError(f"cannot load {name}: not an array variable")
+                    self.emit(f'ref_load("{name}", {sym.cname}, sizeof({sym.cname}));')
+        if load_after and hit != 1:
+            raise TranslateError(f"no statement starts on line {load_after[0]}")
         if self.blocks:
             raise TranslateError(f"unclosed {self.blocks[-1].upper()} block at the end")
         if self.timed_loop and not self.timer_used:
@@ -1139,7 +1151,7 @@ class Translator:
             head.append(f"  {CTYPE[sym.ftype]}* d_{a} = ({CTYPE[sym.ftype]}*)p{k};")
         return head + body + ["}", ""]
 
-    def translate(self, stmts, dump=(), load=(), subroutines=()):
+    def translate(self, stmts, dump=(), load=(), subroutines=(), load_after=None):
         """C source of the main program (and of the subroutine units given as
         (name, dummy names, statements)), with `load`ed variables read from
         the input directory before the first statement and `dump`ed ones
@@ -1154,7 +1166,7 @@ class Translator:
             sub_funcs += fn
             cap = max(cap, c_)
             self.subs[sname] = len(args)
-        body = self.body(stmts)
+        body = self.body(stmts, load_after)
         self.ind = 1
         for name in load:
             s = self.syms.get(name)
@@ -1353,14 +1365,15 @@ def _assign_pos(s: str):
 # ---------------------------------------------------------------------------
 def translate_file(src: str, overrides: dict | None = None, dump=(), bounds=True,
                    stf: str | None = None, timed_loop: str | None = None, load=(),
-                   subroutines=(), io: bool = False):
+                   subroutines=(), io: bool = False, load_after=None):
     """C source and dump manifest of src's main program. subroutines lists
     (file, name) units to translate beside it and call; io translates the
-    main program's WRITE/OPEN/CLOSE as well (always done in subroutines)."""
+    main program's WRITE/OPEN/CLOSE as well (always done in subroutines);
+    load and load_after name variables read from files (Translator.body)."""
     stmts = main_program(read_statements(src, stf))
     units = [(name, *subroutine_unit(read_statements(path), name)) for path, name in subroutines]
     T = Translator(overrides, bounds, timed_loop, io=io)
-    return T.translate(stmts, dump, load, units)
+    return T.translate(stmts, dump, load, units, load_after)
 
 
 @dataclass
@@ -1427,13 +1440,14 @@ TIMING_FLAGS = ["-O3"]
 
 def build(src: str, tag: str, overrides: dict | None = None, dump=(), bounds=True,
           stf: str | None = None, timed_loop: str | None = None, cc: str = "gcc",
-          flags: list | None = None, load=(), subroutines=(), io: bool = False) -> RefProgram:
+          flags: list | None = None, load=(), subroutines=(), io: bool = False,
+          load_after=None) -> RefProgram:
     """Translate src with the given parameter overrides (and source-time
     function, when stf names one) into oracle/_ref/<tag>.c, then compile it
     for this machine (compile_translated) with `flags` (PARITY_FLAGS by
     default)."""
     code, manifest = translate_file(src, overrides, dump, bounds, stf, timed_loop, load,
-                                    subroutines, io)
+                                    subroutines, io, load_after)
     os.makedirs(REF_OUT, exist_ok=True)
     cpath = os.path.join(REF_OUT, tag + ".c")
     if not (os.path.exists(cpath) and open(cpath).read() == code):

@@ -31,6 +31,7 @@ from __future__ import annotations
 import argparse
 import hashlib
 import os
+import re
 import sys
 import time
 
@@ -72,12 +73,18 @@ FIELDS = {
 }
 
 # name -> (program, overrides, source-time function or None for the
-#          program's active line, emulated ranks, keep full fields)
+#          program's active line, emulated ranks, keep full fields
+#          [, seed of a per-cell model read in after the material fill])
 CASES = {
     # the programs exactly as shipped
     "refpin_2d_shipped": ("cpml2d", {}, None, 1, False),
     "refpin_2d4_shipped": ("cpml2d4", {}, None, 1, False),
     "refpin_pml2d_shipped": ("pml2d", {}, None, 1, False),
+    # the 2D plain workload (101 x 641, 2000 steps): Ricker at the centre
+    # (51, 321), 45 degrees, no PML on the top edge, receivers by the
+    # program's own rule relative to that source
+    "refpin_2d_plain": ("cpml2d", {"ISOURCE": 51, "JSOURCE": 321, "ANGLE_FORCE": "45.d0",
+                                   "USE_PML_YMAX": ".false."}, "ricker", 1, False),
     # small grids with the parameters moved: one PML face off, another
     # angle, three receivers, the Ricker wavelet (as in the 2D plain workload)
     "refpin_2d_small": ("cpml2d", {"NX": 41, "NY": 61, "NSTEP": 400, "USE_PML_YMAX": ".false.",
@@ -106,6 +113,13 @@ CASES = {
                                       "DELTAT": "1.2d-3", "NPOWER": "2.5d0", "K_MAX_PML": "4.d0",
                                       "NPOINTS_PML": 9, "ANGLE_FORCE": "200.d0", "ydeb": "220.d0",
                                       "yfin": "80.d0"}, "gaussian", 2, False),
+    # per-cell models (the programs' lambda, mu and rho arrays, 2D:204, with
+    # their averaging rules, 2D:560-562, 586, 627): a seeded layered model
+    # with anomalies, read in after the programs' homogeneous fill
+    "refpin_2d_het": ("cpml2d", {"NX": 61, "NY": 73, "NSTEP": 600, "DELTAT": "1.5d-3",
+                                 "ydeb": "500.d0", "yfin": "200.d0"}, "ricker", 1, True, 11),
+    "refpin_2d4_het": ("cpml2d4", {"NX": 57, "NY": 65, "NSTEP": 800, "ydeb": "450.d0",
+                                   "yfin": "150.d0"}, None, 1, True, 12),
     # 3D on 2 and 4 ranks: the z-slab exchanges of 3D:811-823 and 951-963 run
     "refpin_3d_2ranks": ("cpml3d", {"NX": 36, "NY": 40, "NZ": 40, "NPROC": 2, "NSTEP": 200,
                                     "ydeb": "300.d0", "yfin": "100.d0"}, None, 2, False),
@@ -125,8 +139,24 @@ def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
 
 
+def fill_end_line(src: str) -> int:
+    """Source line of the END DO that closes the 2D programs' homogeneous
+    material fill (the loop nest that sets rho(i,j) = density, 2D:467-473)."""
+    lines = open(src, encoding="latin-1").read().split("\n")
+    start = next(k for k, ln in enumerate(lines) if re.match(r"\s*rho\(i,j\)\s*=\s*density", ln, re.I))
+    ends = [k for k in range(start, len(lines)) if re.match(r"\s*end\s*do\s*$", lines[k], re.I)]
+    return ends[1] + 1
+
+
+def model_2d(nx, ny, seed):
+    """Seeded float32 lambda, mu, rho of shape (ny, nx) (tests/models.py)."""
+    from types import SimpleNamespace
+    from tests.models import layered_2d
+    return layered_2d(SimpleNamespace(nx=nx, ny=ny, cp=3300.0), seed)
+
+
 def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
-    prog, overrides, stf, nprocs, keep = CASES[name]
+    prog, overrides, stf, nprocs, keep, *seed = CASES[name]
     src = os.path.join(ref_dir, PROGRAMS[prog])
     three_d = prog == "cpml3d"
     fields = FIELDS[prog]
@@ -137,8 +167,17 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
     big = name.endswith("_full")
     dump = outs + PARAMS[prog] + ([] if big else arrays)
     t0 = time.time()
-    exe = ref_f90c.build(src, name, overrides, dump, bounds=not big, stf=stf)
-    ranks = exe.run(nprocs=nprocs, timeout=7200)
+    model, load_after, inputs = None, None, None
+    if seed:      # the model goes into the program's own arrays after its fill
+        model = model_2d(int(overrides["NX"]), int(overrides["NY"]), seed[0])
+        load_after = (fill_end_line(src), ["lambda", "mu", "rho"])
+        # the fourth-order program's arrays are (0:NX+1, 0:NY+1): its fill
+        # leaves the halo cells at their static zero, which no update reads
+        pad = 1 if prog == "cpml2d4" else 0
+        inputs = {k: np.pad(m.T.astype(np.float64), pad) for k, m in zip(load_after[1], model)}
+    exe = ref_f90c.build(src, name, overrides, dump, bounds=not big, stf=stf,
+                         load_after=load_after)
+    ranks = exe.run(nprocs=nprocs, timeout=7200, inputs=inputs)
     cut = int(ranks[0]["rank_cut_plane"]) if three_d else 0
     d = ranks[cut]
     out = {"program": np.array(PROGRAMS[prog]), "stf": np.array(stf or "program default"),
@@ -153,6 +192,8 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
             out["sha_" + k] = np.array(digest(tr))
         else:
             out[k] = tr
+    if model is not None:
+        out["lam"], out["mu"], out["rho"] = model
     if three_d:
         out["energy"] = d["total_energy"]
     else:

@@ -9,14 +9,15 @@ the other GPU tests do not:
   - the Ricker and Gaussian wavelets of the programs' alternative lines;
   - receiver lines of three points;
   - the fourth-order program with its x-min face off;
-  - 3D with the x-min and z-max faces off.
+  - 3D with the x-min and z-max faces off;
+  - per-cell models in the second- and fourth-order programs.
 Tolerances (relative L2, the reference's FP64 run as truth): seismograms
 1e-5, energy curve 1e-6. The 3D program records vx and vy only.
 """
 import pytest
 
 from seismic_cpml_gb300.solver import Solver
-from tests.test_ref_pin import SHIPPED, SMALL, compare_fp32, load, params_of
+from tests.test_ref_pin import SHIPPED, SMALL, compare_fp32, load, model_of, params_of
 
 pytestmark = pytest.mark.gpu
 
@@ -25,7 +26,7 @@ pytestmark = pytest.mark.gpu
 def test_gpu_matches_reference(name):
     fx = load(name)
     p, rec = params_of(fx)
-    with Solver(p, rec) as s:
+    with Solver(p, rec, model=model_of(fx)) as s:
         s.run()
         vx, vy, _ = s.seismograms()
         ek, ep = s.energy()

@@ -35,8 +35,9 @@ from seismic_cpml_gb300 import params as P
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 REF_DIR = ref_f90c.DEFAULT_REF_DIR
 SMALL = ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small", "refpin_3d_2ranks",
-         "refpin_3d_4ranks", "refpin_2d_profiles", "refpin_2d4_profiles", "refpin_3d_profiles"]
-SHIPPED = ["refpin_2d_shipped", "refpin_2d4_shipped", "refpin_pml2d_shipped"]
+         "refpin_3d_4ranks", "refpin_2d_profiles", "refpin_2d4_profiles", "refpin_3d_profiles",
+         "refpin_2d_het", "refpin_2d4_het"]
+SHIPPED = ["refpin_2d_shipped", "refpin_2d4_shipped", "refpin_pml2d_shipped", "refpin_2d_plain"]
 STF = {"ricker": P.STF_RICKER, "gaussian": P.STF_GAUSSIAN, "program default": P.STF_DGAUSSIAN}
 
 
@@ -106,22 +107,30 @@ def check(fx, r):
             assert digest(r.fields[k[4:]]) == str(fx[k]), f"field {k[4:]} differs"
 
 
+def model_of(fx):
+    """The per-cell model (lambda, mu, rho) a fixture's run read in, or None."""
+    return (fx["lam"], fx["mu"], fx["rho"]) if "lam" in fx else None
+
+
 @pytest.mark.parametrize("name", SMALL + SHIPPED)
 def test_oracle_reproduces_reference(name):
     fx = load(name)
     p, rec = params_of(fx)
-    check(fx, oracle_c.run(p, rec=rec, keep_fields=True))
+    m = model_of(fx)
+    kw = dict(lam=m[0], mu=m[1], rho=m[2]) if m else {}
+    check(fx, oracle_c.run(p, rec=rec, keep_fields=True, **kw))
 
 
 @pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small",
-                                  "refpin_3d_2ranks"])
+                                  "refpin_3d_2ranks", "refpin_2d_het"])
 def test_numpy_restatement_reproduces_reference(name):
     fx = load(name)
     p, rec = params_of(fx)
     run = oracle_np.run3d if p.ndim == 3 else (
         oracle_np.run2d4 if p.order == 4 else
         oracle_np.run_split if p.scheme == P.SCHEME_SPLIT else oracle_np.run2d)
-    r = run(p, rec=rec)
+    m = model_of(fx)
+    r = run(p, rec=rec, **(dict(lam=m[0], mu=m[1], rho=m[2]) if m else {}))
     assert np.array_equal(r.sisvx, fx["sisvx"])
     assert np.array_equal(r.sisvy, fx["sisvy"])
     e_ref = fx["energy"] if "energy" in fx else fx["ek"] + fx["ep"]
@@ -129,10 +138,10 @@ def test_numpy_restatement_reproduces_reference(name):
 
 
 def test_shipped_fixtures_are_the_reference():
-    """The oracle's fixtures of the programs as shipped (used by the GPU
-    tests) equal the reference's own outputs."""
+    """The oracle's fixtures of the programs as shipped and of the 2D plain
+    workload (used by the GPU tests) equal the reference's own outputs."""
     for ours, ref in (("ref2d_default", "refpin_2d_shipped"), ("ref2d_fourth", "refpin_2d4_shipped"),
-                      ("ref2d_split", "refpin_pml2d_shipped")):
+                      ("ref2d_split", "refpin_pml2d_shipped"), ("config_2d_plain", "refpin_2d_plain")):
         a, b = load(ours), load(ref)
         assert np.array_equal(a["rec"][:, :2], b["rec"]), ours
         for k in ("sisvx", "sisvy", "ek", "ep"):
@@ -359,7 +368,8 @@ def test_fp32_restatement_within_tolerance_of_reference(name):
     GPU runs, here on the CPU."""
     fx = load(name)
     p, rec = params_of(fx)
-    r = oracle_c.run(p, rec=rec, double=False)
+    m = model_of(fx)
+    r = oracle_c.run(p, rec=rec, double=False, **(dict(lam=m[0], mu=m[1], rho=m[2]) if m else {}))
     compare_fp32(fx, r.sisvx, r.sisvy, r.ek, r.ep)
 
 
