@@ -1,7 +1,11 @@
 // driver.cpp -- cpml_program: the two reference programs as one C++ host
 // program over the C ABI.
 //
-// Usage:  cpml_program [2d|3d] [params.par] [output_dir]
+// Usage:  cpml_program [2d|3d] [params.par | program.f90] [output_dir] [--print-params]
+//
+// The parameters come from a params.par file of "NAME = value" lines, or
+// from a reference program's own source file (.f90): its parameter block,
+// evaluated as Fortran evaluates it (read_fortran_params).
 //
 // It replaces the main program units of
 //   seismic_CPML_2D_isotropic_second_order.f90  (program seismic_CPML_2D_iso_second)
@@ -122,6 +126,304 @@ int read_params(const char* path, Setup& S) {
   return 0;
 }
 
+// ---- the reference program's own source as the parameter file -------------
+// A reference program is configured by editing its `parameter` lines
+// (2D:138-218, 3D:124-218). Given that .f90 file, the driver evaluates those
+// declarations as Fortran does: integer arithmetic truncates, literals
+// without a D exponent are single precision, ** with an integer exponent is
+// repeated multiplication. It also reads Rcoef from its assignment (2D:289)
+// and the wavelet from whichever source_term line is not commented out
+// (2D:648-654). Names the solver has no use for (PI, HUGEVAL, NPROC, ...)
+// are evaluated and ignored.
+struct FVal {
+  double v = 0;
+  int kind = 2;   // 0 integer/logical, 1 single precision, 2 double precision
+};
+
+FVal fnorm(FVal x) {
+  if (x.kind == 1) x.v = double(float(x.v));
+  return x;
+}
+
+class FExpr {
+ public:
+  FExpr(const std::string& s, const std::map<std::string, FVal>& sym) : s_(s), sym_(sym) {}
+  bool eval(FVal* out, std::string* err) {
+    FVal v = add();
+    skip();
+    if (!err_.empty() || i_ != s_.size()) {
+      *err = err_.empty() ? "unexpected '" + s_.substr(i_) + "'" : err_;
+      return false;
+    }
+    *out = v;
+    return true;
+  }
+
+ private:
+  const std::string& s_;
+  const std::map<std::string, FVal>& sym_;
+  size_t i_ = 0;
+  std::string err_;
+  void skip() { while (i_ < s_.size() && std::isspace((unsigned char)s_[i_])) ++i_; }
+  bool eat(const char* t) {
+    skip();
+    const size_t n = std::strlen(t);
+    if (s_.compare(i_, n, t) == 0) { i_ += n; return true; }
+    return false;
+  }
+  static FVal arith(char op, FVal a, FVal b) {
+    FVal r;
+    r.kind = std::max(a.kind, b.kind);
+    if (r.kind == 0) {
+      const long long x = (long long)a.v, y = (long long)b.v;
+      r.v = double(op == '+' ? x + y : op == '-' ? x - y : op == '*' ? x * y : (y ? x / y : 0));
+      return r;
+    }
+    r.v = op == '+' ? a.v + b.v : op == '-' ? a.v - b.v : op == '*' ? a.v * b.v : a.v / b.v;
+    return fnorm(r);
+  }
+  FVal add() {
+    FVal v;
+    if (eat("-")) { v = mul(); v.v = -v.v; }
+    else { eat("+"); v = mul(); }
+    for (;;) {
+      if (eat("+")) v = arith('+', v, mul());
+      else if (eat("-")) v = arith('-', v, mul());
+      else return v;
+    }
+  }
+  FVal mul() {
+    FVal v = pw();
+    for (;;) {
+      skip();
+      if (s_.compare(i_, 2, "**") == 0) return v;
+      if (eat("*")) v = arith('*', v, pw());
+      else if (eat("/")) v = arith('/', v, pw());
+      else return v;
+    }
+  }
+  FVal pw() {
+    FVal b = prim();
+    if (!eat("**")) return b;
+    FVal e = pw();
+    FVal r;
+    if (e.kind == 0) {             // repeated multiplication
+      const long long n = (long long)e.v;
+      r.kind = b.kind;
+      double acc = 1.0;
+      for (long long k = 0; k < (n < 0 ? -n : n); ++k) acc = (r.kind == 1) ? double(float(acc * b.v)) : acc * b.v;
+      r.v = n < 0 ? 1.0 / acc : acc;
+      return fnorm(r);
+    }
+    r.kind = (b.kind == 2 || e.kind == 2) ? 2 : 1;   // a real power of reals
+    r.v = std::pow(b.v, e.v);
+    return fnorm(r);
+  }
+  FVal prim() {
+    skip();
+    FVal v;
+    if (eat("(")) {
+      v = add();
+      if (!eat(")")) err_ = "missing ')'";
+      return v;
+    }
+    if (eat(".true.")) { v.v = 1; v.kind = 0; return v; }
+    if (eat(".false.")) { v.v = 0; v.kind = 0; return v; }
+    if (i_ < s_.size() && (std::isdigit((unsigned char)s_[i_]) || s_[i_] == '.')) {
+      const size_t b = i_;
+      while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+      bool real = false;
+      if (i_ < s_.size() && s_[i_] == '.' && !(i_ + 1 < s_.size() && std::isalpha((unsigned char)s_[i_ + 1]) &&
+                                                 s_[i_ + 1] != 'd' && s_[i_ + 1] != 'e')) {
+        real = true;
+        ++i_;
+        while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+      }
+      int kind = real ? 1 : 0;
+      if (i_ < s_.size() && (s_[i_] == 'd' || s_[i_] == 'e')) {
+        kind = s_[i_] == 'd' ? 2 : 1;
+        ++i_;
+        if (i_ < s_.size() && (s_[i_] == '+' || s_[i_] == '-')) ++i_;
+        while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+      }
+      std::string t = s_.substr(b, i_ - b);
+      for (char& c : t) if (c == 'd') c = 'e';
+      v.kind = kind;
+      v.v = kind == 0 ? double(std::strtoll(t.c_str(), nullptr, 10))
+                      : kind == 1 ? double(std::strtof(t.c_str(), nullptr)) : std::strtod(t.c_str(), nullptr);
+      return v;
+    }
+    size_t b = i_;
+    while (i_ < s_.size() && (std::isalnum((unsigned char)s_[i_]) || s_[i_] == '_')) ++i_;
+    const std::string name = s_.substr(b, i_ - b);
+    auto it = sym_.find(name);
+    if (name.empty() || it == sym_.end()) {
+      if (err_.empty()) err_ = name.empty() ? "expected a value" : "unknown name " + name;
+      return v;
+    }
+    return it->second;
+  }
+};
+
+// statements of a free-form Fortran file: comments removed, continuation
+// lines joined, lower case outside string literals
+std::vector<std::string> fortran_statements(std::istream& in) {
+  std::vector<std::string> out;
+  std::string line, buf;
+  char quote = 0;
+  while (std::getline(in, line)) {
+    if (!buf.empty()) {
+      const size_t b = line.find_first_not_of(" \t");
+      line = b == std::string::npos ? "" : line.substr(b);
+      if (!line.empty() && line[0] == '&') line = line.substr(1);
+    }
+    std::string t;
+    for (char c : line) {
+      if (quote) { t += c; if (c == quote) quote = 0; continue; }
+      if (c == '\'' || c == '"') { quote = c; t += c; continue; }
+      if (c == '!') break;
+      t += (char)std::tolower((unsigned char)c);
+    }
+    t.erase(t.find_last_not_of(" \t\r") + 1);
+    if (t.empty()) continue;
+    if (t.back() == '&') { t.pop_back(); buf += t; continue; }
+    buf += t;
+    const size_t b = buf.find_first_not_of(" \t");
+    out.push_back(buf.substr(b));
+    buf.clear();
+    quote = 0;
+  }
+  return out;
+}
+
+std::vector<std::string> split_top(const std::string& s) {
+  std::vector<std::string> out;
+  int depth = 0;
+  std::string cur;
+  for (char c : s) {
+    if (c == '(') ++depth;
+    if (c == ')') --depth;
+    if (c == ',' && depth == 0) { out.push_back(cur); cur.clear(); continue; }
+    cur += c;
+  }
+  out.push_back(cur);
+  return out;
+}
+
+std::string trim(const std::string& s) {
+  const size_t b = s.find_first_not_of(" \t"), e = s.find_last_not_of(" \t");
+  return b == std::string::npos ? "" : s.substr(b, e - b + 1);
+}
+
+int read_fortran_params(const char* path, Setup& S, bool three_d) {
+  std::ifstream f(path);
+  if (!f) { std::fprintf(stderr, "cannot open %s\n", path); return 1; }
+  std::map<std::string, FVal> sym;
+  int n_source_lines = 0;
+  for (const std::string& st : fortran_statements(f)) {
+    const bool decl = st.rfind("integer", 0) == 0 || st.rfind("double precision", 0) == 0 ||
+                      st.rfind("logical", 0) == 0 || st.rfind("real", 0) == 0;
+    const size_t dc = st.find("::");
+    if (decl && dc != std::string::npos && st.substr(0, dc).find("parameter") != std::string::npos) {
+      const int kind = st.rfind("integer", 0) == 0 || st.rfind("logical", 0) == 0 ? 0
+                       : st.rfind("real", 0) == 0 ? 1 : 2;
+      for (const std::string& ent : split_top(st.substr(dc + 2))) {
+        const size_t eq = ent.find('=');
+        if (eq == std::string::npos) continue;
+        const std::string name = trim(ent.substr(0, eq)), ex = trim(ent.substr(eq + 1));
+        FVal v;
+        std::string err;
+        if (!FExpr(ex, sym).eval(&v, &err)) {
+          std::fprintf(stderr, "%s: parameter %s = %s: %s\n", path, name.c_str(), ex.c_str(), err.c_str());
+          return 1;
+        }
+        if (kind == 0) v.v = double((long long)v.v);   // integer parameters truncate
+        v.kind = kind;
+        sym[name] = fnorm(v);
+      }
+      continue;
+    }
+    // Rcoef is assigned, not declared a parameter (2D:289, 3D:408)
+    if (st.rfind("rcoef", 0) == 0 && st.find('=') != std::string::npos) {
+      FVal v;
+      std::string err;
+      if (FExpr(trim(st.substr(st.find('=') + 1)), sym).eval(&v, &err)) sym["rcoef"] = v;
+      continue;
+    }
+    // the active source-time function (2D:648-654): its source_term line
+    if (st.rfind("source_term", 0) == 0 && st.find('=') != std::string::npos) {
+      ++n_source_lines;
+      const std::string r = st.substr(st.find('=') + 1);
+      S.p.stf = r.find("(1.d0 - 2.d0") != std::string::npos ? CPML_STF_RICKER
+              : r.find("2.d0*a*(t-t0)") != std::string::npos ? CPML_STF_DGAUSSIAN : CPML_STF_GAUSSIAN;
+    }
+  }
+  if (n_source_lines != 1) {
+    std::fprintf(stderr, "%s: expected one active source_term line, found %d\n", path, n_source_lines);
+    return 1;
+  }
+  auto get = [&](const char* k, double* dst) {
+    auto it = sym.find(k);
+    if (it != sym.end()) { *dst = it->second.v; S.given[upper(k)] = true; }
+    return it != sym.end();
+  };
+  auto geti = [&](const char* k, int* dst) {
+    double v;
+    if (get(k, &v)) *dst = (int)v;
+  };
+  cpml_params& p = S.p;
+  const char* need[] = {"nx", "ny", "deltax", "deltat", "nstep", "npoints_pml", "cp", "cs", "f0",
+                        "factor", "isource", "jsource", "angle_force"};
+  for (const char* k : need)
+    if (!sym.count(k)) { std::fprintf(stderr, "%s: no parameter %s\n", path, k); return 1; }
+  geti("nx", &p.nx); geti("ny", &p.ny); geti("nstep", &p.nstep); geti("npoints_pml", &p.npoints_pml);
+  get("deltax", &p.deltax); get("deltay", &p.deltay); get("deltat", &p.deltat);
+  get("cp", &p.cp); get("cs", &p.cs); get("f0", &p.f0); get("t0", &p.t0); get("factor", &p.factor);
+  if (!get("density", &p.rho)) get("rho", &p.rho);
+  geti("isource", &p.isource); geti("jsource", &p.jsource); get("angle_force", &p.angle_force);
+  geti("it_display", &p.it_display);
+  get("npower", &p.npower); get("k_max_pml", &p.k_max_pml); get("alpha_max_pml", &p.alpha_max_pml);
+  get("rcoef", &p.rcoef);
+  const char* faces[6] = {"use_pml_xmin", "use_pml_xmax", "use_pml_ymin", "use_pml_ymax",
+                          "use_pml_zmin", "use_pml_zmax"};
+  for (int q = 0; q < (three_d ? 6 : 4); ++q) geti(faces[q], &p.use_pml[q]);
+  if (three_d) {
+    geti("nz", &p.nz);
+    get("deltaz", &p.deltaz);
+    p.ksource = p.nz / 2;      // the cut plane of rank nb_procs/2 - 1 (3D:346, 1080)
+    S.given["KSOURCE"] = true;
+  }
+  int nrec = S.nrec;
+  geti("nrec", &nrec);
+  S.nrec = nrec;
+  get("xdeb", &S.xdeb); get("ydeb", &S.ydeb); get("xfin", &S.xfin); get("yfin", &S.yfin);
+  S.rec_given = true;
+  return 0;
+}
+
+void print_params(const Setup& S, bool three_d) {
+  const cpml_params& p = S.p;
+  std::printf("NX = %d\nNY = %d\n", p.nx, p.ny);
+  if (three_d) std::printf("NZ = %d\n", p.nz);
+  std::printf("NSTEP = %d\nNPOINTS_PML = %d\nIT_DISPLAY = %d\n", p.nstep, p.npoints_pml, p.it_display);
+  std::printf("DELTAX = %.17g\nDELTAY = %.17g\n", p.deltax, p.deltay);
+  if (three_d) std::printf("DELTAZ = %.17g\n", p.deltaz);
+  std::printf("DELTAT = %.17g\ncp = %.17g\ncs = %.17g\nrho = %.17g\n", p.deltat, p.cp, p.cs, p.rho);
+  std::printf("f0 = %.17g\nt0 = %.17g\nfactor = %.17g\nANGLE_FORCE = %.17g\n", p.f0, p.t0, p.factor,
+              p.angle_force);
+  std::printf("ISOURCE = %d\nJSOURCE = %d\n", p.isource, p.jsource);
+  if (three_d) std::printf("KSOURCE = %d\n", p.ksource);
+  std::printf("NPOWER = %.17g\nK_MAX_PML = %.17g\nALPHA_MAX_PML = %.17g\nRCOEF = %.17g\n", p.npower,
+              p.k_max_pml, p.alpha_max_pml, p.rcoef);
+  const char* faces[6] = {"USE_PML_XMIN", "USE_PML_XMAX", "USE_PML_YMIN", "USE_PML_YMAX",
+                          "USE_PML_ZMIN", "USE_PML_ZMAX"};
+  for (int q = 0; q < (three_d ? 6 : 4); ++q) std::printf("%s = %s\n", faces[q], p.use_pml[q] ? ".true." : ".false.");
+  std::printf("SOURCE_TIME_FUNCTION = %s\n", p.stf == CPML_STF_RICKER ? "ricker"
+                                            : p.stf == CPML_STF_DGAUSSIAN ? "derivative_of_gaussian" : "gaussian");
+  std::printf("NREC = %d\nXDEB = %.17g\nYDEB = %.17g\nXFIN = %.17g\nYFIN = %.17g\n", S.nrec, S.xdeb, S.ydeb,
+              S.xfin, S.yfin);
+}
+
 void write_gnuplot(const std::string& dir, bool three_d, int nrec) {
   FILE* f = std::fopen((dir + "/plot_energy").c_str(), "w");
   if (f) {
@@ -165,11 +467,25 @@ void write_gnuplot(const std::string& dir, bool three_d, int nrec) {
 
 }  // namespace
 
-int main(int argc, char** argv) {
+int main(int argc_in, char** argv_in) {
+  // --print-params: print the resolved parameter block (params.par format)
+  // and the receiver points, then stop before any device call
+  bool print_only = false;
+  std::vector<char*> args;
+  for (int a = 0; a < argc_in; ++a) {
+    if (std::strcmp(argv_in[a], "--print-params") == 0) print_only = true;
+    else args.push_back(argv_in[a]);
+  }
+  const int argc = (int)args.size();
+  char** argv = args.data();
   const bool three_d = argc > 1 && std::strcmp(argv[1], "3d") == 0;
   Setup S;
   if (three_d) cpml_params_default_3d(&S.p); else cpml_params_default_2d(&S.p);
-  if (argc > 2 && std::strcmp(argv[2], "-") != 0 && read_params(argv[2], S)) return 2;
+  if (argc > 2 && std::strcmp(argv[2], "-") != 0) {
+    const std::string path = argv[2];
+    const bool f90 = path.size() > 4 && upper(path.substr(path.size() - 4)) == ".F90";
+    if ((f90 ? read_fortran_params(argv[2], S, three_d) : read_params(argv[2], S))) return 2;
+  }
   const std::string dir = argc > 3 ? argv[3] : ".";
   cpml_params& p = S.p;
   // derived constants of the parameter block follow the grid unless given
@@ -202,6 +518,10 @@ int main(int argc, char** argv) {
                 xr, yr, ix[r], iy[r]);
   }
   std::printf(" Courant number is %.15g\n\n", cpml_courant(&p, p.cp));
+  if (print_only) {
+    print_params(S, three_d);
+    return 0;
+  }
 
   cpml_handle* h = nullptr;
   int st = cpml_create(&p, &h);

@@ -68,3 +68,108 @@ def test_program_2d_default_outputs(program, tmp_path, golden):
     assert (tmp_path / "plotgnu").exists() and (tmp_path / "plot_energy").exists()
     cmp_script = (tmp_path / "plot_comparison").read_text()   # 2D:764-777
     assert '"../collino/energy.dat" us 1:4' in cmp_script and "compare_total_energy_semilog.eps" in cmp_script
+
+
+# ---------------------------------------------------------------------------
+# the reference program's own source as the parameter file
+# ---------------------------------------------------------------------------
+REF_CASES = ["refpin_2d_shipped", "refpin_2d_small", "refpin_2d_profiles", "refpin_2d_plain",
+             "refpin_3d_2ranks", "refpin_3d_4ranks", "refpin_3d_profiles", "refpin_3d_plain_full"]
+
+
+def edited_source(src, overrides, stf):
+    """The program's text with its parameter lines edited as a user edits
+    them, and the chosen wavelet line active."""
+    import re
+    from oracle import ref_f90c
+    lines = open(src, encoding="latin-1").read().split("\n")
+    for name, value in overrides.items():
+        rx = re.compile(r"(?i)(\b%s\s*=\s*)([^,!]+)" % re.escape(name))
+        for k, ln in enumerate(lines):
+            if not ln.lstrip().startswith("!") and "parameter" in ln.lower() and rx.search(ln):
+                lines[k] = rx.sub(lambda m: m.group(1) + str(value) + " ", ln, count=1)
+                break
+        else:
+            raise AssertionError(f"no parameter line for {name}")
+    if stf is not None:
+        lines = ref_f90c.select_source_time_function(lines, stf)
+    return "\n".join(lines)
+
+
+@pytest.mark.parametrize("name", REF_CASES)
+def test_reference_source_as_parameter_file(program, tmp_path, name):
+    """cpml_program reads a reference program's .f90 file as its parameter
+    file. Every parameter it resolves, and every receiver point, equals what
+    the program itself evaluated when translated and run (the p_* values and
+    receivers of the reference vectors), bit for bit."""
+    import ast
+    import os
+    import sys
+    from oracle import ref_f90c
+    if not os.path.isdir(ref_f90c.DEFAULT_REF_DIR):
+        pytest.skip("needs the reference sources")
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, gold)
+    import make_ref_vectors as M
+    prog, overrides, stf = M.CASES[name][:3]
+    fx = dict(np.load(os.path.join(gold, name + ".npz")))
+    src = tmp_path / "program.f90"
+    src.write_text(edited_source(os.path.join(ref_f90c.DEFAULT_REF_DIR, M.PROGRAMS[prog]), overrides, stf))
+    three_d = prog == "cpml3d"
+    r = subprocess.run([program, "3d" if three_d else "2d", str(src), str(tmp_path), "--print-params"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = {}
+    for ln in r.stdout.splitlines():
+        if " = " in ln and not ln.startswith(" "):
+            k, v = ln.split(" = ", 1)
+            got[k.lower()] = v.strip()
+    rho = "rho" if three_d else "density"
+    pairs = {"nx": "nx", "ny": "ny", "nstep": "nstep", "npoints_pml": "npoints_pml",
+             "it_display": "it_display", "deltax": "deltax", "deltay": "deltay", "deltat": "deltat",
+             "cp": "cp", "cs": "cs", "rho": rho, "f0": "f0", "t0": "t0", "factor": "factor",
+             "angle_force": "angle_force", "isource": "isource", "jsource": "jsource", "nrec": "nrec",
+             "use_pml_xmin": "use_pml_xmin", "use_pml_xmax": "use_pml_xmax",
+             "use_pml_ymin": "use_pml_ymin", "use_pml_ymax": "use_pml_ymax"}
+    if "p_npower" in fx:
+        pairs.update(npower="npower", k_max_pml="k_max_pml", alpha_max_pml="alpha_max_pml")
+    if three_d:
+        pairs.update(nz="nz", deltaz="deltaz", use_pml_zmin="use_pml_zmin", use_pml_zmax="use_pml_zmax")
+    for ours, theirs in pairs.items():
+        want = fx["p_" + theirs].item()
+        v = got[ours]
+        have = {".true.": 1, ".false.": 0}.get(v, None)
+        have = ast.literal_eval(v) if have is None else have
+        assert float(have) == float(want), (ours, v, want)
+    stf_name = {"ricker": "ricker", "gaussian": "gaussian", "program default": "derivative_of_gaussian"}
+    assert got["source_time_function"] == stf_name[str(fx["stf"])]
+    recs = [tuple(int(x) for x in ln.split("=")[1].split()) for ln in r.stdout.splitlines()
+            if "closest grid point found in i,j" in ln]
+    assert recs == [tuple(int(v) for v in rr) for rr in fx["rec"]]
+
+
+def test_fortran_parameter_file_errors(program, tmp_path):
+    """An expression naming something undefined, or a program whose
+    source_term lines are all commented out, stops with a message before
+    any device call."""
+    base = ("program p\n  implicit none\n  integer, parameter :: NX = 40, NY = 50\n"
+            "  double precision, parameter :: DELTAX = 10.d0, DELTAT = 1.d-3\n"
+            "  integer, parameter :: NSTEP = 10, NPOINTS_PML = 5, ISOURCE = NX / 2, JSOURCE = 2 * NY / 3\n"
+            "  double precision, parameter :: cp = 3000.d0, cs = cp / 1.732d0, density = 2000.d0\n"
+            "  double precision, parameter :: f0 = 10.d0, factor = 1.d7, ANGLE_FORCE = 0.d0\n")
+    src = tmp_path / "bad.f90"
+    src.write_text(base + "  double precision, parameter :: t0 = 1.2d0 / fzero\n"
+                   "  source_term = factor\nend program p\n")
+    r = subprocess.run([program, "2d", str(src), str(tmp_path), "--print-params"], capture_output=True,
+                       text=True)
+    assert r.returncode == 2 and "unknown name fzero" in r.stderr
+    src.write_text(base + "! source_term = factor\nend program p\n")
+    r = subprocess.run([program, "2d", str(src), str(tmp_path), "--print-params"], capture_output=True,
+                       text=True)
+    assert r.returncode == 2 and "one active source_term line, found 0" in r.stderr
+    src.write_text(base + "  source_term = factor * exp(-a*(t-t0)**2)\nend program p\n")
+    r = subprocess.run([program, "2d", str(src), str(tmp_path), "--print-params"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert "ISOURCE = 20" in r.stdout and "JSOURCE = 33" in r.stdout      # integer division
+    assert "SOURCE_TIME_FUNCTION = gaussian" in r.stdout
