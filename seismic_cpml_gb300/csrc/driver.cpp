@@ -1,7 +1,11 @@
 // driver.cpp -- cpml_program: the two reference programs as one C++ host
 // program over the C ABI.
 //
-// Usage:  cpml_program [2d|3d] [params.par | program.f90] [output_dir] [--print-params]
+// Usage:  cpml_program [2d|2d4|2dpml|3d] [params.par | program.f90] [output_dir] [--print-params]
+//
+// 2d4 and 2dpml run the fourth-order program and the classical split-field
+// PML program (seismic_CPML_2D_isotropic_fourth_order.f90,
+// seismic_PML_Collino_2D_isotropic.f90) with the same flow and outputs.
 //
 // The parameters come from a params.par file of "NAME = value" lines, or
 // from a reference program's own source file (.f90): its parameter block,
@@ -372,11 +376,16 @@ int read_fortran_params(const char* path, Setup& S, bool three_d) {
     if (get(k, &v)) *dst = (int)v;
   };
   cpml_params& p = S.p;
-  const char* need[] = {"nx", "ny", "deltax", "deltat", "nstep", "npoints_pml", "cp", "cs", "f0",
+  const char* need[] = {"nx", "ny", "deltat", "nstep", "npoints_pml", "cp", "cs", "f0",
                         "factor", "isource", "jsource", "angle_force"};
   for (const char* k : need)
     if (!sym.count(k)) { std::fprintf(stderr, "%s: no parameter %s\n", path, k); return 1; }
+  if (!sym.count("deltax") && !sym.count("h")) { std::fprintf(stderr, "%s: no parameter DELTAX or h\n", path); return 1; }
   geti("nx", &p.nx); geti("ny", &p.ny); geti("nstep", &p.nstep); geti("npoints_pml", &p.npoints_pml);
+  if (get("h", &p.deltax)) {     // the split-field program's one grid spacing (PML:100)
+    p.deltay = p.deltax;
+    S.given["DELTAX"] = S.given["DELTAY"] = true;
+  }
   get("deltax", &p.deltax); get("deltay", &p.deltay); get("deltat", &p.deltat);
   get("cp", &p.cp); get("cs", &p.cs); get("f0", &p.f0); get("t0", &p.t0); get("factor", &p.factor);
   if (!get("density", &p.rho)) get("rho", &p.rho);
@@ -418,6 +427,8 @@ void print_params(const Setup& S, bool three_d) {
   const char* faces[6] = {"USE_PML_XMIN", "USE_PML_XMAX", "USE_PML_YMIN", "USE_PML_YMAX",
                           "USE_PML_ZMIN", "USE_PML_ZMAX"};
   for (int q = 0; q < (three_d ? 6 : 4); ++q) std::printf("%s = %s\n", faces[q], p.use_pml[q] ? ".true." : ".false.");
+  std::printf("! program: %s\n", p.scheme == CPML_SCHEME_SPLIT ? "split-field PML (PML)"
+                                 : p.order == 4 ? "fourth order (2D4)" : three_d ? "3D" : "2D");
   std::printf("SOURCE_TIME_FUNCTION = %s\n", p.stf == CPML_STF_RICKER ? "ricker"
                                             : p.stf == CPML_STF_DGAUSSIAN ? "derivative_of_gaussian" : "gaussian");
   std::printf("NREC = %d\nXDEB = %.17g\nYDEB = %.17g\nXFIN = %.17g\nYFIN = %.17g\n", S.nrec, S.xdeb, S.ydeb,
@@ -478,9 +489,20 @@ int main(int argc_in, char** argv_in) {
   }
   const int argc = (int)args.size();
   char** argv = args.data();
-  const bool three_d = argc > 1 && std::strcmp(argv[1], "3d") == 0;
+  // 2d: seismic_CPML_2D_isotropic_second_order; 2d4: the fourth-order
+  // program; 2dpml: seismic_PML_Collino_2D_isotropic; 3d: the MPI program
+  const std::string mode = argc > 1 ? argv[1] : "2d";
+  if (mode != "2d" && mode != "3d" && mode != "2d4" && mode != "2dpml") {
+    std::fprintf(stderr, "usage: cpml_program [2d|2d4|2dpml|3d] [params.par | program.f90 | -] [output_dir] "
+                         "[--print-params]\n");
+    return 2;
+  }
+  const bool three_d = mode == "3d";
   Setup S;
-  if (three_d) cpml_params_default_3d(&S.p); else cpml_params_default_2d(&S.p);
+  if (three_d) cpml_params_default_3d(&S.p);
+  else if (mode == "2d4") cpml_params_default_2d_fourth(&S.p);
+  else if (mode == "2dpml") cpml_params_default_2d_split(&S.p);
+  else cpml_params_default_2d(&S.p);
   if (argc > 2 && std::strcmp(argv[2], "-") != 0) {
     const std::string path = argv[2];
     const bool f90 = path.size() > 4 && upper(path.substr(path.size() - 4)) == ".F90";

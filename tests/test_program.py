@@ -70,11 +70,36 @@ def test_program_2d_default_outputs(program, tmp_path, golden):
     assert '"../collino/energy.dat" us 1:4' in cmp_script and "compare_total_energy_semilog.eps" in cmp_script
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode, fixture, nstep, display", [("2d4", "ref2d_fourth", 4000, 200),
+                                                           ("2dpml", "ref2d_split", 2000, 100)])
+def test_program_other_2d_programs(program, tmp_path, golden, mode, fixture, nstep, display):
+    """The fourth-order and split-field PML programs as shipped, run by
+    cpml_program: seismogram files within FP32 parity of the FP64 fixtures
+    (equal to the reference's own outputs), energy.dat, snapshots."""
+    r = subprocess.run([program, mode, "-", str(tmp_path)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    g = golden(fixture)
+    for comp, key in (("Vx", "sisvx"), ("Vy", "sisvy")):
+        tr = np.stack([np.loadtxt(tmp_path / f"{comp}_file_{k:03d}.dat")[:, 1] for k in (1, 2)])
+        err = np.linalg.norm(tr - g[key]) / np.linalg.norm(g[key])
+        assert err < 1e-5, (comp, err)
+    e = np.loadtxt(tmp_path / "energy.dat")
+    assert e.shape == (nstep, 4)
+    tot = g["ek"] + g["ep"]
+    assert np.linalg.norm(e[:, 3] - tot) / np.linalg.norm(tot) < 1e-6
+    for it in (5, display, nstep):
+        assert (tmp_path / f"image{it:06d}_Vx.pnm").exists()
+
+
 # ---------------------------------------------------------------------------
 # the reference program's own source as the parameter file
 # ---------------------------------------------------------------------------
 REF_CASES = ["refpin_2d_shipped", "refpin_2d_small", "refpin_2d_profiles", "refpin_2d_plain",
+             "refpin_2d4_shipped", "refpin_2d4_small", "refpin_2d4_profiles",
+             "refpin_pml2d_shipped", "refpin_pml2d_small",
              "refpin_3d_2ranks", "refpin_3d_4ranks", "refpin_3d_profiles", "refpin_3d_plain_full"]
+MODE = {"cpml2d": "2d", "cpml2d4": "2d4", "pml2d": "2dpml", "cpml3d": "3d"}
 
 
 def edited_source(src, overrides, stf):
@@ -115,8 +140,8 @@ def test_reference_source_as_parameter_file(program, tmp_path, name):
     fx = dict(np.load(os.path.join(gold, name + ".npz")))
     src = tmp_path / "program.f90"
     src.write_text(edited_source(os.path.join(ref_f90c.DEFAULT_REF_DIR, M.PROGRAMS[prog]), overrides, stf))
-    three_d = prog == "cpml3d"
-    r = subprocess.run([program, "3d" if three_d else "2d", str(src), str(tmp_path), "--print-params"],
+    three_d, split = prog == "cpml3d", prog == "pml2d"
+    r = subprocess.run([program, MODE[prog], str(src), str(tmp_path), "--print-params"],
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     got = {}
@@ -124,13 +149,16 @@ def test_reference_source_as_parameter_file(program, tmp_path, name):
         if " = " in ln and not ln.startswith(" "):
             k, v = ln.split(" = ", 1)
             got[k.lower()] = v.strip()
-    rho = "rho" if three_d else "density"
+    rho = "rho" if three_d or split else "density"
     pairs = {"nx": "nx", "ny": "ny", "nstep": "nstep", "npoints_pml": "npoints_pml",
-             "it_display": "it_display", "deltax": "deltax", "deltay": "deltay", "deltat": "deltat",
+             "it_display": "it_display", "deltat": "deltat",
              "cp": "cp", "cs": "cs", "rho": rho, "f0": "f0", "t0": "t0", "factor": "factor",
-             "angle_force": "angle_force", "isource": "isource", "jsource": "jsource", "nrec": "nrec",
-             "use_pml_xmin": "use_pml_xmin", "use_pml_xmax": "use_pml_xmax",
-             "use_pml_ymin": "use_pml_ymin", "use_pml_ymax": "use_pml_ymax"}
+             "angle_force": "angle_force", "isource": "isource", "jsource": "jsource", "nrec": "nrec"}
+    if split:        # one grid spacing h, PML on every edge (PML:100)
+        pairs.update(deltax="h", deltay="h")
+    else:
+        pairs.update(deltax="deltax", deltay="deltay", use_pml_xmin="use_pml_xmin",
+                     use_pml_xmax="use_pml_xmax", use_pml_ymin="use_pml_ymin", use_pml_ymax="use_pml_ymax")
     if "p_npower" in fx:
         pairs.update(npower="npower", k_max_pml="k_max_pml", alpha_max_pml="alpha_max_pml")
     if three_d:
