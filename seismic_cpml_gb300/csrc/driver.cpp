@@ -435,12 +435,15 @@ void print_params(const Setup& S, bool three_d) {
               S.xfin, S.yfin);
 }
 
-void write_gnuplot(const std::string& dir, bool three_d, int nrec) {
+// split: the Collino program's scripts (PML:562-606), which name the energy
+// plot collino_total_energy_semilog.eps and write no plot_comparison
+void write_gnuplot(const std::string& dir, bool three_d, bool split, int nrec) {
   FILE* f = std::fopen((dir + "/plot_energy").c_str(), "w");
   if (f) {
     std::fprintf(f, " # set term x11\n set term postscript landscape monochrome dashed \"Helvetica\" 22\n\n"
                     " set xlabel \"Time (s)\"\n set ylabel \"Total energy\"\n\n set output \"%s\"\n set logscale y\n",
-                 three_d ? "CPML3D_total_energy_semilog.eps" : "cpml_total_energy_semilog.eps");
+                 three_d ? "CPML3D_total_energy_semilog.eps"
+                 : split ? "collino_total_energy_semilog.eps" : "cpml_total_energy_semilog.eps");
     if (three_d)
       std::fprintf(f, " plot \"energy.dat\" t 'Total energy' w l lc 1\n");
     else
@@ -449,7 +452,7 @@ void write_gnuplot(const std::string& dir, bool three_d, int nrec) {
     std::fprintf(f, " pause -1 \"Hit any key...\"\n\n");
     std::fclose(f);
   }
-  if (!three_d) {
+  if (!three_d && !split) {
     // energy of this run against the classical split-field PML run of the
     // Collino program in ../collino (2D:764-777)
     f = std::fopen((dir + "/plot_comparison").c_str(), "w");
@@ -594,7 +597,7 @@ int main(int argc_in, char** argv_in) {
     cpml_destroy(h);
     return 6;
   }
-  write_gnuplot(dir, three_d, S.nrec);
+  write_gnuplot(dir, three_d, mode == "2dpml", S.nrec);
   cpml_destroy(h);
   std::printf("\n End of the simulation\n\n");
   return 0;

@@ -90,6 +90,15 @@ def test_program_other_2d_programs(program, tmp_path, golden, mode, fixture, nst
     assert np.linalg.norm(e[:, 3] - tot) / np.linalg.norm(tot) < 1e-6
     for it in (5, display, nstep):
         assert (tmp_path / f"image{it:06d}_Vx.pnm").exists()
+    # each program's own scripts: the split-field program names its energy
+    # plot after Collino and writes no comparison script (PML:562-606)
+    energy_plot = (tmp_path / "plot_energy").read_text()
+    if mode == "2dpml":
+        assert "collino_total_energy_semilog.eps" in energy_plot
+        assert not (tmp_path / "plot_comparison").exists()
+    else:
+        assert "cpml_total_energy_semilog.eps" in energy_plot
+        assert (tmp_path / "plot_comparison").exists()
 
 
 # ---------------------------------------------------------------------------
