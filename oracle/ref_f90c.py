@@ -460,7 +460,6 @@ class Translator:
         self.tmp = 0
         self.ln = 0
         self.blocks: list[str] = []
-        self.uses_mpi = False
 
     # ---- constant evaluation (integer parameters size the arrays) --------
     def const_int(self, e):
@@ -852,7 +851,6 @@ class Translator:
             return
         elif name in MPI_CALLS:
             arity, target = MPI_CALLS[name], f"ref_{name}"
-            self.uses_mpi = True
         else:
             raise TranslateError(f"line {self.ln}: call of {name} is outside the subset")
         p = Parser(tokenize("(" + (m.group(2) or "") + ")", self.ln), self.ln)

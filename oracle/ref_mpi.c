@@ -37,6 +37,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/mman.h>
+#include <sys/prctl.h>
 #include <sys/wait.h>
 #include <time.h>
 #include <unistd.h>
@@ -331,6 +332,10 @@ int main(int argc, char** argv) {
       return 2;
     }
     if (p == 0) {
+      /* a rank never outlives the parent: killed from outside, the parent
+         cannot end the ranks waiting at the barrier itself */
+      prctl(PR_SET_PDEATHSIG, SIGKILL);
+      if (getppid() == 1) _exit(8);
       g_rank = r;
       ref_main();
       fflush(stdout);
