@@ -1186,9 +1186,13 @@ class Translator:
         dumps = self.out
         params, glob, cap_main = self.declarations()
         cap = max(cap, cap_main)
+        # the dumps are written at the end, and by a STOP too (the state the
+        # program stopped in: e.g. the step at which it blew up)
         src = [C_PRELUDE, f"const long ref_message_capacity = {cap}L;", *params, *sub_params,
                *glob, *sub_glob, "", *sub_funcs,
-               "void ref_main(void) {", *loads, *body, *dumps, "}", ""]
+               "static void ref_dump_all(void) {", *dumps, "}", "",
+               "void ref_main(void) {", "  ref_set_stop_hook(ref_dump_all);", *loads, *body,
+               "  ref_dump_all();", "}", ""]
         manifest = {}
         for name in dump:
             s = self.syms[name]
@@ -1206,6 +1210,7 @@ C_PRELUDE = r"""/* Generated from a reference Fortran program by oracle/ref_f90c
 #include <stdlib.h>
 
 void ref_stop(const char* msg, int line);
+void ref_set_stop_hook(void (*hook)(void));
 void ref_dump(const char* name, const void* data, size_t bytes);
 void ref_timer(int end);
 void ref_load(const char* name, void* data, size_t bytes);
@@ -1381,7 +1386,7 @@ class RefProgram:
     overrides: dict = field(default_factory=dict)
 
     def run(self, nprocs: int = 1, workdir: str | None = None, timeout: float = 900.0,
-            inputs: dict | None = None, files=()):
+            inputs: dict | None = None, files=(), allow_stop: bool = False):
         """Run the translated program on nprocs emulated MPI ranks; returns
         one {name: array} per rank (Fortran-ordered arrays, shaped by their
         declared bounds), plus `loop_seconds` when the program times a loop.
@@ -1389,7 +1394,9 @@ class RefProgram:
         is removed afterwards: its dump files and the files it opens go
         there. inputs maps the names the program loads to arrays, written
         in Fortran order; `files` names files it writes, returned as text
-        under out[0]["files"]."""
+        under out[0]["files"]. With allow_stop, a program that ends on a
+        STOP returns its dumps of that moment and the STOP message under
+        out[r]["stop"]; otherwise a STOP is an error."""
         import shutil
         import tempfile
         own = workdir is None
@@ -1404,7 +1411,8 @@ class RefProgram:
             proc = subprocess.run([os.path.abspath(self.exe), "-np", str(nprocs), "-o", workdir,
                                    "-i", indir, "-t", str(int(timeout))], capture_output=True,
                                   text=True, timeout=timeout + 30, cwd=workdir)
-            if proc.returncode != 0:
+            stopped = proc.returncode == 3 and allow_stop
+            if proc.returncode != 0 and not stopped:
                 raise RuntimeError(f"{os.path.basename(self.exe)} exited with {proc.returncode}: "
                                    f"{proc.stderr.strip()[-2000:]}")
             out = []
@@ -1417,6 +1425,10 @@ class RefProgram:
                 t = os.path.join(workdir, f"loop_seconds.{r}.bin")
                 if os.path.exists(t):
                     d["loop_seconds"] = float(np.fromfile(t, dtype="<f8")[0])
+                t = os.path.join(workdir, f"stop.{r}.txt")
+                if os.path.exists(t):
+                    with open(t) as f:
+                        d["stop"] = f.read().strip()
                 out.append(d)
             if files:
                 out[0]["files"] = {}

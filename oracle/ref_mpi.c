@@ -80,18 +80,31 @@ static size_t type_size(int t) {
   return 0;
 }
 
-void ref_stop(const char* msg, int line) {
-  fprintf(stderr, "rank %d: STOP at line %d: %s\n", g_rank, line, msg);
-  fflush(stderr);
-  _exit(3);
-}
-
 void ref_dump(const char* name, const void* data, size_t bytes) {
   char path[4096];
   snprintf(path, sizeof path, "%s/%s.%d.bin", g_outdir, name, g_rank);
   FILE* f = fopen(path, "wb");
   if (!f || fwrite(data, 1, bytes, f) != bytes) fail("cannot write a dump file");
   fclose(f);
+}
+
+/* STOP: the program's dumps of this moment (a hook the translated program
+   registers), stop.<rank>.txt with the message, exit status 3 */
+static void (*g_stop_hook)(void) = NULL;
+void ref_set_stop_hook(void (*hook)(void)) { g_stop_hook = hook; }
+
+void ref_stop(const char* msg, int line) {
+  if (g_stop_hook) g_stop_hook();
+  char path[4096];
+  snprintf(path, sizeof path, "%s/stop.%d.txt", g_outdir, g_rank);
+  FILE* f = fopen(path, "w");
+  if (f) {
+    fprintf(f, "line %d: %s\n", line, msg);
+    fclose(f);
+  }
+  fprintf(stderr, "rank %d: STOP at line %d: %s\n", g_rank, line, msg);
+  fflush(stderr);
+  _exit(3);
 }
 
 /* variables a test fills before the first statement: <indir>/<name>.bin,

@@ -74,7 +74,9 @@ FIELDS = {
 
 # name -> (program, overrides, source-time function or None for the
 #          program's active line, emulated ranks, keep full fields
-#          [, seed of a per-cell model read in after the material fill])
+#          [, options: "model" seed of a per-cell model read in after the
+#           material fill, "scale" of its lambda and mu, "stop": the run is
+#           expected to end on a STOP])
 CASES = {
     # the programs exactly as shipped
     "refpin_2d_shipped": ("cpml2d", {}, None, 1, False),
@@ -117,9 +119,16 @@ CASES = {
     # their averaging rules, 2D:560-562, 586, 627): a seeded layered model
     # with anomalies, read in after the programs' homogeneous fill
     "refpin_2d_het": ("cpml2d", {"NX": 61, "NY": 73, "NSTEP": 600, "DELTAT": "1.5d-3",
-                                 "ydeb": "500.d0", "yfin": "200.d0"}, "ricker", 1, True, 11),
+                                 "ydeb": "500.d0", "yfin": "200.d0"}, "ricker", 1, True, {"model": 11}),
     "refpin_2d4_het": ("cpml2d4", {"NX": 57, "NY": 65, "NSTEP": 800, "ydeb": "450.d0",
-                                   "yfin": "150.d0"}, None, 1, True, 12),
+                                   "yfin": "150.d0"}, None, 1, True, {"model": 12}),
+    # the blow-up stop (2D:716-726): a model 1.6x faster than the cp the
+    # Courant check sees (2D:513-516), so the run passes that check and then
+    # grows without bound; the program stops at the first display step
+    # (it = 5 or a multiple of IT_DISPLAY) where max |v| exceeds 1e25
+    "refpin_2d_blowup": ("cpml2d", {"NX": 51, "NY": 61, "NSTEP": 600, "IT_DISPLAY": 50,
+                                    "ydeb": "450.d0", "yfin": "150.d0"}, None, 1, False,
+                         {"model": 13, "scale": 2.56, "stop": True}),
     # 3D on 2 and 4 ranks: the z-slab exchanges of 3D:811-823 and 951-963 run
     "refpin_3d_2ranks": ("cpml3d", {"NX": 36, "NY": 40, "NZ": 40, "NPROC": 2, "NSTEP": 200,
                                     "ydeb": "300.d0", "yfin": "100.d0"}, None, 2, False),
@@ -156,7 +165,8 @@ def model_2d(nx, ny, seed):
 
 
 def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
-    prog, overrides, stf, nprocs, keep, *seed = CASES[name]
+    prog, overrides, stf, nprocs, keep, *opt = CASES[name]
+    opt = opt[0] if opt else {}
     src = os.path.join(ref_dir, PROGRAMS[prog])
     three_d = prog == "cpml3d"
     fields = FIELDS[prog]
@@ -165,11 +175,14 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
     outs += ["total_energy", "rank_cut_plane"] if three_d else ["total_energy_kinetic",
                                                                "total_energy_potential"]
     big = name.endswith("_full")
-    dump = outs + PARAMS[prog] + ([] if big else arrays)
+    stop = opt.get("stop", False)
+    dump = outs + PARAMS[prog] + ([] if big or stop else arrays) + (["it"] if stop else [])
     t0 = time.time()
     model, load_after, inputs = None, None, None
-    if seed:      # the model goes into the program's own arrays after its fill
-        model = model_2d(int(overrides["NX"]), int(overrides["NY"]), seed[0])
+    if "model" in opt:      # the model goes into the program's own arrays after its fill
+        model = model_2d(int(overrides["NX"]), int(overrides["NY"]), opt["model"])
+        if "scale" in opt:   # faster waves: lambda and mu scaled, rho kept
+            model = (model[0] * np.float32(opt["scale"]), model[1] * np.float32(opt["scale"]), model[2])
         load_after = (fill_end_line(src), ["lambda", "mu", "rho"])
         # the fourth-order program's arrays are (0:NX+1, 0:NY+1): its fill
         # leaves the halo cells at their static zero, which no update reads
@@ -177,9 +190,11 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
         inputs = {k: np.pad(m.T.astype(np.float64), pad) for k, m in zip(load_after[1], model)}
     exe = ref_f90c.build(src, name, overrides, dump, bounds=not big, stf=stf,
                          load_after=load_after)
-    ranks = exe.run(nprocs=nprocs, timeout=7200, inputs=inputs)
+    ranks = exe.run(nprocs=nprocs, timeout=7200, inputs=inputs, allow_stop=stop)
     cut = int(ranks[0]["rank_cut_plane"]) if three_d else 0
     d = ranks[cut]
+    if stop != ("stop" in d):
+        raise RuntimeError(f"{name}: the run {'did not stop' if stop else 'stopped: ' + d['stop']}")
     out = {"program": np.array(PROGRAMS[prog]), "stf": np.array(stf or "program default"),
            "nprocs": np.array(nprocs),
            "overrides": np.array(repr(sorted(overrides.items())))}
@@ -194,12 +209,14 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
             out[k] = tr
     if model is not None:
         out["lam"], out["mu"], out["rho"] = model
+    if stop:     # where the program stopped, and why
+        out["stop"], out["stop_it"] = np.array(d["stop"]), np.array(int(d["it"]))
     if three_d:
         out["energy"] = d["total_energy"]
     else:
         out["ek"] = d["total_energy_kinetic"]
         out["ep"] = d["total_energy_potential"]
-    if not big:
+    if not big and not stop:
         for fname, parts in fields.items():
             if three_d:   # local planes 1..NZ_LOCAL of every rank, in rank order
                 full = np.concatenate([r[parts[0]][:, :, 1:-1] for r in ranks], axis=2)

@@ -415,3 +415,23 @@ def test_pnm_writer_reproduces_reference(case, cpml_lib, tmp_path):
     bad = [k for k in range(3, len(ref)) if ours[k] != ref[k]]
     assert not bad, f"{len(bad)} pixels differ, first at record {bad[0]}: {ours[bad[0]]!r} vs {ref[bad[0]]!r}"
 
+
+
+def test_blow_up_stops_where_the_reference_stops():
+    """The stop rule (2D:716-726): a per-cell model 1.6x faster than the cp
+    of the Courant check runs unstable. The reference program stops at the
+    first display step (it = 5 or a multiple of IT_DISPLAY) where
+    max |v| > 1e25. The oracle's max |v| crosses the threshold at that same
+    step, and its traces equal the reference's up to it."""
+    fx = load("refpin_2d_blowup")
+    p, rec = params_of(fx)
+    m = model_of(fx)
+    stop = int(fx["stop_it"])
+    assert "blew up" in str(fx["stop"])
+    r = oracle_c.run(p, rec=rec, vmax=True, lam=m[0], mu=m[1], rho=m[2])
+    display = [it for it in range(1, p.nstep + 1) if it % p.it_display == 0 or it == 5]
+    first = next(it for it in display if r.vmax[it - 1] > 1e25)
+    assert first == stop
+    for k in ("sisvx", "sisvy"):
+        assert np.array_equal(getattr(r, k)[:, :stop], fx[k][:, :stop]), k
+    assert np.array_equal(r.ek[:stop], fx["ek"][:stop]) and np.array_equal(r.ep[:stop], fx["ep"][:stop])
