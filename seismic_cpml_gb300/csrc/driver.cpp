@@ -23,6 +23,7 @@
 // gnuplot scripts (2D:738-808, 3D:1247-1319). The reference's stop messages
 // are printed and the program exits non-zero where the reference stops.
 #include <cerrno>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -561,6 +562,7 @@ int main(int argc_in, char** argv_in) {
   int it = 0;
   const int use4[4] = {p.use_pml[0], p.use_pml[1], p.use_pml[2], p.use_pml[3]};
   std::vector<double> ek(p.nstep), ep(p.nstep);
+  const auto t_start = std::chrono::steady_clock::now();
   while (it < p.nstep) {
     int next = (it / p.it_display + 1) * p.it_display;
     if (it < 5) next = std::min(next, 5);
@@ -579,6 +581,25 @@ int main(int argc_in, char** argv_in) {
       std::printf(" Time step # %d out of %d\n Time: %g seconds\n Max norm velocity vector V (m/s) = %.15g\n"
                   " total energy = %.15g\n\n", it, p.nstep, (float)((it - 1) * p.deltat), vmax,
                   ek[it - 1] + ep[it - 1]);
+      if (three_d) {   // elapsed time, and its timestamp file (3D:1197-1228)
+        const double tcpu =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        const int itc = (int)tcpu, hh = itc / 3600, mm = (itc - 3600 * hh) / 60, ss = itc - 3600 * hh - 60 * mm;
+        char lines[512];
+        std::snprintf(lines, sizeof lines,
+                      " Elapsed time in seconds = %.15g\n Elapsed time in hh:mm:ss = %4d h %02d m %02d s\n"
+                      " Mean elapsed time per time step in seconds = %.15g\n", tcpu, hh, mm, ss, tcpu / it);
+        std::printf("%s\n", lines);
+        char name[64];
+        std::snprintf(name, sizeof name, "/timestamp%06d", it);
+        FILE* ts = std::fopen((dir + name).c_str(), "w");
+        if (ts) {
+          std::fprintf(ts, " Time step # %d\n Time: %g seconds\n Max norm velocity vector V (m/s) = %.15g\n"
+                           " Total energy = %.15g\n%s", it, (float)((it - 1) * p.deltat), vmax,
+                       ek[it - 1] + ep[it - 1], lines);
+          std::fclose(ts);
+        }
+      }
       const int k = three_d ? p.ksource : 1;
       for (int fld = 0; fld < 2; ++fld) {
         cpml_get_plane(h, fld == 0 ? CPML_FIELD_VX : CPML_FIELD_VY, 2, k, plane.data());

@@ -101,6 +101,29 @@ def test_program_other_2d_programs(program, tmp_path, golden, mode, fixture, nst
         assert (tmp_path / "plot_comparison").exists()
 
 
+@pytest.mark.gpu
+def test_program_3d_outputs(program, tmp_path):
+    """The 3D program on a small grid: progress and elapsed-time lines, a
+    timestamp file per display step (3D:1197-1228), snapshots of the cut
+    plane, 2-column energy.dat (3D:1255), vx and vy files but no vz ones,
+    which its gnuplot script names nonetheless (3D:1293-1296, 1330-1364)."""
+    par = tmp_path / "p.par"
+    par.write_text("NX = 40\nNY = 40\nNZ = 36\nNSTEP = 120\nIT_DISPLAY = 50\n"
+                   "YDEB = 300.d0\nYFIN = 100.d0\n")
+    r = subprocess.run([program, "3d", str(par), str(tmp_path)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Elapsed time in hh:mm:ss" in r.stdout
+    for it in (5, 50, 100):
+        ts = (tmp_path / f"timestamp{it:06d}").read_text()
+        assert f"Time step # {it}" in ts and "Mean elapsed time per time step" in ts
+        assert (tmp_path / f"image{it:06d}_Vx.pnm").exists()
+    e = np.loadtxt(tmp_path / "energy.dat")
+    assert e.shape == (120, 2) and np.isfinite(e).all() and e[:, 1].max() > 0
+    assert (tmp_path / "Vx_file_001.dat").exists() and (tmp_path / "Vy_file_002.dat").exists()
+    assert not (tmp_path / "Vz_file_001.dat").exists()
+    assert "Vz_file_001.dat" in (tmp_path / "plotgnu").read_text()
+
+
 # ---------------------------------------------------------------------------
 # the reference program's own source as the parameter file
 # ---------------------------------------------------------------------------
