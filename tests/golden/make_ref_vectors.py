@@ -72,6 +72,17 @@ FIELDS = {
                "szz": ["sigmazz"], "sxy": ["sigmaxy"], "sxz": ["sigmaxz"], "syz": ["sigmayz"]},
 }
 
+# the C-PML profiles (R1, 2D:283-465, 3D:399-667) per axis, in the order the
+# C ABI's cpml_pml_profile returns them; the split-field program's damping
+# profiles divided by two (PML:180-250)
+_PROF = ["d", "k", "alpha", "a", "b"]
+PROFILES = {
+    "cpml2d": {ax: [f"{q}_{ax}" for q in _PROF] + [f"{q}_{ax}_half" for q in _PROF] for ax in "xy"},
+    "cpml3d": {ax: [f"{q}_{ax}" for q in _PROF] + [f"{q}_{ax}_half" for q in _PROF] for ax in "xyz"},
+    "pml2d": {ax: [f"d{ax}_over_two", f"d{ax}_half_over_two"] for ax in "xy"},
+}
+PROFILES["cpml2d4"] = PROFILES["cpml2d"]
+
 # name -> (program, overrides, source-time function or None for the
 #          program's active line, emulated ranks, keep full fields
 #          [, options: "model" seed of a per-cell model read in after the
@@ -176,7 +187,9 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
                                                                "total_energy_potential"]
     big = name.endswith("_full")
     stop = opt.get("stop", False)
-    dump = outs + PARAMS[prog] + ([] if big or stop else arrays) + (["it"] if stop else [])
+    profiles = {} if big else PROFILES[prog]
+    dump = outs + PARAMS[prog] + ([] if big or stop else arrays) + (["it"] if stop else []) \
+        + [n for names in profiles.values() for n in names]
     t0 = time.time()
     model, load_after, inputs = None, None, None
     if "model" in opt:      # the model goes into the program's own arrays after its fill
@@ -207,6 +220,8 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
             out["sha_" + k] = np.array(digest(tr))
         else:
             out[k] = tr
+    for ax, names in profiles.items():
+        out["prof_" + ax] = np.stack([d[n] for n in names])
     if model is not None:
         out["lam"], out["mu"], out["rho"] = model
     if stop:     # where the program stopped, and why

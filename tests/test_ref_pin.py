@@ -435,3 +435,39 @@ def test_blow_up_stops_where_the_reference_stops():
     for k in ("sisvx", "sisvy"):
         assert np.array_equal(getattr(r, k)[:, :stop], fx[k][:, :stop]), k
     assert np.array_equal(r.ek[:stop], fx["ek"][:stop]) and np.array_equal(r.ep[:stop], fx["ep"][:stop])
+
+
+PROFILE_CASES = [n for n in SMALL + SHIPPED if n != "refpin_3d_plain_full"] + ["refpin_2d_blowup"]
+
+
+@pytest.mark.parametrize("name", PROFILE_CASES)
+def test_pml_profiles_reproduce_reference(name, cpml_lib):
+    """R1 at the C ABI: cpml_pml_profile (FP64 d, K, alpha, a, b at grid and
+    half points per axis, what the device tables are rounded from) against
+    the reference program's own profile arrays, bit for bit. For the
+    split-field program: its damping profiles divided by two.
+
+    One documented exception: the reference clamps alpha >= 0 along x only
+    (2D:383-384, 3D:514-515). On y and z, the half point past the last grid
+    point (j = NY, k = NZ, which lies outside the layer) keeps a negative
+    alpha, and the a_half and b_half computed from it. No loop of the
+    programs reads that entry (half-point arrays are read up to N - 1). Here
+    every axis is clamped, so at that one entry alpha_half is max(alpha, 0)."""
+    import ctypes
+    fx = load(name)
+    p, _ = params_of(fx)
+    dp = ctypes.POINTER(ctypes.c_double)
+    for axis, ax in enumerate("xyz"[:p.ndim]):
+        if "prof_" + ax not in fx:
+            continue
+        ref = fx["prof_" + ax]
+        n = ref.shape[1]
+        arrs = [np.zeros(n) for _ in range(10)]
+        assert cpml_lib.cpml_pml_profile(ctypes.byref(p), axis, n, *[a.ctypes.data_as(dp) for a in arrs]) == 0
+        ours = np.stack([arrs[0], arrs[5]]) if p.scheme == P.SCHEME_SPLIT else np.stack(arrs)
+        keep = np.ones(n, bool)
+        if p.scheme != P.SCHEME_SPLIT and ax != "x" and ref[7][-1] < 0:
+            assert ours[7][-1] == 0.0                # clamped here, not in the reference
+            keep[-1] = False
+        for q in range(ref.shape[0]):
+            assert np.array_equal(ours[q][keep], ref[q][keep]), (ax, q, np.abs(ours[q] - ref[q]).max())
