@@ -134,7 +134,10 @@ int cpml_params_default_2d_split(cpml_params* p);
    single-domain semantics: source and receivers on global plane k = NZ/2. */
 int cpml_params_default_3d(cpml_params* p);
 
-/* Courant number cp*dt*sqrt(sum 1/d^2) (2D:513, 3D:712) for velocity cp_max. */
+/* Courant number cp*dt*sqrt(sum 1/d^2) (2D:513, 3D:712) for velocity cp_max;
+   for CPML_SCHEME_SPLIT the split-field program's own one-dimensional number
+   cp*dt/h (seismic_PML_Collino_2D_isotropic.f90:304), which lets time steps
+   up to sqrt(2) beyond the 2D limit pass its check, as the program does. */
 double cpml_courant(const cpml_params* p, double cp_max);
 
 /* Nearest grid point to (x, y) metres by the reference's brute-force search:

@@ -116,6 +116,8 @@ int cpml_params_default_2d_split(cpml_params* p) {
 
 double cpml_courant(const cpml_params* p, double cp_max) {
   if (!p) return NAN;
+  // the split-field program checks a one-dimensional number (PML:304)
+  if (p->scheme == CPML_SCHEME_SPLIT) return cp_max * p->deltat / p->deltax;
   double s = 1.0 / (p->deltax * p->deltax) + 1.0 / (p->deltay * p->deltay);
   if (p->ndim == 3) s += 1.0 / (p->deltaz * p->deltaz);
   return cp_max * p->deltat * std::sqrt(s);

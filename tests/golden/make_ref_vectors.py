@@ -189,7 +189,7 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
     stop = opt.get("stop", False)
     profiles = {} if big else PROFILES[prog]
     dump = outs + PARAMS[prog] + ([] if big or stop else arrays) + (["it"] if stop else []) \
-        + [n for names in profiles.values() for n in names]
+        + [n for names in profiles.values() for n in names] + ([] if big else ["courant_number"])
     t0 = time.time()
     model, load_after, inputs = None, None, None
     if "model" in opt:      # the model goes into the program's own arrays after its fill
@@ -222,6 +222,8 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
             out[k] = tr
     for ax, names in profiles.items():
         out["prof_" + ax] = np.stack([d[n] for n in names])
+    if not big:
+        out["courant"] = np.array(d["courant_number"])
     if model is not None:
         out["lam"], out["mu"], out["rho"] = model
     if stop:     # where the program stopped, and why

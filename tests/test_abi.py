@@ -276,3 +276,17 @@ def test_pnm_writer_follows_the_colour_rules(lib, tmp_path):
     assert tuple(px[row(10), 15]) == (255, 157, 0)   # source cross at (15, 10)
     assert tuple(px[row(30), 5]) == (30, 180, 60)    # receiver square
     assert tuple(px[0, 0]) == (0, 0, 0)              # frame
+
+
+def test_split_program_courant_check_is_its_own(lib):
+    """The split-field program checks cp * DELTAT / h (PML:304): 0.9 passes
+    that check (its 2D number is 1.27) and goes on to the device, 1.1 stops."""
+    h = ctypes.c_void_p()
+    p = P.default_2d_split()
+    p.deltat = 0.9 * p.deltax / p.cp
+    st = lib.cpml_create(ctypes.byref(p), ctypes.byref(h))
+    assert st != -2
+    if st == 0:
+        lib.cpml_destroy(h)
+    p.deltat = 1.1 * p.deltax / p.cp
+    assert lib.cpml_create(ctypes.byref(p), ctypes.byref(h)) == -2

@@ -471,3 +471,17 @@ def test_pml_profiles_reproduce_reference(name, cpml_lib):
             keep[-1] = False
         for q in range(ref.shape[0]):
             assert np.array_equal(ours[q][keep], ref[q][keep]), (ax, q, np.abs(ours[q] - ref[q]).max())
+
+
+@pytest.mark.parametrize("name", PROFILE_CASES)
+def test_courant_number_reproduces_reference(name, cpml_lib):
+    """R4: cpml_courant equals the Courant number each program computes for
+    its check (2D:513, 2D4:514, 3D:712, PML:304: the split-field program's
+    is one-dimensional, cp * DELTAT / h), bit for bit."""
+    import ctypes
+    fx = load(name)
+    p, _ = params_of(fx)
+    cpml_lib.cpml_courant.restype = ctypes.c_double
+    cpml_lib.cpml_courant.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    assert cpml_lib.cpml_courant(ctypes.byref(p), p.cp) == fx["courant"].item()
+
