@@ -212,11 +212,16 @@ class FExpr {
     if (!eat("**")) return b;
     FVal e = pw();
     FVal r;
-    if (e.kind == 0) {             // repeated multiplication
+    if (e.kind == 0) {   // by multiplication, squaring (gfortran's lowering of x**n)
       const long long n = (long long)e.v;
+      unsigned long long m = n < 0 ? 0ull - (unsigned long long)n : (unsigned long long)n;
       r.kind = b.kind;
-      double acc = 1.0;
-      for (long long k = 0; k < (n < 0 ? -n : n); ++k) acc = (r.kind == 1) ? double(float(acc * b.v)) : acc * b.v;
+      auto mul = [&](double x, double y) { return r.kind == 1 ? double(float(x * y)) : x * y; };
+      double x = b.v, acc = (m & 1) ? x : 1.0;
+      while (m >>= 1) {
+        x = mul(x, x);
+        if (m & 1) acc = mul(acc, x);
+      }
       r.v = n < 0 ? 1.0 / acc : acc;
       return fnorm(r);
     }

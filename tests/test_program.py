@@ -212,7 +212,7 @@ def test_fortran_parameter_file_errors(program, tmp_path):
     """An expression naming something undefined, or a program whose
     source_term lines are all commented out, stops with a message before
     any device call."""
-    base = ("program p\n  implicit none\n  integer, parameter :: NX = 40, NY = 50\n"
+    base = ("program p\n  implicit none\n  integer, parameter :: NX = 2**5 + 8, NY = 50\n"
             "  double precision, parameter :: DELTAX = 10.d0, DELTAT = 1.d-3\n"
             "  integer, parameter :: NSTEP = 10, NPOINTS_PML = 5, ISOURCE = NX / 2, JSOURCE = 2 * NY / 3\n"
             "  double precision, parameter :: cp = 3000.d0, cs = cp / 1.732d0, density = 2000.d0\n"
@@ -231,5 +231,6 @@ def test_fortran_parameter_file_errors(program, tmp_path):
     r = subprocess.run([program, "2d", str(src), str(tmp_path), "--print-params"], capture_output=True,
                        text=True)
     assert r.returncode == 0, r.stderr
+    assert "NX = 40" in r.stdout                                           # 2**5 + 8
     assert "ISOURCE = 20" in r.stdout and "JSOURCE = 33" in r.stdout      # integer division
     assert "SOURCE_TIME_FUNCTION = gaussian" in r.stdout
