@@ -30,8 +30,9 @@ The supported subset is what the four programs on the path use:
     dummy arguments arrive by reference, and their arrays may have bounds
     that are dummy arguments (adjustable arrays). The output subroutines
     use WRITE (to a unit or a character variable, with literal strings and
-    Iw / Iw.m edits, or list-directed integers and strings), OPEN and
-    CLOSE.
+    Iw / Iw.m edits, or list-directed integers, reals and strings), OPEN
+    and CLOSE. List-directed spacing is the compiler's choice; reals are
+    written with the digits that read back to the same value.
 Anything outside the subset raises TranslateError with its line number, so
 nothing is dropped silently. In a main program, statements that only
 produce text (print, write, open, close, format) are skipped unless `io` is
@@ -1041,10 +1042,13 @@ class Translator:
                     code.append(f"ref_ld_s({json.dumps(e[1])});")
                 else:
                     c, t = self.scalar(e)
-                    if t != "i":
-                        raise TranslateError(f"line {self.ln}: list-directed output of non-integers "
+                    if t == "i":
+                        code.append(f"ref_ld_i({c});")
+                    elif t in ("r", "d"):   # written so that reading back gives the value exactly
+                        code.append(f"ref_ld_r((double)({c}), {1 if t == 'r' else 2});")
+                    else:
+                        raise TranslateError(f"line {self.ln}: list-directed output of logicals "
                                              "is outside the subset")
-                    code.append(f"ref_ld_i({c});")
         else:
             tok = tokenize(fmt, self.ln)
             if len(tok) != 1 or tok[0][0] != "str":
@@ -1218,6 +1222,7 @@ void ref_rec_begin(void);
 void ref_put_s(const char* s);
 void ref_put_i(long v, int w, int m);
 void ref_ld_i(long v);
+void ref_ld_r(double v, int kind);
 void ref_ld_s(const char* s);
 void ref_rec_internal(char* buf, int len);
 void ref_rec_unit(int unit);

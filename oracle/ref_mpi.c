@@ -155,6 +155,13 @@ void ref_ld_i(long v) {
   const int n = snprintf(b, sizeof b, "%12ld", v);
   rec_put(b, (size_t)n);
 }
+/* list-directed reals: 9 significant digits for single precision, 17 for
+   double, so that reading the text back gives the value exactly */
+void ref_ld_r(double v, int kind) {
+  char b[48];
+  const int n = snprintf(b, sizeof b, kind == 1 ? "  %.8E" : "  %.16E", v);
+  rec_put(b, (size_t)n);
+}
 void ref_ld_s(const char* s) {
   rec_put(" ", 1);
   ref_put_s(s);

@@ -17,6 +17,8 @@ Parameters are overridden as a user edits the `parameter` lines, and the
 source-time function is chosen among the program's three `source_term`
 lines. Nothing else in the programs changes.
 
+refpin_files.npz holds the seismogram files and energy.dat the 2D and 3D
+programs write themselves (their WRITE statements translated too).
 refpin_pnm.npz holds PNM snapshots from the programs' create_color_image
 subroutine (2D:861-999, the same in all four programs), run by a small
 driver of this project's own on planes given to it.
@@ -334,14 +336,44 @@ def generate_pnm(ref_dir: str, out_dir: str = HERE) -> str:
 PNM_PAR = ["IT", "ISRC", "JSRC", "NPML", "FIELD", "UXMIN", "UXMAX", "UYMIN", "UYMAX"]
 
 
+# ---------------------------------------------------------------------------
+# output files: the programs' seismogram files (write_seismograms, 2D:826-857)
+# and energy.dat (2D:741-746, 3D:1253-1257), written by the programs' own
+# WRITE statements; the runs of refpin_2d_small and refpin_3d_2ranks
+# ---------------------------------------------------------------------------
+FILE_CASES = {"d2": "refpin_2d_small", "d3": "refpin_3d_2ranks"}
+
+
+def generate_files(ref_dir: str, out_dir: str = HERE) -> str:
+    t0 = time.time()
+    out = {}
+    for key, case in FILE_CASES.items():
+        prog, overrides, stf, nprocs = CASES[case][:4]
+        src = os.path.join(ref_dir, PROGRAMS[prog])
+        exe = ref_f90c.build(src, "files_" + case, overrides, ["nrec"], stf=stf, io=True,
+                             subroutines=[(src, "write_seismograms")])
+        nrec = int(dict(np.load(os.path.join(HERE, case + ".npz")))["p_nrec"])
+        names = [f"{c}_file_{r:03d}.dat" for c in ("Vx", "Vy") for r in range(1, nrec + 1)]
+        names.append("energy.dat")
+        r = exe.run(nprocs=nprocs, files=names)
+        for n in names:
+            out[f"{key}__{n.replace('.', '_')}"] = np.frombuffer(r[0]["files"][n].encode(), np.uint8)
+    path = os.path.join(out_dir, "refpin_files.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote refpin_files in {time.time() - t0:.1f} s")
+    return path
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-dir", default=ref_f90c.DEFAULT_REF_DIR)
     ap.add_argument("names", nargs="*")
     a = ap.parse_args()
-    for n in a.names or list(CASES) + ["refpin_pnm"]:
+    for n in a.names or list(CASES) + ["refpin_pnm", "refpin_files"]:
         if n == "refpin_pnm":
             generate_pnm(a.ref_dir)
+        elif n == "refpin_files":
+            generate_files(a.ref_dir)
         else:
             generate(n, a.ref_dir)
 

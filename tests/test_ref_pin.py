@@ -290,6 +290,7 @@ program iotest
   write(12,"('no items ',i4,' after')")
   write(12,*) k, -3
   write(12,*) 'abc'
+  write(12,*) 1.5d0, 0.1
   close(12)
 end program iotest
 """
@@ -310,7 +311,11 @@ def test_translator_io(tmp_path):
     subprocess.run(["gcc", "-O2", "-std=gnu11", "-w", "-o", str(exe), str(tmp_path / "iotest.c"),
                     ref_f90c.MPI_RUNTIME, "-lm", "-lpthread"], check=True)
     out = ref_f90c.RefProgram(str(exe), manifest).run(files=["out042.txt"])[0]["files"]["out042.txt"]
-    assert out.splitlines() == ["  7 ** x -0042", "no items ", "          42          -3", " abc"]
+    lines = out.splitlines()
+    assert lines[:4] == ["  7 ** x -0042", "no items ", "          42          -3", " abc"]
+    # list-directed reals: digits enough to read the value back exactly
+    d, r = (float(v) for v in lines[4].split())
+    assert d == 1.5 and np.float32(r) == np.float32(0.1) and r != 0.1
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
@@ -485,3 +490,41 @@ def test_courant_number_reproduces_reference(name, cpml_lib):
     cpml_lib.cpml_courant.argtypes = [ctypes.c_void_p, ctypes.c_double]
     assert cpml_lib.cpml_courant(ctypes.byref(p), p.cp) == fx["courant"].item()
 
+
+
+@pytest.mark.parametrize("key, case", [("d2", "refpin_2d_small"), ("d3", "refpin_3d_2ranks")])
+def test_output_files_reproduce_reference(key, case, cpml_lib, tmp_path):
+    """The seismogram files and energy.dat (2D:826-857, 741-746;
+    3D:1253-1257): cpml_write_seismograms and cpml_write_energy, given the
+    reference run's own seismograms and energies, write the same files as
+    the programs' own WRITE statements. Same names, same lines, and every
+    number the same when read back: single precision for the time stamps,
+    the traces and the 2D energies, double for the 3D total energy. The
+    list-directed spacing is the compiler's choice and is not compared."""
+    import ctypes
+    files, fx = load("refpin_files"), load(case)
+    p, _ = params_of(fx)
+    nrec, nt = fx["sisvx"].shape
+    dp = ctypes.POINTER(ctypes.c_double)
+    vx, vy = np.ascontiguousarray(fx["sisvx"]), np.ascontiguousarray(fx["sisvy"])
+    d = str(tmp_path).encode()
+    assert cpml_lib.cpml_write_seismograms(d, vx.ctypes.data_as(dp), vy.ctypes.data_as(dp), None, nt,
+                                           nrec, ctypes.c_double(p.deltat)) == 0
+    if key == "d3":
+        ek, ep = np.ascontiguousarray(fx["energy"]), np.zeros(nt)
+    else:
+        ek, ep = np.ascontiguousarray(fx["ek"]), np.ascontiguousarray(fx["ep"])
+    assert cpml_lib.cpml_write_energy(d, ek.ctypes.data_as(dp), ep.ctypes.data_as(dp), nt,
+                                      ctypes.c_double(p.deltat), 2 if key == "d3" else 4) == 0
+    ref_names = sorted(k[len(key) + 2:] for k in files if k.startswith(key + "__"))
+    ours = sorted(f.name.replace(".", "_") for f in tmp_path.iterdir())
+    assert ours == ref_names
+    for n in ref_names:
+        ref = np.loadtxt(bytes(files[f"{key}__{n}"]).decode().splitlines(), ndmin=2)
+        got = np.loadtxt(tmp_path / n.replace("_dat", ".dat"), ndmin=2)
+        assert ref.shape == got.shape == (nt, ref.shape[1]), n
+        single = [0] if (key == "d3" and n == "energy_dat") else list(range(ref.shape[1]))
+        for c in range(ref.shape[1]):   # REAL(4) columns compared as the floats they hold
+            a, b = (ref[:, c].astype(np.float32), got[:, c].astype(np.float32)) if c in single \
+                else (ref[:, c], got[:, c])
+            assert np.array_equal(a, b), (n, c, np.abs(ref[:, c] - got[:, c]).max())
