@@ -1,7 +1,8 @@
 // driver.cpp -- cpml_program: the two reference programs as one C++ host
 // program over the C ABI.
 //
-// Usage:  cpml_program [2d|2d4|2dpml|3d] [params.par | program.f90] [output_dir] [--print-params]
+// Usage:  cpml_program [2d|2d4|2dpml|3d] [params.par | program.f90] [output_dir]
+//                      [--print-params | --scripts-only]
 //
 // 2d4 and 2dpml run the fourth-order program and the classical split-field
 // PML program (seismic_CPML_2D_isotropic_fourth_order.f90,
@@ -453,7 +454,8 @@ void write_gnuplot(const std::string& dir, bool three_d, bool split, int nrec) {
     if (three_d)
       std::fprintf(f, " plot \"energy.dat\" t 'Total energy' w l lc 1\n");
     else
-      std::fprintf(f, " plot \"energy.dat\" us 1:2 t 'Ec' w l lc 1, \"energy.dat\" us 1:3 t 'Ep' w l lc 3, "
+      // two blanks where the programs continue the string literal (2D:759-760)
+      std::fprintf(f, " plot \"energy.dat\" us 1:2 t 'Ec' w l lc 1, \"energy.dat\" us 1:3  t 'Ep' w l lc 3, "
                       "\"energy.dat\" us 1:4 t 'Total energy' w l lc 4\n");
     std::fprintf(f, " pause -1 \"Hit any key...\"\n\n");
     std::fclose(f);
@@ -466,7 +468,7 @@ void write_gnuplot(const std::string& dir, bool three_d, bool split, int nrec) {
       std::fprintf(f, " # set term x11\n set term postscript landscape monochrome dashed \"Helvetica\" 22\n\n"
                       " set xlabel \"Time (s)\"\n set ylabel \"Total energy\"\n\n"
                       " set output \"compare_total_energy_semilog.eps\"\n set logscale y\n"
-                      " plot \"energy.dat\" us 1:4 t 'Total energy CPML' w l lc 1, "
+                      " plot \"energy.dat\" us 1:4 t 'Total energy CPML' w l lc 1,  "
                       "\"../collino/energy.dat\" us 1:4 t 'Total energy Collino' w l lc 2\n"
                       " pause -1 \"Hit any key...\"\n\n");
       std::fclose(f);
@@ -476,8 +478,11 @@ void write_gnuplot(const std::string& dir, bool three_d, bool split, int nrec) {
   if (f) {
     std::fprintf(f, " set term x11\n # set term postscript landscape monochrome dashed \"Helvetica\" 22\n\n"
                     " set xlabel \"Time (s)\"\n set ylabel \"Amplitude (m / s)\"\n\n");
+    // the programs plot receivers 1 and 2, written out, whatever NREC is
+    // (2D:784-806, 3D:1273-1310); 3D adds Vz files it never writes (3D:1293-1296)
+    (void)nrec;
     const char* comps[3] = {"Vx", "Vy", "Vz"};
-    for (int r = 1; r <= nrec; ++r)
+    for (int r = 1; r <= 2; ++r)
       for (int c = 0; c < (three_d ? 3 : 2); ++c)
         std::fprintf(f, " set output \"v_sigma_%s_receiver_%03d.eps\"\n plot \"%s_file_%03d.dat\" t '%s C-PML' w l lc 1\n"
                         " pause -1 \"Hit any key...\"\n\n", comps[c], r, comps[c], r, comps[c]);
@@ -490,10 +495,12 @@ void write_gnuplot(const std::string& dir, bool three_d, bool split, int nrec) {
 int main(int argc_in, char** argv_in) {
   // --print-params: print the resolved parameter block (params.par format)
   // and the receiver points, then stop before any device call
-  bool print_only = false;
+  // --scripts-only: write the gnuplot scripts of the resolved run and stop
+  bool print_only = false, scripts_only = false;
   std::vector<char*> args;
   for (int a = 0; a < argc_in; ++a) {
     if (std::strcmp(argv_in[a], "--print-params") == 0) print_only = true;
+    else if (std::strcmp(argv_in[a], "--scripts-only") == 0) scripts_only = true;
     else args.push_back(argv_in[a]);
   }
   const int argc = (int)args.size();
@@ -551,6 +558,10 @@ int main(int argc_in, char** argv_in) {
   std::printf(" Courant number is %.15g\n\n", cpml_courant(&p, p.cp));
   if (print_only) {
     print_params(S, three_d);
+    return 0;
+  }
+  if (scripts_only) {
+    write_gnuplot(dir, three_d, mode == "2dpml", S.nrec);
     return 0;
   }
 

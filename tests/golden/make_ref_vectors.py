@@ -17,8 +17,9 @@ Parameters are overridden as a user edits the `parameter` lines, and the
 source-time function is chosen among the program's three `source_term`
 lines. Nothing else in the programs changes.
 
-refpin_files.npz holds the seismogram files and energy.dat the 2D and 3D
-programs write themselves (their WRITE statements translated too).
+refpin_files.npz holds the seismogram files, energy.dat and the gnuplot
+scripts the four programs write themselves (their WRITE statements
+translated too).
 refpin_pnm.npz holds PNM snapshots from the programs' create_color_image
 subroutine (2D:861-999, the same in all four programs), run by a small
 driver of this project's own on planes given to it.
@@ -341,7 +342,12 @@ PNM_PAR = ["IT", "ISRC", "JSRC", "NPML", "FIELD", "UXMIN", "UXMAX", "UYMIN", "UY
 # and energy.dat (2D:741-746, 3D:1253-1257), written by the programs' own
 # WRITE statements; the runs of refpin_2d_small and refpin_3d_2ranks
 # ---------------------------------------------------------------------------
-FILE_CASES = {"d2": "refpin_2d_small", "d3": "refpin_3d_2ranks"}
+FILE_CASES = {"d2": "refpin_2d_small", "d3": "refpin_3d_2ranks", "d24": "refpin_2d4_small",
+              "dpml": "refpin_pml2d_small"}
+# the gnuplot scripts each program writes (2D:748-808, 3D:1258-1312, PML:560-606)
+SCRIPTS = {"cpml2d": ["plot_energy", "plot_comparison", "plotgnu"],
+           "cpml2d4": ["plot_energy", "plot_comparison", "plotgnu"],
+           "cpml3d": ["plot_energy", "plotgnu"], "pml2d": ["plot_energy", "plotgnu"]}
 
 
 def generate_files(ref_dir: str, out_dir: str = HERE) -> str:
@@ -354,7 +360,7 @@ def generate_files(ref_dir: str, out_dir: str = HERE) -> str:
                              subroutines=[(src, "write_seismograms")])
         nrec = int(dict(np.load(os.path.join(HERE, case + ".npz")))["p_nrec"])
         names = [f"{c}_file_{r:03d}.dat" for c in ("Vx", "Vy") for r in range(1, nrec + 1)]
-        names.append("energy.dat")
+        names += ["energy.dat"] + SCRIPTS[prog]
         r = exe.run(nprocs=nprocs, files=names)
         for n in names:
             out[f"{key}__{n.replace('.', '_')}"] = np.frombuffer(r[0]["files"][n].encode(), np.uint8)

@@ -234,3 +234,40 @@ def test_fortran_parameter_file_errors(program, tmp_path):
     assert "NX = 40" in r.stdout                                           # 2**5 + 8
     assert "ISOURCE = 20" in r.stdout and "JSOURCE = 33" in r.stdout      # integer division
     assert "SOURCE_TIME_FUNCTION = gaussian" in r.stdout
+
+
+SCRIPT_CASES = {"refpin_2d_small": "d2", "refpin_3d_2ranks": "d3", "refpin_2d4_small": "d24",
+                "refpin_pml2d_small": "dpml"}
+
+
+@pytest.mark.parametrize("name", list(SCRIPT_CASES))
+def test_gnuplot_scripts_reproduce_reference(program, tmp_path, name):
+    """The gnuplot scripts cpml_program writes equal the ones each program
+    writes itself (translated with its WRITE statements; refpin_files.npz),
+    line for line. Only the leading blank of a list-directed record, the
+    compiler's choice, is not compared."""
+    import os
+    import sys
+    from oracle import ref_f90c
+    if not os.path.isdir(ref_f90c.DEFAULT_REF_DIR):
+        pytest.skip("needs the reference sources")
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, gold)
+    import make_ref_vectors as M
+    prog, overrides, stf = M.CASES[name][:3]
+    src = tmp_path / "program.f90"
+    src.write_text(edited_source(os.path.join(ref_f90c.DEFAULT_REF_DIR, M.PROGRAMS[prog]), overrides, stf))
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([program, MODE[prog], str(src), str(out), "--scripts-only"], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    files = dict(np.load(os.path.join(gold, "refpin_files.npz")))
+    key = SCRIPT_CASES[name]
+    norm = lambda t: [ln[1:].rstrip() if ln.startswith(" ") else ln.rstrip() for ln in t.splitlines()]  # noqa: E731
+    for script in M.SCRIPTS[prog]:
+        ref = norm(bytes(files[f"{key}__{script}"]).decode())
+        ours = norm((out / script).read_text())
+        assert ours == ref, (script, [(a, b) for a, b in zip(ours, ref) if a != b][:3], len(ours), len(ref))
+    extra = {f.name for f in out.iterdir()} - set(M.SCRIPTS[prog])
+    assert not extra, extra
