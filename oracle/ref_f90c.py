@@ -1020,7 +1020,9 @@ class Translator:
         keyed = {}
         for k, x in enumerate(parts):
             m = re.match(r"(\w+)\s*=(?!=)\s*(.*)$", x)
-            keyed[m.group(1) if m else ("unit", "fmt")[min(k, 1)]] = m.group(2) if m else x
+            if not m and k > 1:
+                raise TranslateError(f"line {self.ln}: {kw.upper()} with more than two positional items")
+            keyed[m.group(1) if m else ("unit", "fmt")[k]] = m.group(2) if m else x
         if kw == "close":
             self.emit(f"ref_close({self.scalar(parse_expr(keyed['unit'], self.ln))[0]});")
             return
