@@ -528,3 +528,53 @@ def test_output_files_reproduce_reference(key, case, cpml_lib, tmp_path):
             a, b = (ref[:, c].astype(np.float32), got[:, c].astype(np.float32)) if c in single \
                 else (ref[:, c], got[:, c])
             assert np.array_equal(a, b), (n, c, np.abs(ref[:, c] - got[:, c]).max())
+
+
+@pytest.mark.parametrize("fn, name", [("cpml_params_default_2d", "refpin_2d_shipped"),
+                                      ("cpml_params_default_2d_fourth", "refpin_2d4_shipped"),
+                                      ("cpml_params_default_2d_split", "refpin_pml2d_shipped")])
+def test_default_parameter_blocks_are_the_shipped_programs(fn, name, cpml_lib):
+    """The C ABI's default parameter blocks are the shipped programs' own
+    (2D:138-218, 2D4:132-190, PML:96-141): every value equals what the
+    program evaluated when run as shipped."""
+    import ctypes
+    q = P.CpmlParams()
+    assert getattr(cpml_lib, fn)(ctypes.byref(q)) == 0
+    p, _ = params_of(load(name))
+    for f, _t in P.CpmlParams._fields_:
+        if f.startswith("reserved") or f in ("flags", "ksource", "nz", "deltaz"):
+            continue
+        a, b = getattr(q, f), getattr(p, f)
+        if f == "use_pml":
+            a, b = list(a)[:4], list(b)[:4]
+        assert a == b, (f, a, b)
+
+
+def test_default_3d_block_is_the_shipped_program(cpml_lib, tmp_path):
+    """cpml_params_default_3d against the shipped 3D program's parameter
+    block (3D:124-218) as cpml_program evaluates it from the source (that
+    evaluator is pinned against the program's own evaluation above), with
+    the source and receivers on the cut plane NZ/2."""
+    import ctypes
+    from seismic_cpml_gb300.build import PROGRAM, build
+    if not os.path.isdir(REF_DIR):
+        pytest.skip("needs the reference sources")
+    build()
+    src = os.path.join(REF_DIR, ref_f90c.REFERENCE_PROGRAMS["cpml3d"])
+    r = subprocess.run([PROGRAM, "3d", src, str(tmp_path), "--print-params"], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    got = dict(ln.split(" = ", 1) for ln in r.stdout.splitlines() if " = " in ln and not ln.startswith((" ", "!")))
+    q = P.CpmlParams()
+    assert cpml_lib.cpml_params_default_3d(ctypes.byref(q)) == 0
+    amax = 2.0 * math.pi * (q.f0 / 2.0) if q.alpha_max_pml < 0 else q.alpha_max_pml
+    want = {"NX": q.nx, "NY": q.ny, "NZ": q.nz, "NSTEP": q.nstep, "NPOINTS_PML": q.npoints_pml,
+            "IT_DISPLAY": q.it_display, "DELTAX": q.deltax, "DELTAY": q.deltay, "DELTAZ": q.deltaz,
+            "DELTAT": q.deltat, "cp": q.cp, "cs": q.cs, "rho": q.rho, "f0": q.f0, "t0": q.t0,
+            "factor": q.factor, "ANGLE_FORCE": q.angle_force, "ISOURCE": q.isource,
+            "JSOURCE": q.jsource, "KSOURCE": q.ksource, "NPOWER": q.npower, "K_MAX_PML": q.k_max_pml,
+            "ALPHA_MAX_PML": amax, "RCOEF": q.rcoef}
+    for k, v in want.items():
+        assert float(got[k]) == float(v), (k, got[k], v)
+    for k, face in zip(["XMIN", "XMAX", "YMIN", "YMAX", "ZMIN", "ZMAX"], q.use_pml):
+        assert got["USE_PML_" + k] == (".true." if face else ".false."), k
