@@ -136,6 +136,12 @@ CASES = {
                                  "ydeb": "500.d0", "yfin": "200.d0"}, "ricker", 1, True, {"model": 11}),
     "refpin_2d4_het": ("cpml2d4", {"NX": 57, "NY": 65, "NSTEP": 800, "ydeb": "450.d0",
                                    "yfin": "150.d0"}, None, 1, True, {"model": 12}),
+    # the receiver rule (2D:483-509): 41 targets on half-cell positions,
+    # equidistant from two or four grid points, where the strict < keeps the
+    # first minimum in the program's scan order (j outer, i inner)
+    "refpin_2d_receivers": ("cpml2d", {"NX": 41, "NY": 31, "NSTEP": 5, "NREC": 41,
+                                       "xdeb": "5.d0", "xfin": "405.d0", "ydeb": "5.d0",
+                                       "yfin": "305.d0"}, None, 1, False),
     # the blow-up stop (2D:716-726): a model 1.6x faster than the cp the
     # Courant check sees (2D:513-516), so the run passes that check and then
     # grows without bound; the program stops at the first display step
@@ -192,7 +198,8 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
     stop = opt.get("stop", False)
     profiles = {} if big else PROFILES[prog]
     dump = outs + PARAMS[prog] + ([] if big or stop else arrays) + (["it"] if stop else []) \
-        + [n for names in profiles.values() for n in names] + ([] if big else ["courant_number"])
+        + [n for names in profiles.values() for n in names] \
+        + ([] if big else ["courant_number", "xrec", "yrec"])
     t0 = time.time()
     model, load_after, inputs = None, None, None
     if "model" in opt:      # the model goes into the program's own arrays after its fill
@@ -227,6 +234,7 @@ def generate(name: str, ref_dir: str, out_dir: str = HERE) -> str:
         out["prof_" + ax] = np.stack([d[n] for n in names])
     if not big:
         out["courant"] = np.array(d["courant_number"])
+        out["rec_xy"] = np.stack([d["xrec"], d["yrec"]], axis=1)   # the targets, in metres
     if model is not None:
         out["lam"], out["mu"], out["rho"] = model
     if stop:     # where the program stopped, and why

@@ -578,3 +578,24 @@ def test_default_3d_block_is_the_shipped_program(cpml_lib, tmp_path):
         assert float(got[k]) == float(v), (k, got[k], v)
     for k, face in zip(["XMIN", "XMAX", "YMIN", "YMAX", "ZMIN", "ZMAX"], q.use_pml):
         assert got["USE_PML_" + k] == (".true." if face else ".false."), k
+
+
+RECEIVER_CASES = PROFILE_CASES + ["refpin_2d_receivers"]
+
+
+@pytest.mark.parametrize("name", RECEIVER_CASES)
+def test_nearest_gridpoint_reproduces_reference(name, cpml_lib):
+    """R3: cpml_nearest_gridpoint, given each program's receiver targets in
+    metres, returns the grid points the program chose (2D:483-509,
+    3D:683-706), ties included: refpin_2d_receivers puts 41 targets on
+    half-cell positions, where the strict < keeps the first minimum."""
+    import ctypes
+    fx = load(name)
+    p, _ = params_of(fx)
+    i, j = ctypes.c_int(), ctypes.c_int()
+    for (x, y), (ri, rj) in zip(fx["rec_xy"], fx["rec"]):
+        assert cpml_lib.cpml_nearest_gridpoint(p.nx, p.ny, ctypes.c_double(p.deltax),
+                                               ctypes.c_double(p.deltay), ctypes.c_double(x),
+                                               ctypes.c_double(y), ctypes.byref(i), ctypes.byref(j)) == 0
+        assert (i.value, j.value) == (int(ri), int(rj)), (x, y)
+
