@@ -599,3 +599,70 @@ def test_nearest_gridpoint_reproduces_reference(name, cpml_lib):
                                                ctypes.c_double(y), ctypes.byref(i), ctypes.byref(j)) == 0
         assert (i.value, j.value) == (int(ri), int(rj)), (x, y)
 
+
+
+SEMANTICS_TEST = """\
+program semantics
+  implicit none
+  real :: x, y
+  double precision :: d, e
+  double precision, dimension(-2:3) :: a
+  integer :: i, n1, n2, n3, n4, m1, m2, trips, mx, mn
+  logical :: p, q, r
+  x = 0.1
+  y = x * 3.0 + 1.0e-3
+  d = x * 3.0d0
+  e = 0.1d0 * 3.0d0
+  n1 = nint(2.5d0)
+  n2 = nint(-2.5d0)
+  n3 = nint(0.49999997)
+  n4 = int(-3.7d0)
+  m1 = mod(-7, 3)
+  m2 = mod(7, -3)
+  mx = max(3, -1, 8, 2)
+  mn = min(3, -1, 8, 2)
+  trips = 0
+  do i = 5, 4
+    trips = trips + 1
+  enddo
+  a(:) = 0.d0
+  a(-1:1) = 2.d0
+  a(3) = sum(a(-2:2)) / 4.d0
+  p = .true.
+  q = (n1 == 3) .eqv. (n2 == -3)
+  r = p .neqv. q
+  if (q) then
+    if (.not. r) n4 = n4 * 10
+  endif
+end program semantics
+"""
+
+
+def test_translator_arithmetic_semantics(tmp_path):
+    """Fortran's rules as the translation keeps them: single-precision
+    arithmetic rounds every operation to float, mixed kinds promote to
+    double, NINT rounds halves away from zero, INT and MOD truncate, a DO
+    loop whose range is empty runs no trip, sections keep declared lower
+    bounds, .EQV./.NEQV. compare logicals."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "semantics.f90"
+    src.write_text(SEMANTICS_TEST)
+    names = ["x", "y", "d", "e", "a", "n1", "n2", "n3", "n4", "m1", "m2", "mx", "mn", "trips", "q", "r"]
+    code, manifest = ref_f90c.translate_file(str(src), dump=names)
+    (tmp_path / "s.c").write_text(code)
+    exe = tmp_path / "s"
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-w", "-o", str(exe), str(tmp_path / "s.c"),
+                    ref_f90c.MPI_RUNTIME, "-lm", "-lpthread"], check=True)
+    v = ref_f90c.RefProgram(str(exe), manifest).run()[0]
+    f = np.float32
+    assert v["x"] == f(0.1)
+    assert v["y"] == f(f(f(0.1) * f(3.0)) + f(1.0e-3))         # every step rounded to float
+    assert v["d"] == float(f(0.1)) * 3.0 and v["d"] != 0.1 * 3.0  # the float 0.1, promoted
+    assert v["e"] == 0.1 * 3.0
+    assert (int(v["n1"]), int(v["n2"]), int(v["n3"])) == (3, -3, 0)
+    assert (int(v["m1"]), int(v["m2"])) == (-1, 1)              # sign of the first operand
+    assert (int(v["mx"]), int(v["mn"]), int(v["trips"])) == (8, -1, 0)
+    assert v["a"].tolist() == [0.0, 2.0, 2.0, 2.0, 0.0, 1.5]   # a(-2..3)
+    assert int(v["q"]) == 1 and int(v["r"]) == 0
+    assert int(v["n4"]) == -30                                  # INT truncates; nested IF taken
