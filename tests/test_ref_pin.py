@@ -122,7 +122,9 @@ def test_oracle_reproduces_reference(name):
 
 
 @pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_2d4_small", "refpin_pml2d_small",
-                                  "refpin_3d_2ranks", "refpin_2d_het"])
+                                  "refpin_3d_2ranks", "refpin_3d_4ranks", "refpin_2d_het",
+                                  "refpin_2d4_het", "refpin_2d_profiles", "refpin_2d4_profiles",
+                                  "refpin_3d_profiles"])
 def test_numpy_restatement_reproduces_reference(name):
     fx = load(name)
     p, rec = params_of(fx)
