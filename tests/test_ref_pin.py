@@ -332,9 +332,28 @@ def test_pnm_vectors_regenerate_from_reference_source(tmp_path):
         assert np.array_equal(a[k], b[k]), k
 
 
+def _regenerable():
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_ref_vectors as M
+    return [n for n in M.CASES if not n.endswith("_full")]
+
+
 @pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
                     reason="needs the reference sources and gcc")
-@pytest.mark.parametrize("name", ["refpin_2d_small", "refpin_3d_4ranks"])
+def test_file_vectors_regenerate_from_reference_source(tmp_path):
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_ref_vectors as M
+    a, b = dict(np.load(M.generate_files(REF_DIR, str(tmp_path)))), load("refpin_files")
+    assert sorted(a) == sorted(b)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_DIR) or shutil.which("gcc") is None,
+                    reason="needs the reference sources and gcc")
+@pytest.mark.parametrize("name", _regenerable())
 def test_vectors_regenerate_from_reference_source(name, tmp_path):
     import sys
     sys.path.insert(0, GOLD)
